@@ -1,0 +1,429 @@
+"""Benchmark of the voxel step on GB300.
+
+Headline workload (one "step" = one 64-step segment of the batched pool):
+2048 independent worlds, dims iid from {16,24,32,48,64,96,128}^3 (seeded),
+stepped together by the bit-plane step kernel inside one CUDA graph per
+segment.  The same line carries:
+  * plain_per_world: the drop-in byte kernel launched once per world per step
+    (2048 x 64 launches per segment) on the same worlds;
+  * plain_512: the drop-in byte kernel on one 512^3 pillar world (HBM-bound);
+  * roofline of the dominant kernel (CUDA-event time per launch);
+  * cpu_baseline: the CPU oracle timed on this host (bounded sample);
+  * e2e: the same metric through the C ABI from pinned host buffers
+    (admit = H2D + conversion, one segment, retire = conversion + D2H).
+`--impl reference` times the CPU oracle (the upstream project has no step of
+its own) on a bounded sample of the same workload with all host threads.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fs3d|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import re
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-updates/s: batched+served vs plain per-world launch, 1 GB300, bit-exact"
+UNIT = "voxel-updates/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def baseline_metric():
+    try:
+        with open(os.path.join(ROOT, "BASELINE.json")) as f:
+            return json.load(f).get("metric", METRIC)
+    except OSError:
+        return METRIC
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ workload
+def batch_worlds(fs3d, master: int, count: int):
+    dims, seeds = fs3d.gen_batch_dims(master, count)
+    return [(tuple(int(v) for v in dims[w]), int(seeds[w])) for w in range(count)]
+
+
+def gen_grids(fs3d, worlds, pinned_torch=None):
+    """Host grids (pinned when torch is given), generated in parallel."""
+    def one(w):
+        (X, Y, Z), seed = w
+        return fs3d.gen_batch_world(seed, X, Y, Z)
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        grids = list(ex.map(one, worlds))
+    if pinned_torch is not None:
+        out = []
+        for g in grids:
+            t = pinned_torch.empty(g.shape, dtype=pinned_torch.uint8, pin_memory=True)
+            t.numpy()[...] = g
+            out.append(t)
+        return out
+    return grids
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """Per-launch DRAM bytes recorded from an ncu capture under profiles/."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None, None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    c = re.search(r"traffic_cells_per_launch:\s*([0-9.eE+]+)", txt)
+    if not m:
+        return None, None
+    return float(m.group(1)), (float(c.group(1)) if c else None)
+
+
+# ------------------------------------------------------------------ CPU oracle timing
+def cpu_sample(worlds, budget_s: float, threads: int):
+    """Times the oracle step on a bounded sample of the batch workload: worlds
+    are stepped concurrently (one thread each) until ~budget_s has passed."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    orc = oracle_lib.load()
+    import fallingsand3d_gb300 as fs3d
+    sample = worlds[: max(threads * 4, 64)]
+    grids = gen_grids(fs3d, sample)
+    cells = [g.size for g in grids]
+    steps_each = 4
+
+    def run(i):
+        (X, Y, Z), seed = sample[i]
+        orc.L.orc_run(grids[i].ctypes.data, X, Y, Z, seed, 0, steps_each, None, 1)
+        return cells[i] * steps_each
+
+    done = 0
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        rounds = 0
+        while True:
+            done += sum(ex.map(run, range(len(sample))))
+            rounds += 1
+            if time.perf_counter() - t0 > budget_s or rounds >= 50:
+                break
+    dt = time.perf_counter() - t0
+    return done / dt, {"worlds": len(sample), "steps_per_round": steps_each, "rounds": rounds,
+                       "voxel_updates": done, "seconds": round(dt, 3)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import fallingsand3d_gb300 as fs3d
+    threads = os.cpu_count() or 1
+    worlds = batch_worlds(fs3d, args.master, args.worlds)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(worlds, 1.0, threads)
+    for _ in range(args.steps):
+        v, info = cpu_sample(worlds, args.cpu_budget / max(args.steps, 1), threads)
+        vals.append(v)
+    v = float(np.mean(vals))
+    line = {"metric": baseline_metric(), "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"batched: {args.worlds} mixed worlds (bounded CPU sample)",
+                       "master_seed": args.master},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{info['worlds']} of the {args.worlds} worlds, {info['steps_per_round']} "
+                                       f"steps per round, one world per thread; the upstream project has no step "
+                                       f"of its own, so the CPU oracle (FS3D-rule v1) stands in"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_fs3d(args):
+    import torch
+    import fallingsand3d_gb300 as fs3d
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    master = args.master + rank  # weak scaling: each rank steps its own 2048-world batch
+    worlds = batch_worlds(fs3d, master, args.worlds)
+    cells = int(sum(X * Y * Z for (X, Y, Z), _ in worlds))
+    S = args.segment
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    # ---- headline: batched pool, device-resident
+    host = gen_grids(fs3d, worlds, pinned_torch=torch)
+    b = fs3d.Batch(150 << 30, steps_per_segment=S)
+    total_steps = S * (args.warmup + args.steps + 1)
+    tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
+    bstream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(args.warmup):
+        b.run_segment()
+    b.sync()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    seg_ms = []
+    launches0 = fs3d.kernel_launches()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)  # L2 flush between timed segments (outside the events)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(bstream)
+            b.run_segment()
+            e1.record(bstream)
+            e1.synchronize()
+            seg_ms.append(e0.elapsed_time(e1))
+    launches = fs3d.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    ms = float(np.mean(seg_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * S * world / (ms / 1e3)
+    # parity spot check of the timed run: a few worlds against the oracle
+    parity = None
+    if rank == 0 and not args.no_check:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        orc = oracle_lib.load()
+        b.sync()
+        ok = True
+        for i in range(3):
+            (X, Y, Z), seed = worlds[i]
+            g = host[i].numpy().copy()
+            orc.run(g, seed, 0, S * (args.warmup + args.steps), nthreads=0)
+            got = b.retire(tickets[i], (Y, Z, X))
+            ok &= bool((got == g).all())
+        parity = "3 worlds bit-exact after the timed segments" if ok else "MISMATCH"
+    b.close()
+
+    # ---- e2e through the C ABI from pinned host buffers
+    e2e_ms, h2d, d2h = [], cells, cells
+    outs = [torch.empty(g.shape, dtype=torch.uint8, pin_memory=True) for g in host]
+    for it in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
+            ts = [eb.admit(g.numpy(), seed, S) for g, (_, seed) in zip(host, worlds)]
+            eb.run_segment()
+            for t, o in zip(ts, outs):
+                fs3d.check(fs3d.lib().fs3d_batch_retire(eb.handle, t, o.data_ptr()))
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_val = cells * S / (e2e_ms[-1] / 1e3)
+
+    # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
+    offs, off = [], 0
+    for (X, Y, Z), _ in worlds:
+        offs.append(off)
+        off += (X * Y * Z + 255) // 256 * 256
+    pool = torch.empty(off, dtype=torch.uint8, device=dev)
+    for o, g in zip(offs, host):
+        pool[o:o + g.numel()].copy_(g.reshape(-1), non_blocking=True)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream(dev)
+    sp = st.cuda_stream
+    base = pool.data_ptr()
+
+    def plain_segment(t0):
+        for s in range(S):
+            for o, ((X, Y, Z), seed) in zip(offs, worlds):
+                fs3d.lib().fs3d_step_device(base + o, X, Y, Z, seed, t0 + s, 1, sp)
+
+    plain_segment(0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    plain_segment(S)
+    e1.record(st)
+    e1.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_val = cells * S / (plain_ms / 1e3)
+    del pool
+
+    # ---- plain single world 512^3 (drop-in byte kernel, HBM-bound)
+    p512 = None
+    if not args.skip_512:
+        X = Y = Z = 512
+        g = fs3d.gen_pillars(1, X, Y, Z)
+        d = torch.from_numpy(g).to(dev)
+        fs3d.step_device(d.data_ptr(), X, Y, Z, 1, 0, 8, sp)
+        torch.cuda.synchronize()
+        n = 256
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fs3d.step_device(d.data_ptr(), X, Y, Z, 1, 8, n, sp)
+        e1.record(st)
+        e1.synchronize()
+        t512 = e0.elapsed_time(e1) / n
+        hbm, src = peaks()
+        gbs = 2.0 * X * Y * Z / (t512 / 1e3) / 1e9
+        p512 = {"workload": "512^3 pillars, drop-in byte kernel, steps 8..263", "us_per_step": round(t512 * 1e3, 2),
+                "voxel_updates_per_s": X * Y * Z / (t512 / 1e3), "algorithmic_gbs": round(gbs, 1),
+                "hbm_frac": round(gbs / hbm, 3), "peak_gbs": hbm, "peak_source": src,
+                "note": "134 MB grid read+written per step, in place (comparable to the 126 MB L2)"}
+        # same world through the plane layout (the batched kernel, one world)
+        with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
+            w.step(8)
+            ws = torch.cuda.ExternalStream(w.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ws)
+            w.step(n)
+            e1.record(ws)
+            e1.synchronize()
+            tp = e0.elapsed_time(e1) / n
+        p512["planes_us_per_step"] = round(tp * 1e3, 2)
+        p512["planes_voxel_updates_per_s"] = X * Y * Z / (tp / 1e3)
+        del d
+
+    # ---- roofline of the dominant kernel (the plane step, 64 launches per segment)
+    hbm, src = peaks()
+    per_launch_ms = ms / S
+    alg_bytes = 0.5 * cells  # 2 bits read + 2 bits written per cell per step
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    traffic, traffic_cells = profile_traffic("k_plane_step")
+    if traffic is not None and traffic_cells:
+        traffic = traffic * cells / traffic_cells
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 3), "traffic": traffic, "kernel": "k_plane_step",
+                "peak_source": src, "alg_bytes_per_launch": alg_bytes,
+                "dense_equiv_gbs": round(2.0 * cells / (per_launch_ms / 1e3) / 1e9, 1)}
+
+    # ---- CPU baseline (rank 0, N=1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, info = cpu_sample(worlds, args.cpu_budget, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{info['worlds']} of the {args.worlds} worlds x {info['steps_per_round']} steps x "
+                         f"{info['rounds']} rounds, one world per thread ({info['seconds']} s)"}
+
+    if rank == 0:
+        line = {"metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+                "config": {"workload": f"batched: {args.worlds} worlds, dims iid from {{16,24,32,48,64,96,128}}^3, "
+                                       f"{S}-step CUDA-graph segments (one step = one segment)",
+                           "worlds_per_gpu": args.worlds, "cells_per_gpu": cells, "steps_per_segment": S,
+                           "master_seed": args.master, "l2": "flushed between timed segments (512 MB write)",
+                           "layout": "2-bit planes", "parallelism": f"replicas x{world}"},
+                "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms": round(e2e_ms[-1], 2),
+                        "path": "fs3d_batch_admit (pinned) + fs3d_batch_run_segment + fs3d_batch_retire"},
+                "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
+                                    "launches_per_segment": S * len(worlds),
+                                    "speedup_batched_vs_plain": round(value / world / plain_val, 2)},
+                "plain_512": p512, "parity": parity, "segment_ms": [round(x, 4) for x in seg_ms]}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
+    ap.add_argument("--worlds", type=int, default=2048)
+    ap.add_argument("--master", type=int, default=1)
+    ap.add_argument("--segment", type=int, default=64)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--skip-512", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_fs3d(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,407 @@
+"""fallingsand3d_gb300 — Python binding of libfs3d (the GB300 voxel step).
+
+A thin ctypes layer over the C ABI in ``include/fs3d.h``; every call goes to
+the CUDA library and there is no CPU fallback: importing works without a GPU
+(so host-side code and tests can run), but any call that needs the device
+fails loudly if the library or the GPU is missing.
+
+Grids are numpy ``uint8`` arrays in the canonical layout
+``idx = x + X*(z + Z*y)``, i.e. shape ``(Y, Z, X)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfs3d.so")
+
+LAYOUT_BYTES = 0
+LAYOUT_PLANES = 1
+RENDER_DDA = 0
+RENDER_SDF_SPHERE = 1
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_OOM = -2
+ERR_BUDGET = -3
+ERR_CUDA = -4
+ERR_TIMEOUT = -5
+ERR_MISMATCH = -6
+ERR_STATE = -7
+ERR_NOT_FOUND = -8
+ERR_IO = -9
+
+# every entry point of include/fs3d.h (checked by the tests)
+EXPORTS = (
+    "fs3d_abi_version", "fs3d_status_string", "fs3d_last_error", "fs3d_kernel_launch_count",
+    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_hash_device", "fs3d_first_diff_device",
+    "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
+    "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
+    "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit",
+    "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
+    "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_render", "fs3d_render_sdf",
+    "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_gen_parity", "fs3d_gen_pillars",
+    "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
+)
+
+
+class Fs3dError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"fs3d status {status}: {msg}")
+        self.status = status
+
+
+class Camera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
+                ("up", C.c_float * 3), ("tan_half_fov", C.c_float), ("aspect", C.c_float),
+                ("light_pos", C.c_float * 3), ("reserved", C.c_int32)]
+
+
+class Config(C.Structure):
+    _fields_ = [("steps_per_segment", C.c_int), ("ctas_per_sm", C.c_int), ("use_graphs", C.c_int),
+                ("reserved", C.c_int * 13)]
+
+
+_lib: Optional[C.CDLL] = None
+
+u8p = C.POINTER(C.c_uint8)
+vp = C.c_void_p
+i32, i64, u64 = C.c_int, C.c_int64, C.c_uint64
+
+
+def _bind(lib: C.CDLL) -> None:
+    S = C.c_int
+    sig = {
+        "fs3d_abi_version": (C.c_int, []),
+        "fs3d_status_string": (C.c_char_p, [S]),
+        "fs3d_last_error": (C.c_char_p, []),
+        "fs3d_kernel_launch_count": (u64, []),
+        "fs3d_default_config": (Config, []),
+        "fs3d_step_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_step_device_simple": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_hash_device": (S, [vp, i64, vp, C.POINTER(u64)]),
+        "fs3d_first_diff_device": (S, [vp, vp, i64, vp, C.POINTER(i64)]),
+        "fs3d_world_create": (S, [vp, i32, i32, i32, u64, u64, i32, C.POINTER(vp)]),
+        "fs3d_world_step": (S, [vp, i32]),
+        "fs3d_world_sync": (S, [vp, i64]),
+        "fs3d_world_read": (S, [vp, vp]),
+        "fs3d_world_write": (S, [vp, vp]),
+        "fs3d_world_hash": (S, [vp, C.POINTER(u64)]),
+        "fs3d_world_info": (S, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(u64),
+                                C.POINTER(u64), C.POINTER(i32)]),
+        "fs3d_world_device_ptr": (S, [vp, C.POINTER(vp), C.POINTER(i32)]),
+        "fs3d_world_stream": (S, [vp, C.POINTER(vp)]),
+        "fs3d_world_destroy": (S, [vp]),
+        "fs3d_world_save": (S, [vp, C.c_char_p]),
+        "fs3d_world_load": (S, [C.c_char_p, i32, C.POINTER(vp)]),
+        "fs3d_batch_create": (S, [C.c_size_t, C.POINTER(Config), C.POINTER(vp)]),
+        "fs3d_batch_admit": (S, [vp, vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
+        "fs3d_batch_run_segment": (S, [vp]),
+        "fs3d_batch_sync": (S, [vp, i64]),
+        "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
+        "fs3d_batch_retire": (S, [vp, u64, vp]),
+        "fs3d_batch_stats": (S, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_size_t),
+                                 C.POINTER(C.c_size_t)]),
+        "fs3d_batch_stream": (S, [vp, C.POINTER(vp)]),
+        "fs3d_batch_destroy": (S, [vp]),
+        "fs3d_render": (S, [vp, C.POINTER(Camera), i32, i32, i32, vp, i32]),
+        "fs3d_render_sdf": (S, [C.POINTER(Camera), i32, i32, vp, vp]),
+        "fs3d_camera_fs_raymarch": (None, [C.POINTER(Camera)]),
+        "fs3d_camera_world_view": (None, [C.POINTER(Camera), i32, i32, i32, i32, i32]),
+        "fs3d_gen_parity": (S, [u64, i32, i32, i32, vp]),
+        "fs3d_gen_pillars": (S, [u64, i32, i32, i32, vp]),
+        "fs3d_gen_batch_dims": (S, [u64, i32, vp, vp]),
+        "fs3d_gen_batch_world": (S, [u64, i32, i32, i32, vp]),
+        "fs3d_gen_dunes": (S, [u64, i32, i32, i32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib() -> C.CDLL:
+    """The loaded libfs3d; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -m fallingsand3d_gb300.build` first")
+        lib_ = C.CDLL(LIB_PATH)
+        _bind(lib_)
+        _lib = lib_
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        L = lib()
+        raise Fs3dError(status, f"{L.fs3d_status_string(status).decode()}: {L.fs3d_last_error().decode()}")
+
+
+def _ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+def kernel_launches() -> int:
+    return int(lib().fs3d_kernel_launch_count())
+
+
+# ---------------------------------------------------------------- generators
+def _gen(fn: str, seed: int, X: int, Y: int, Z: int) -> np.ndarray:
+    g = np.empty((Y, Z, X), np.uint8)
+    check(getattr(lib(), fn)(seed, X, Y, Z, _ptr(g)))
+    return g
+
+
+def gen_parity(seed: int, X: int = 64, Y: int = 64, Z: int = 64) -> np.ndarray:
+    """Stone floor, upper half iid sand 0.25 / water 0.15."""
+    return _gen("fs3d_gen_parity", seed, X, Y, Z)
+
+
+def gen_pillars(seed: int, X: int = 512, Y: int = 512, Z: int = 512) -> np.ndarray:
+    """Stone floor + 256 stone pillars, upper 60% iid sand 0.30 / water 0.10."""
+    return _gen("fs3d_gen_pillars", seed, X, Y, Z)
+
+
+def gen_batch_world(seed: int, X: int, Y: int, Z: int) -> np.ndarray:
+    return _gen("fs3d_gen_batch_world", seed, X, Y, Z)
+
+
+def gen_dunes(seed: int, X: int = 1024, Y: int = 1024, Z: int = 1024) -> np.ndarray:
+    return _gen("fs3d_gen_dunes", seed, X, Y, Z)
+
+
+def gen_batch_dims(master: int, count: int):
+    dims = np.empty((count, 3), np.int32)
+    seeds = np.empty(count, np.uint64)
+    check(lib().fs3d_gen_batch_dims(master, count, _ptr(dims), _ptr(seeds)))
+    return dims, seeds
+
+
+# ---------------------------------------------------------------- cameras
+def camera_fs_raymarch() -> Camera:
+    c = Camera()
+    lib().fs3d_camera_fs_raymarch(C.byref(c))
+    return c
+
+
+def camera_world_view(X: int, Y: int, Z: int, W: int, H: int) -> Camera:
+    c = Camera()
+    lib().fs3d_camera_world_view(C.byref(c), X, Y, Z, W, H)
+    return c
+
+
+# ---------------------------------------------------------------- device entry points
+def step_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
+    """Drop-in step of a device grid (pointer) in place; async on `stream`."""
+    check(lib().fs3d_step_device(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
+
+
+def step_device_simple(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int,
+                       stream: int = 0) -> None:
+    """One-thread-per-block reference kernel (same contract as step_device)."""
+    check(lib().fs3d_step_device_simple(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
+
+
+def hash_device(grid_ptr: int, n_cells: int, stream: int = 0) -> int:
+    out = u64(0)
+    check(lib().fs3d_hash_device(grid_ptr, n_cells, stream, C.byref(out)))
+    return int(out.value)
+
+
+def first_diff_device(a_ptr: int, b_ptr: int, n_cells: int, stream: int = 0) -> int:
+    out = i64(0)
+    check(lib().fs3d_first_diff_device(a_ptr, b_ptr, n_cells, stream, C.byref(out)))
+    return int(out.value)
+
+
+def render_sdf_device(cam: Camera, W: int, H: int, rgba_ptr: int, stream: int = 0) -> None:
+    check(lib().fs3d_render_sdf(C.byref(cam), W, H, rgba_ptr, stream))
+
+
+# ---------------------------------------------------------------- world
+class World:
+    """One device-resident world (library-owned memory and stream)."""
+
+    def __init__(self, grid: np.ndarray, seed: int, start_step: int = 0, layout: int = LAYOUT_PLANES):
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        if g.ndim != 3:
+            raise ValueError("grid must have shape (Y, Z, X)")
+        Y, Z, X = g.shape
+        h = vp()
+        check(lib().fs3d_world_create(_ptr(g), X, Y, Z, seed, start_step, layout, C.byref(h)))
+        self._h = h
+        self.X, self.Y, self.Z, self.seed, self.layout = X, Y, Z, seed, layout
+
+    @classmethod
+    def load(cls, path: str, layout: int = LAYOUT_PLANES) -> "World":
+        self = cls.__new__(cls)
+        h = vp()
+        check(lib().fs3d_world_load(path.encode(), layout, C.byref(h)))
+        self._h = h
+        X, Y, Z, L = i32(), i32(), i32(), i32()
+        seed, step = u64(), u64()
+        check(lib().fs3d_world_info(h, C.byref(X), C.byref(Y), C.byref(Z), C.byref(seed), C.byref(step),
+                                    C.byref(L)))
+        self.X, self.Y, self.Z, self.seed, self.layout = X.value, Y.value, Z.value, seed.value, L.value
+        return self
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise Fs3dError(ERR_STATE, "world destroyed")
+        return self._h
+
+    @property
+    def step_counter(self) -> int:
+        s = u64()
+        check(lib().fs3d_world_info(self.handle, None, None, None, None, C.byref(s), None))
+        return int(s.value)
+
+    def step(self, n: int = 1) -> None:
+        check(lib().fs3d_world_step(self.handle, n))
+
+    def sync(self, timeout_ns: int = -1) -> None:
+        check(lib().fs3d_world_sync(self.handle, timeout_ns))
+
+    def read(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        g = out if out is not None else np.empty((self.Y, self.Z, self.X), np.uint8)
+        check(lib().fs3d_world_read(self.handle, _ptr(g)))
+        return g
+
+    def write(self, grid: np.ndarray) -> None:
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        if g.shape != (self.Y, self.Z, self.X):
+            raise ValueError("shape mismatch")
+        check(lib().fs3d_world_write(self.handle, _ptr(g)))
+
+    def hash(self) -> int:
+        out = u64()
+        check(lib().fs3d_world_hash(self.handle, C.byref(out)))
+        return int(out.value)
+
+    def device_ptr(self) -> int:
+        p, L = vp(), i32()
+        check(lib().fs3d_world_device_ptr(self.handle, C.byref(p), C.byref(L)))
+        return int(p.value or 0)
+
+    def stream(self) -> int:
+        p = vp()
+        check(lib().fs3d_world_stream(self.handle, C.byref(p)))
+        return int(p.value or 0)
+
+    def save(self, path: str) -> None:
+        check(lib().fs3d_world_save(self.handle, path.encode()))
+
+    def render(self, cam: Camera, W: int, H: int, mode: int = RENDER_DDA, out_ptr: Optional[int] = None):
+        if out_ptr is not None:
+            check(lib().fs3d_render(self.handle, C.byref(cam), W, H, mode, out_ptr, 1))
+            return None
+        img = np.empty((H, W, 4), np.float32)
+        check(lib().fs3d_render(self.handle, C.byref(cam), W, H, mode, _ptr(img), 0))
+        return img
+
+    def close(self) -> None:
+        if self._h is not None:
+            check(lib().fs3d_world_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- batch
+class Batch:
+    """Pool of many worlds stepped together in graph-captured segments."""
+
+    def __init__(self, budget_bytes: int, steps_per_segment: int = 64, use_graphs: bool = True,
+                 ctas_per_sm: int = 0):
+        cfg = lib().fs3d_default_config()
+        cfg.steps_per_segment = steps_per_segment
+        cfg.use_graphs = 1 if use_graphs else 0
+        cfg.ctas_per_sm = ctas_per_sm
+        h = vp()
+        check(lib().fs3d_batch_create(budget_bytes, C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise Fs3dError(ERR_STATE, "batch destroyed")
+        return self._h
+
+    def admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> int:
+        g = np.ascontiguousarray(grid, dtype=np.uint8)
+        Y, Z, X = g.shape
+        t = u64()
+        check(lib().fs3d_batch_admit(self.handle, _ptr(g), X, Y, Z, seed, start_step, n_steps, C.byref(t)))
+        return int(t.value)
+
+    def try_admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> Optional[int]:
+        try:
+            return self.admit(grid, seed, n_steps, start_step)
+        except Fs3dError as e:
+            if e.status == ERR_BUDGET:
+                return None
+            raise
+
+    def run_segment(self) -> None:
+        check(lib().fs3d_batch_run_segment(self.handle))
+
+    def sync(self, timeout_ns: int = -1) -> None:
+        check(lib().fs3d_batch_sync(self.handle, timeout_ns))
+
+    def poll(self, ticket: int, with_hash: bool = True):
+        done, h = i32(), u64()
+        check(lib().fs3d_batch_poll(self.handle, ticket, C.byref(done), C.byref(h) if with_hash else None))
+        return bool(done.value), (int(h.value) if done.value and with_hash else None)
+
+    def retire(self, ticket: int, shape=None) -> Optional[np.ndarray]:
+        if shape is None:
+            check(lib().fs3d_batch_retire(self.handle, ticket, None))
+            return None
+        g = np.empty(shape, np.uint8)
+        check(lib().fs3d_batch_retire(self.handle, ticket, _ptr(g)))
+        return g
+
+    def stats(self):
+        w, c = i64(), i64()
+        u, b = C.c_size_t(), C.c_size_t()
+        check(lib().fs3d_batch_stats(self.handle, C.byref(w), C.byref(c), C.byref(u), C.byref(b)))
+        return {"live_worlds": w.value, "live_cells": c.value, "bytes_used": u.value, "bytes_budget": b.value}
+
+    def stream(self) -> int:
+        p = vp()
+        check(lib().fs3d_batch_stream(self.handle, C.byref(p)))
+        return int(p.value or 0)
+
+    def close(self) -> None:
+        if self._h is not None:
+            check(lib().fs3d_batch_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

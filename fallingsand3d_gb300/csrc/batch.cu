@@ -1,0 +1,415 @@
+// fs3d_batch: many independent worlds of mixed sizes in one device pool (bit
+// plane format), stepped together.  A segment is `steps_per_segment` launches
+// of the multi-world step kernel captured once as a CUDA graph; the graph
+// reads the world and work-item tables from device memory, so worlds join
+// (admit) and leave (retire) between segments without a re-capture.  Each
+// world keeps its own step counter, so its trajectory is the same whether it
+// runs alone or inside any mix.
+//
+// Streams: `stream` runs segments; `side` runs admissions (upload + format
+// conversion) and retirements (conversion + download), ordered against the
+// segments with events, so requests arriving while a segment runs are
+// uploaded concurrently.
+#include <string.h>
+
+#include <chrono>
+#include <map>
+#include <thread>
+#include <vector>
+
+#include "fs3d_common.h"
+#include "planes.h"
+
+using namespace fs3d;
+
+namespace {
+
+struct BWorld {
+    int X = 0, Y = 0, Z = 0, nw = 0;
+    uint64_t seed = 0, t = 0;
+    int64_t remaining = 0;
+    uint4* rows = nullptr;
+    uint8_t* statics = nullptr;
+    size_t bytes = 0;
+    bool done = false;
+    cudaEvent_t ready = nullptr;     // admission finished (side stream)
+    cudaEvent_t finished = nullptr;  // last segment that stepped it
+    bool hash_valid = false;
+    uint64_t hash = 0;
+};
+
+template <class T>
+struct PinnedArray {
+    T* h = nullptr;
+    T* d = nullptr;
+    size_t cap = 0;
+    fs3d_status reserve(size_t n) {
+        if (n <= cap) return FS3D_OK;
+        size_t c = cap ? cap : 64;
+        while (c < n) c *= 2;
+        T *nh = nullptr, *nd = nullptr;
+        FS3D_CUDA(cudaMallocHost((void**)&nh, sizeof(T) * c));
+        cudaError_t e = cudaMalloc((void**)&nd, sizeof(T) * c);
+        if (e != cudaSuccess) {
+            cudaFreeHost(nh);
+            return cuda_fail(e, "cudaMalloc(batch tables)");
+        }
+        cudaFreeHost(h);
+        cudaFree(d);
+        h = nh;
+        d = nd;
+        cap = c;
+        return FS3D_OK;
+    }
+    void release() {
+        cudaFreeHost(h);
+        cudaFree(d);
+        h = d = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct fs3d_batch {
+    size_t budget = 0, used = 0;
+    fs3d_config cfg{};
+    cudaStream_t stream = nullptr, side = nullptr;
+    std::map<uint64_t, BWorld> worlds;
+    uint64_t next_ticket = 1;
+    PinnedArray<PlaneWorld> tw;
+    PinnedArray<PlaneItem> ti;
+    PinnedArray<int> tn;
+    cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
+    cudaEvent_t last_segment = nullptr;
+    std::vector<cudaEvent_t> pending_ready;  // admissions the next segment must wait for
+    cudaGraphExec_t graph = nullptr;
+    void* graph_worlds = nullptr;  // table pointers baked into the graph
+    void* graph_items = nullptr;
+    int grid = 0;
+    unsigned long long* hash_dev = nullptr;
+    uint64_t segments = 0;
+};
+
+namespace {
+
+fs3d_status wait_stream(cudaStream_t st, int64_t timeout_ns) {
+    if (timeout_ns < 0) {
+        FS3D_CUDA(cudaStreamSynchronize(st));
+        return FS3D_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) return FS3D_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(e, "cudaStreamQuery");
+        if (std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count() >=
+            timeout_ns)
+            return set_error(FS3D_ERR_TIMEOUT, "batch stream did not finish within the timeout");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+void free_world(fs3d_batch* b, BWorld& w) {
+    if (w.rows) cudaFreeAsync(w.rows, b->side);
+    if (w.statics) cudaFreeAsync(w.statics, b->side);
+    if (w.ready) cudaEventDestroy(w.ready);
+    if (w.finished) cudaEventDestroy(w.finished);
+    w.rows = nullptr;
+    w.statics = nullptr;
+    w.ready = w.finished = nullptr;
+}
+
+fs3d_status capture_graph(fs3d_batch* b) {
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaStream_t cs;
+    FS3D_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    fs3d_status s = FS3D_OK;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int a = 0; a < b->cfg.steps_per_segment && s == FS3D_OK; ++a)
+            s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, a, cs);
+        e = cudaStreamEndCapture(cs, &g);
+    }
+    if (e == cudaSuccess && s == FS3D_OK) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (s != FS3D_OK) return s;
+    if (e != cudaSuccess) return cuda_fail(e, "segment graph capture");
+    b->graph_worlds = b->tw.d;
+    b->graph_items = b->ti.d;
+    return FS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch** out) {
+    if (!out || budget == 0) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_create: bad args");
+    *out = nullptr;
+    fs3d_batch* b = new fs3d_batch();
+    b->budget = budget;
+    b->cfg = cfg ? *cfg : fs3d_default_config();
+    if (b->cfg.steps_per_segment <= 0) b->cfg.steps_per_segment = 64;
+    if (b->cfg.steps_per_segment > 4096) b->cfg.steps_per_segment = 4096;
+    const int resident = plane_step_ctas_per_sm();
+    const int per_sm = b->cfg.ctas_per_sm > 0 && b->cfg.ctas_per_sm < resident ? b->cfg.ctas_per_sm : resident;
+    b->grid = sm_count_public() * per_sm;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        // keep freed pool memory cached so admissions after retirements are cheap
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_create");
+    if (s == FS3D_OK) s = b->tn.reserve(1);
+    if (s != FS3D_OK) {
+        fs3d_batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t seed,
+                             uint64_t start_step, int64_t n_steps, uint64_t* ticket) {
+    if (!b || !g || !ticket || X <= 0 || Y <= 0 || Z <= 0 || X > kPlaneMaxX || Y > 65536 || Z > 65536 ||
+        n_steps < 0)
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit: bad args (X must be 1..2048)");
+    const size_t n = (size_t)X * Y * Z;
+    bool stat = false;
+    for (size_t i = 0; i < n && !stat; ++i) stat = g[i] >= 4;
+    BWorld w;
+    w.X = X;
+    w.Y = Y;
+    w.Z = Z;
+    w.nw = plane_nw(X);
+    w.seed = seed;
+    w.t = start_step;
+    w.remaining = n_steps;
+    w.done = n_steps == 0;
+    w.bytes = plane_bytes(X, Y, Z) + (stat ? n : 0) + sizeof(PlaneWorld);
+    if (b->used + w.bytes > b->budget)
+        return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
+    uint8_t* staging = nullptr;
+    FS3D_CUDA(cudaMallocAsync((void**)&w.rows, plane_bytes(X, Y, Z), b->side));
+    cudaError_t e = cudaMallocAsync((void**)&staging, n, b->side);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(staging, g, n, cudaMemcpyHostToDevice, b->side);
+    fs3d_status s = e == cudaSuccess ? planes_from_bytes(staging, X, Y, Z, w.rows, b->side) : cuda_fail(e, "admit upload");
+    if (stat)
+        w.statics = staging;
+    else if (staging)
+        cudaFreeAsync(staging, b->side);
+    if (s == FS3D_OK) {
+        e = cudaEventCreateWithFlags(&w.ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(w.ready, b->side);
+        // the caller's buffer may be reused as soon as this returns
+        if (e == cudaSuccess) e = cudaEventSynchronize(w.ready);
+        if (e != cudaSuccess) s = cuda_fail(e, "admit event");
+    }
+    if (s != FS3D_OK) {
+        free_world(b, w);
+        return s;
+    }
+    b->used += w.bytes;
+    *ticket = b->next_ticket++;
+    b->worlds.emplace(*ticket, w);
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_run_segment: NULL batch");
+    const int S = b->cfg.steps_per_segment;
+    // the pinned tables may be rewritten once the previous upload has run
+    FS3D_CUDA(cudaEventSynchronize(b->tables_free));
+    size_t nw_ = 0, ni = 0;
+    for (auto& kv : b->worlds) {
+        BWorld& w = kv.second;
+        if (w.done) continue;
+        ++nw_;
+        ni += (size_t)plane_items_for(w.Y, w.Z, w.nw);
+    }
+    if (nw_ == 0) return FS3D_OK;
+    void* old_w = b->tw.d;
+    void* old_i = b->ti.d;
+    // growing the tables frees device arrays a running segment may still read
+    if (nw_ > b->tw.cap || ni > b->ti.cap) FS3D_CUDA(cudaStreamSynchronize(b->stream));
+    fs3d_status s = b->tw.reserve(nw_);
+    if (s == FS3D_OK) s = b->ti.reserve(ni);
+    if (s != FS3D_OK) return s;
+    size_t wi = 0, ii = 0;
+    for (auto& kv : b->worlds) {
+        BWorld& w = kv.second;
+        if (w.done) continue;
+        const int steps = (int)(w.remaining < S ? w.remaining : S);
+        PlaneWorld& d = b->tw.h[wi];
+        memset(&d, 0, sizeof(d));
+        d.rows = w.rows;
+        d.seed = w.seed;
+        d.t = w.t;
+        d.X = w.X;
+        d.Y = w.Y;
+        d.Z = w.Z;
+        d.nw = w.nw;
+        d.steps = steps;
+        d.lg = plane_lg(w.nw);
+        const int per = 32 >> d.lg, items = plane_items_for(w.Y, w.Z, w.nw);
+        for (int a = 0; a < items; ++a) b->ti.h[ii++] = PlaneItem{(int32_t)wi, a * per};
+        ++wi;
+    }
+    b->tn.h[0] = (int)ii;
+    // admissions complete before the segment reads their planes
+    for (auto& kv : b->worlds)
+        if (kv.second.ready) {
+            FS3D_CUDA(cudaStreamWaitEvent(b->stream, kv.second.ready, 0));
+            cudaEventDestroy(kv.second.ready);
+            kv.second.ready = nullptr;
+        }
+    FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * wi, cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
+    if (b->cfg.use_graphs) {
+        if (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || old_w != b->tw.d ||
+            old_i != b->ti.d) {
+            s = capture_graph(b);
+            if (s != FS3D_OK) return s;
+        }
+        FS3D_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        note_launch((uint64_t)S);
+    } else {
+        for (int a = 0; a < S; ++a) {
+            s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, a, b->stream);
+            if (s != FS3D_OK) return s;
+        }
+    }
+    FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
+    for (auto& kv : b->worlds) {
+        BWorld& w = kv.second;
+        if (w.done) continue;
+        const int steps = (int)(w.remaining < S ? w.remaining : S);
+        w.t += (uint64_t)steps;
+        w.remaining -= steps;
+        if (w.remaining == 0) {
+            w.done = true;
+            if (!w.finished) FS3D_CUDA(cudaEventCreateWithFlags(&w.finished, cudaEventDisableTiming));
+            FS3D_CUDA(cudaEventRecord(w.finished, b->stream));
+        }
+    }
+    ++b->segments;
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_sync: NULL batch");
+    fs3d_status s = wait_stream(b->stream, timeout_ns);
+    if (s != FS3D_OK) return s;
+    return wait_stream(b->side, timeout_ns);
+}
+
+fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash) {
+    if (!b || !done) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_poll: bad args");
+    auto it = b->worlds.find(ticket);
+    if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_poll: unknown ticket");
+    BWorld& w = it->second;
+    *done = 0;
+    if (!w.done) return FS3D_OK;
+    if (w.finished) {
+        const cudaError_t q = cudaEventQuery(w.finished);
+        if (q == cudaErrorNotReady) return FS3D_OK;
+        if (q != cudaSuccess) return cuda_fail(q, "fs3d_batch_poll");
+    }
+    if (!w.hash_valid && hash) {
+        if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
+        fs3d_status s = planes_hash_async(w.rows, w.statics, w.X, w.Y, w.Z, b->hash_dev, b->side);
+        if (s != FS3D_OK) return s;
+        unsigned long long h = 0;
+        FS3D_CUDA(cudaMemcpyAsync(&h, b->hash_dev, sizeof(h), cudaMemcpyDeviceToHost, b->side));
+        FS3D_CUDA(cudaStreamSynchronize(b->side));
+        w.hash = h;
+        w.hash_valid = true;
+    }
+    *done = 1;
+    if (hash) *hash = w.hash;
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire: NULL batch");
+    auto it = b->worlds.find(ticket);
+    if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire: unknown ticket");
+    BWorld& w = it->second;
+    // the world's planes are final after its last segment (or, if retired
+    // early, after the last segment enqueued so far)
+    FS3D_CUDA(cudaStreamWaitEvent(b->side, w.finished ? w.finished : b->last_segment, 0));
+    if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
+    fs3d_status s = FS3D_OK;
+    if (grid_out) {
+        const size_t n = (size_t)w.X * w.Y * w.Z;
+        uint8_t* staging = nullptr;
+        FS3D_CUDA(cudaMallocAsync((void**)&staging, n, b->side));
+        s = planes_to_bytes(w.rows, w.statics, w.X, w.Y, w.Z, staging, b->side);
+        cudaError_t e = cudaSuccess;
+        if (s == FS3D_OK) e = cudaMemcpyAsync(grid_out, staging, n, cudaMemcpyDeviceToHost, b->side);
+        cudaFreeAsync(staging, b->side);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
+        if (s == FS3D_OK && e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire readback");
+    }
+    b->used -= w.bytes;
+    free_world(b, w);
+    b->worlds.erase(it);
+    return s;
+}
+
+fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells, size_t* bytes_used,
+                             size_t* bytes_budget) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_stats: NULL batch");
+    int64_t cells = 0;
+    for (auto& kv : b->worlds) cells += (int64_t)kv.second.X * kv.second.Y * kv.second.Z;
+    if (live_worlds) *live_worlds = (int64_t)b->worlds.size();
+    if (live_cells) *live_cells = cells;
+    if (bytes_used) *bytes_used = b->used;
+    if (bytes_budget) *bytes_budget = b->budget;
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream) {
+    if (!b || !stream) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_stream: bad args");
+    *stream = (void*)b->stream;
+    return FS3D_OK;
+}
+
+fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_destroy: NULL batch");
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->side) cudaStreamSynchronize(b->side);
+    for (auto& kv : b->worlds) free_world(b, kv.second);
+    b->worlds.clear();
+    if (b->side) cudaStreamSynchronize(b->side);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->tw.release();
+    b->ti.release();
+    b->tn.release();
+    cudaFree(b->hash_dev);
+    if (b->tables_free) cudaEventDestroy(b->tables_free);
+    if (b->last_segment) cudaEventDestroy(b->last_segment);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->side) cudaStreamDestroy(b->side);
+    delete b;
+    return FS3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,285 @@
+// Bit-plane world format and the multi-world bit-sliced step.
+//
+// Format.  A world of X*Y*Z cells is stored as Y*Z rows (row r = y*Z + z) of
+// nw = ceil(X/64) uint4 words; word g of a row covers x in [64g, 64g+64) and
+// holds {A even, A odd, B even, B odd}: bit m of an even word is x = 64g+2m,
+// of an odd word x = 64g+2m+1.  (A,B) = (0,0) empty, (0,1) solid, (1,0) sand,
+// (1,1) water; cells past X are solid.  Static cells never change, so their
+// byte values (stone, or any material >= 4) are taken from an optional byte
+// copy of the initial grid when the world is read back.
+//
+// Step.  The blocks of a block row that start in word g (i = 32g .. 32g+31)
+// are evaluated together: in the even phase their dx=0 / dx=1 cells are the
+// even / odd words of g; in the odd phase (blocks start at odd x) the dx=0
+// cells are the odd word shifted up one bit with the top bit of word g-1
+// carried in, and the dx=1 cells are the even word.  A lane group of
+// G = pow2ceil(nw) lanes handles one block row-pair (4 rows); lane g owns
+// storage word g and the carried bit travels by warp shuffle, so each bit is
+// read for computation and written by exactly one lane.  When X is a multiple
+// of 64 the odd phase has one extra half block per row-pair (cells x = X-1,
+// x = X outside), which the last lane runs with the scalar rule.
+#include <stdint.h>
+
+#include "fs3d_common.h"
+#include "planes.h"
+#include "rule_device.cuh"
+
+namespace fs3d {
+
+// ---------------------------------------------------------------------------
+// conversions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void classify(uint32_t v, uint32_t& a, uint32_t& b) {
+    a = (v == 2u || v == 3u) ? 1u : 0u;
+    b = (v == 0u || v == 2u) ? 0u : 1u;
+}
+
+__global__ void k_bytes_to_planes(const uint8_t* __restrict__ g, int X, int Y, int Z, int nw,
+                                  uint4* __restrict__ rows) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int w = (int)(u % nw);
+        const int64_t r = u / nw;
+        const uint8_t* row = g + r * X;
+        uint32_t ae = 0, ao = 0, be = 0, bo = 0;
+        for (int m = 0; m < 32; ++m) {
+            const int xe = 64 * w + 2 * m, xo = xe + 1;
+            uint32_t a, b;
+            classify(xe < X ? row[xe] : 1u, a, b);
+            ae |= a << m;
+            be |= b << m;
+            classify(xo < X ? row[xo] : 1u, a, b);
+            ao |= a << m;
+            bo |= b << m;
+        }
+        rows[u] = make_uint4(ae, ao, be, bo);
+    }
+}
+
+__device__ __forceinline__ uint32_t cell_value(const uint4& q, int m, int odd, const uint8_t* statics, int64_t idx) {
+    const uint32_t a = ((odd ? q.y : q.x) >> m) & 1u, b = ((odd ? q.w : q.z) >> m) & 1u;
+    if (a) return b ? 3u : 2u;
+    if (!b) return 0u;
+    return statics ? statics[idx] : 1u;
+}
+
+__global__ void k_planes_to_bytes(const uint4* __restrict__ rows, const uint8_t* __restrict__ statics, int X,
+                                  int Y, int Z, int nw, uint8_t* __restrict__ g) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int w = (int)(u % nw);
+        const int64_t r = u / nw;
+        const uint4 q = rows[u];
+        for (int x = 64 * w; x < 64 * w + 64 && x < X; ++x) {
+            const int64_t idx = r * X + x;
+            g[idx] = (uint8_t)cell_value(q, (x >> 1) & 31, x & 1, statics, idx);
+        }
+    }
+}
+
+__global__ void k_hash_planes(const uint4* __restrict__ rows, const uint8_t* __restrict__ statics, int X, int Y,
+                              int Z, int nw, unsigned long long* out) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    uint64_t h = 0;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int w = (int)(u % nw);
+        const int64_t r = u / nw;
+        const uint4 q = rows[u];
+        for (int x = 64 * w; x < 64 * w + 64 && x < X; ++x) {
+            const int64_t idx = r * X + x;
+            h += fmix64((uint64_t)idx * 256u + cell_value(q, (x >> 1) & 31, x & 1, statics, idx));
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) h += __shfl_xor_sync(0xffffffffu, h, off);
+    if ((threadIdx.x & 31) == 0 && h) atomicAdd(out, (unsigned long long)h);
+}
+
+// ---------------------------------------------------------------------------
+// step
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cls_byte(uint32_t a, uint32_t b) { return a ? (b ? 3u : 2u) : (b ? 1u : 0u); }
+
+// One block row-pair of one world; lane gl of a group of G lanes.
+// Returns true if any of the four rows changed.
+__device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, int gl, int G,
+                                              unsigned gmask) {
+    const int NBZ = nblocks(w.Z, o);
+    const int j = rp / NBZ, k = rp - j * NBZ;
+    const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
+    const int y0 = 2 * j - o, z0 = 2 * k - o;
+    const bool has = gl < w.nw;
+    uint4 q[4];
+    uint4* ptr[4];
+    bool in[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+        in[a] = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
+        ptr[a] = in[a] ? w.rows + ((int64_t)y * w.Z + z) * w.nw + gl : w.rows;
+        q[a] = in[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    }
+    // slot s = layer*4 + dz*2 + dx; row a = layer*2 + dz
+    uint32_t A[8], B[8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+        if (o == 0) {
+            A[s0] = q[a].x;
+            B[s0] = q[a].z;
+        } else {
+            uint32_t ua = __shfl_up_sync(gmask, q[a].y, 1, G);
+            uint32_t ub = __shfl_up_sync(gmask, q[a].w, 1, G);
+            if (gl == 0) {
+                ua = 0u;  // x = -1 lies outside: solid
+                ub = 0xFFFFFFFFu;
+            }
+            A[s0] = (q[a].y << 1) | (ua >> 31);
+            B[s0] = (q[a].w << 1) | (ub >> 31);
+        }
+        A[s0 + 1] = (o == 0) ? q[a].y : q[a].x;
+        B[s0 + 1] = (o == 0) ? q[a].w : q[a].z;
+    }
+    if (has) bs_rule(A, B, rk, (uint32_t)gl);
+    // half block at x = X-1 (odd phase, X % 64 == 0): last lane, scalar rule
+    uint32_t half = 0;
+    const bool do_half = o == 1 && has && gl == w.nw - 1 && (w.X & 63) == 0;
+    if (do_half) {
+        uint64_t V = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+            V |= (uint64_t)cls_byte(q[a].y >> 31, q[a].w >> 31) << (8 * s0);
+            V |= (uint64_t)1u << (8 * (s0 + 1));
+        }
+        if (block_can_move((uint32_t)V, (uint32_t)(V >> 32))) V = block_rule(V, rk, 32u * (uint32_t)w.nw);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const uint32_t c = get_byte(V, (a >> 1) * 4 + (a & 1) * 2);
+            half |= ((c == 2u || c == 3u) ? 1u : 0u) << a;                   // A bit
+            half |= ((c == 0u || c == 2u) ? 0u : 1u) << (4 + a);             // B bit
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+        uint4 n;
+        if (o == 0) {
+            n = make_uint4(A[s0], A[s0 + 1], B[s0], B[s0 + 1]);
+        } else {
+            const uint32_t da = __shfl_down_sync(gmask, A[s0], 1, G);
+            const uint32_t db = __shfl_down_sync(gmask, B[s0], 1, G);
+            uint32_t ta, tb;  // new bit 31 of this lane's odd words
+            if (gl < w.nw - 1) {
+                ta = da & 1u;
+                tb = db & 1u;
+            } else if (do_half) {
+                ta = (half >> a) & 1u;
+                tb = (half >> (4 + a)) & 1u;
+            } else {
+                ta = q[a].y >> 31;
+                tb = q[a].w >> 31;
+            }
+            n = make_uint4(A[s0 + 1], (A[s0] >> 1) | (ta << 31), B[s0 + 1], (B[s0] >> 1) | (tb << 31));
+        }
+        if (in[a] && (n.x != q[a].x || n.y != q[a].y || n.z != q[a].z || n.w != q[a].w)) *ptr[a] = n;
+    }
+}
+
+// One launch = one step (segment step s_seg) of every live world.  Work items
+// are warp-sized: item = (world, first row-pair); a warp covers 32 >> lg
+// row-pairs of that world.  Warps loop over items; the item count lives in
+// device memory so a captured graph keeps working as worlds come and go.
+__global__ void __launch_bounds__(256) k_plane_step(const PlaneWorld* __restrict__ worlds,
+                                                   const PlaneItem* __restrict__ items,
+                                                   const int* __restrict__ n_items_p, int s_seg) {
+    const int n_items = *n_items_p;
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += warps) {
+        const PlaneItem item = items[it];
+        const PlaneWorld& w = worlds[item.world];
+        if (s_seg >= w.steps) continue;
+        const uint64_t t = w.t + (uint64_t)s_seg;
+        const int o = (int)(t & 1u);
+        const int G = 1 << w.lg;
+        const int gl = lane & (G - 1);
+        const int rp = item.rp0 + (lane >> w.lg);
+        const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
+        if (rp >= nrp) continue;  // uniform within a lane group
+        const unsigned gmask = (G == 32) ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+        plane_rowpair(w, o, stepkey(w.seed, t), rp, gl, G, gmask);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int sm_count_public();
+
+static int conv_grid(int64_t n) {
+    const int64_t need = (n + 255) / 256, cap = (int64_t)sm_count_public() * 8;
+    return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
+int plane_lg(int nw) {
+    int lg = 0;
+    while ((1 << lg) < nw) ++lg;
+    return lg;
+}
+
+int plane_items_for(int Y, int Z, int nw) {
+    const int per = 32 >> plane_lg(nw);
+    const int nrp = nblocks(Y, 1) * nblocks(Z, 1);
+    return (nrp + per - 1) / per;
+}
+
+fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows, cudaStream_t st) {
+    const int nw = plane_nw(X);
+    k_bytes_to_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(g, X, Y, Z, nw, rows);
+    FS3D_CHECK_LAUNCH("bytes->planes launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, uint8_t* g,
+                            cudaStream_t st) {
+    const int nw = plane_nw(X);
+    k_planes_to_bytes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, statics, X, Y, Z, nw, g);
+    FS3D_CHECK_LAUNCH("planes->bytes launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,
+                              unsigned long long* out_dev, cudaStream_t st) {
+    const int nw = plane_nw(X);
+    FS3D_CUDA(cudaMemsetAsync(out_dev, 0, sizeof(unsigned long long), st));
+    k_hash_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, statics, X, Y, Z, nw, out_dev);
+    FS3D_CHECK_LAUNCH("hash planes launch");
+    return FS3D_OK;
+}
+
+fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev,
+                              int grid, int s_seg, cudaStream_t st) {
+    k_plane_step<<<grid, 256, 0, st>>>(worlds, items, n_items_dev, s_seg);
+    FS3D_CHECK_LAUNCH("plane step launch");
+    return FS3D_OK;
+}
+
+// CTAs of the step kernel that fit on one SM at once
+int plane_step_ctas_per_sm() {
+    static int n = 0;
+    if (!n) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_plane_step, 256, 0) != cudaSuccess || n < 1) n = 1;
+    }
+    return n;
+}
+
+// persistent grid: every CTA resident, so warps pick items without tail waves
+int plane_step_grid(int64_t n_items) {
+    const int64_t warps_per_cta = 8;
+    const int64_t need = (n_items + warps_per_cta - 1) / warps_per_cta;
+    const int64_t cap = (int64_t)sm_count_public() * plane_step_ctas_per_sm();
+    return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
+}  // namespace fs3d

@@ -1,0 +1,59 @@
+// Bit-plane world format: device descriptors and host entry points.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fs3d_common.h"
+
+namespace fs3d {
+
+// One world as the step kernel sees it (device memory, 64 bytes).
+struct PlaneWorld {
+    uint4* rows;      // Y*Z rows of nw uint4 words
+    uint64_t seed;
+    uint64_t t;       // step counter at the start of the current segment
+    int32_t X, Y, Z, nw;
+    int32_t steps;    // steps this world takes in the current segment
+    int32_t lg;       // log2 of the lane-group size (pow2ceil(nw))
+    int32_t pad[4];
+};
+static_assert(sizeof(PlaneWorld) == 64, "PlaneWorld layout");
+
+// Warp-sized work item: 32 >> lg block row-pairs of one world.
+struct PlaneItem {
+    int32_t world;
+    int32_t rp0;
+};
+
+inline int plane_nw(int X) { return (X + 63) / 64; }
+inline size_t plane_bytes(int X, int Y, int Z) { return (size_t)Y * Z * plane_nw(X) * sizeof(uint4); }
+constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
+
+int plane_lg(int nw);
+int plane_items_for(int Y, int Z, int nw);
+int plane_step_grid(int64_t n_items);
+int plane_step_ctas_per_sm();
+fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows, cudaStream_t st);
+fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, uint8_t* g,
+                            cudaStream_t st);
+fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,
+                              unsigned long long* out_dev, cudaStream_t st);
+fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev, int grid,
+                              int s_seg, cudaStream_t st);
+
+// byte-grid kernels (step_bytes.cu)
+bool rows16_ok(const void* grid, int X);
+fs3d_status launch_step_bytes(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t0, int n_steps,
+                              cudaStream_t st);
+fs3d_status hash_bytes_async(const uint8_t* g, int64_t n, unsigned long long* out_dev, cudaStream_t st);
+int sm_count_public();
+
+// render (render.cu)
+fs3d_status launch_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st);
+fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, const fs3d_camera* cam, int W, int H,
+                                    float* rgba_dev, cudaStream_t st);
+fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
+                                     const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st);
+
+}  // namespace fs3d

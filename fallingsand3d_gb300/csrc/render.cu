@@ -1,0 +1,246 @@
+// Headless render kernels.  Built with --fmad=false: every float expression is
+// a sequence of single IEEE operations (+ - * /, sqrtf correctly rounded), in
+// the same order as the CPU restatement, so frames are reproducible bit for
+// bit on the host.
+//
+//  * k_render_sdf: shaders/fs_raymarch.frag:10-81 as a CUDA kernel, one thread
+//    per pixel: 64-step sphere tracing of a radius-0.5 sphere at the origin,
+//    hit at d < 0.001, bail at t > 1000, central-difference normal (h=0.001),
+//    diffuse = max(0.05, dot(n, normalize(p - light))) (the shader's vector
+//    points away from the light), red surface, black miss, alpha 1.
+//    Ray set-up follows fs_raymarch.vert:30-37 (origin = camPos, aspect =
+//    aspect.x) and the fullscreen quad of renderer.cpp:1253-1267.
+//  * k_render_dda: Amanatides & Woo (1987) traversal of the world grid with
+//    the same ray generation and shading conventions; the face normal of the
+//    entered voxel is shaded with the material's colour.
+#include <math.h>
+#include <stdint.h>
+
+#include "fs3d_common.h"
+#include "planes.h"
+
+namespace fs3d {
+
+struct CamDev {
+    float o[3], f[3], r[3], u[3];
+    float tan_half_fov, aspect;
+    float light[3];
+};
+
+__device__ __forceinline__ float dot3(const float* a, const float* b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a[0], b[0]), __fmul_rn(a[1], b[1])), __fmul_rn(a[2], b[2]));
+}
+__device__ __forceinline__ void normalize3(float* v) {
+    const float len = __fsqrt_rn(dot3(v, v));
+    v[0] = __fdiv_rn(v[0], len);
+    v[1] = __fdiv_rn(v[1], len);
+    v[2] = __fdiv_rn(v[2], len);
+}
+__device__ __forceinline__ void pixel_uv2(int px, int py, int W, int H, float& ux, float& uy) {
+    const float u = __fsub_rn(1.0f, __fdiv_rn(__fadd_rn((float)px, 0.5f), (float)W));
+    const float v = __fdiv_rn(__fadd_rn((float)py, 0.5f), (float)H);
+    ux = __fsub_rn(__fmul_rn(u, 2.0f), 1.0f);
+    uy = __fsub_rn(__fmul_rn(v, 2.0f), 1.0f);
+}
+__device__ __forceinline__ float sdf_world(float x, float y, float z) {
+    return __fsub_rn(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z))), 0.5f);
+}
+
+__global__ void k_render_sdf(CamDev cam, int W, int H, float4* __restrict__ out) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= W || py >= H) return;
+    float ux, uy;
+    pixel_uv2(px, py, W, H, ux, uy);
+    uy = __fmul_rn(uy, __fdiv_rn(1.0f, cam.aspect));
+    float d[3] = {ux, uy, 1.0f};
+    normalize3(d);
+    float col = 0.0f, t = 0.0f;
+    for (int it = 0; it < 64; ++it) {
+        const float p[3] = {__fadd_rn(cam.o[0], __fmul_rn(t, d[0])), __fadd_rn(cam.o[1], __fmul_rn(t, d[1])),
+                            __fadd_rn(cam.o[2], __fmul_rn(t, d[2]))};
+        const float dist = sdf_world(p[0], p[1], p[2]);
+        if (dist < 0.001f) {
+            const float h = 0.001f;
+            float n[3] = {
+                __fsub_rn(sdf_world(__fadd_rn(p[0], h), p[1], p[2]), sdf_world(__fsub_rn(p[0], h), p[1], p[2])),
+                __fsub_rn(sdf_world(p[0], __fadd_rn(p[1], h), p[2]), sdf_world(p[0], __fsub_rn(p[1], h), p[2])),
+                __fsub_rn(sdf_world(p[0], p[1], __fadd_rn(p[2], h)), sdf_world(p[0], p[1], __fsub_rn(p[2], h)))};
+            normalize3(n);
+            float l[3] = {__fsub_rn(p[0], cam.light[0]), __fsub_rn(p[1], cam.light[1]), __fsub_rn(p[2], cam.light[2])};
+            normalize3(l);
+            col = fmaxf(0.05f, dot3(n, l));
+            break;
+        } else if (t > 1000.0f) {
+            break;
+        }
+        t = __fadd_rn(t, dist);
+    }
+    out[(size_t)py * W + px] = make_float4(col, 0.0f, 0.0f, 1.0f);
+}
+
+__constant__ float c_palette[5][3] = {
+    {0.0f, 0.0f, 0.0f}, {0.50f, 0.50f, 0.52f}, {0.86f, 0.74f, 0.46f}, {0.20f, 0.42f, 0.90f}, {0.65f, 0.35f, 0.30f}};
+
+// material lookup: canonical bytes
+struct BytesGrid {
+    const uint8_t* g;
+    int X, Y, Z;
+    __device__ __forceinline__ uint32_t at(int x, int y, int z) const {
+        return g[(int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * y)];
+    }
+};
+
+// material lookup: bit planes (A,B) + optional static byte overlay for solids
+struct PlaneGrid {
+    const uint32_t* p;  // rows of nw x {A even, A odd, B even, B odd}
+    const uint8_t* statics;  // nullable: every solid is stone
+    int X, Y, Z, nw;
+    __device__ __forceinline__ uint32_t at(int x, int y, int z) const {
+        const uint32_t* row = p + (size_t)4 * nw * ((size_t)y * Z + z);
+        const int word = x >> 6, bit = (x >> 1) & 31, odd = x & 1;
+        const uint32_t a = (__ldg(row + 4 * word + odd) >> bit) & 1u;
+        const uint32_t b = (__ldg(row + 4 * word + 2 + odd) >> bit) & 1u;
+        if (a) return b ? 3u : 2u;
+        if (!b) return 0u;
+        return statics ? statics[(int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * y)] : 1u;
+    }
+};
+
+template <class G>
+__global__ void k_render_dda(G grid, CamDev cam, int W, int H, float4* __restrict__ out) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= W || py >= H) return;
+    const int N[3] = {grid.X, grid.Y, grid.Z};
+    float ux, uy;
+    pixel_uv2(px, py, W, H, ux, uy);
+    const float sx = __fmul_rn(__fmul_rn(ux, cam.tan_half_fov), cam.aspect);
+    const float sy = __fmul_rn(uy, cam.tan_half_fov);
+    float d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d[a] = __fadd_rn(__fadd_rn(cam.f[a], __fmul_rn(cam.r[a], sx)), __fmul_rn(cam.u[a], sy));
+    normalize3(d);
+    float4 res = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    float inv[3];
+    float tmin = 0.0f, tmax = INFINITY;
+    int entry_axis = -1;
+    bool miss = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] == 0.0f) {
+            inv[a] = INFINITY;
+            if (cam.o[a] < 0.0f || cam.o[a] >= (float)N[a]) miss = true;
+            continue;
+        }
+        inv[a] = __fdiv_rn(1.0f, d[a]);
+        float t0 = __fmul_rn(__fsub_rn(0.0f, cam.o[a]), inv[a]);
+        float t1 = __fmul_rn(__fsub_rn((float)N[a], cam.o[a]), inv[a]);
+        if (t0 > t1) {
+            const float tmp = t0;
+            t0 = t1;
+            t1 = tmp;
+        }
+        if (t0 > tmin) {
+            tmin = t0;
+            entry_axis = a;
+        }
+        if (t1 < tmax) tmax = t1;
+    }
+    if (!miss && tmin <= tmax) {
+        int v[3], step[3];
+        float tmx[3], tdl[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float p = __fadd_rn(cam.o[a], __fmul_rn(d[a], tmin));
+            int c = (int)floorf(p);
+            c = c < 0 ? 0 : (c > N[a] - 1 ? N[a] - 1 : c);
+            v[a] = c;
+            step[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
+            if (d[a] == 0.0f) {
+                tmx[a] = INFINITY;
+                tdl[a] = INFINITY;
+            } else {
+                tmx[a] = __fmul_rn(__fsub_rn((float)(c + (step[a] > 0 ? 1 : 0)), cam.o[a]), inv[a]);
+                tdl[a] = fabsf(inv[a]);
+            }
+        }
+        int last = entry_axis;
+        float tcur = tmin;
+        const int max_iter = N[0] + N[1] + N[2] + 3;
+        for (int it = 0; it < max_iter; ++it) {
+            const uint32_t m = grid.at(v[0], v[1], v[2]);
+            if (m != 0u) {
+                float n[3] = {0.0f, 0.0f, 0.0f};
+                if (last >= 0) n[last] = step[last] > 0 ? -1.0f : 1.0f;
+                float l[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) l[a] = __fsub_rn(__fadd_rn(cam.o[a], __fmul_rn(d[a], tcur)), cam.light[a]);
+                normalize3(l);
+                const float diff = fmaxf(0.05f, dot3(n, l));
+                const int ci = m < 4u ? (int)m : 4;
+                res = make_float4(__fmul_rn(c_palette[ci][0], diff), __fmul_rn(c_palette[ci][1], diff),
+                                  __fmul_rn(c_palette[ci][2], diff), 1.0f);
+                break;
+            }
+            int a;
+            if (tmx[0] < tmx[1])
+                a = tmx[0] < tmx[2] ? 0 : 2;
+            else
+                a = tmx[1] < tmx[2] ? 1 : 2;
+            tcur = tmx[a];
+            v[a] += step[a];
+            if (v[a] < 0 || v[a] >= N[a]) break;
+            tmx[a] = __fadd_rn(tmx[a], tdl[a]);
+            last = a;
+        }
+    }
+    out[(size_t)py * W + px] = res;
+}
+
+static CamDev to_dev(const fs3d_camera* c) {
+    CamDev d;
+    for (int a = 0; a < 3; ++a) {
+        d.o[a] = c->origin[a];
+        d.f[a] = c->forward[a];
+        d.r[a] = c->right[a];
+        d.u[a] = c->up[a];
+        d.light[a] = c->light_pos[a];
+    }
+    d.tan_half_fov = c->tan_half_fov;
+    d.aspect = c->aspect;
+    return d;
+}
+
+fs3d_status launch_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st) {
+    const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+    k_render_sdf<<<grd, blk, 0, st>>>(to_dev(cam), W, H, reinterpret_cast<float4*>(rgba_dev));
+    FS3D_CHECK_LAUNCH("render sdf launch");
+    return FS3D_OK;
+}
+
+fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, const fs3d_camera* cam, int W, int H,
+                                    float* rgba_dev, cudaStream_t st) {
+    const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+    k_render_dda<BytesGrid><<<grd, blk, 0, st>>>(BytesGrid{g, X, Y, Z}, to_dev(cam), W, H,
+                                                 reinterpret_cast<float4*>(rgba_dev));
+    FS3D_CHECK_LAUNCH("render dda launch");
+    return FS3D_OK;
+}
+
+fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
+                                     const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st) {
+    const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+    k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw}, to_dev(cam), W, H,
+                                                 reinterpret_cast<float4*>(rgba_dev));
+    FS3D_CHECK_LAUNCH("render dda (planes) launch");
+    return FS3D_OK;
+}
+
+}  // namespace fs3d
+
+extern "C" fs3d_status fs3d_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_dev, void* stream) {
+    if (!cam || !rgba_dev || W <= 0 || H <= 0)
+        return fs3d::set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_sdf: bad args");
+    return fs3d::launch_render_sdf(cam, W, H, rgba_dev, (cudaStream_t)stream);
+}

@@ -1,0 +1,204 @@
+// Device-side FS3D-rule v1: the scalar per-block rule (bytes) and the
+// bit-sliced rule that runs 32 blocks per 32-bit word (bit planes).
+#pragma once
+
+#include <stdint.h>
+
+#include "fs3d_common.h"
+
+namespace fs3d {
+
+__device__ __forceinline__ uint32_t draw_dev(uint32_t n, uint32_t rk, uint32_t i, uint32_t s) {
+    if (n < 2u) return 0u;
+    const uint32_t g = i >> 5, b = i & 31u;
+    if (n == 2u) return (plane(rk, g, s, 0u) >> b) & 1u;
+    uint32_t u = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < 8u; ++w) u |= ((plane(rk, g, s, w) >> b) & 1u) << w;
+    return u < 85u ? 0u : (u < 170u ? 1u : 2u);
+}
+
+__device__ __forceinline__ uint32_t has_zero_byte(uint32_t v) {
+    return (v - 0x01010101u) & ~v & 0x80808080u;
+}
+
+// Can the block (top layer T, bottom layer B; byte q = column q, cells outside
+// the grid hold 1) change?  Exact, by the stability property of the rule.
+__device__ __forceinline__ bool block_can_move(uint32_t T, uint32_t B) {
+    const uint32_t eT = has_zero_byte(T), eB = has_zero_byte(B);
+    const uint32_t pT = has_zero_byte((T & 0xFEFEFEFEu) ^ 0x02020202u);
+    const uint32_t wT = has_zero_byte(T ^ 0x03030303u), wB = has_zero_byte(B ^ 0x03030303u);
+    return (pT && eB) || (wT && eT) || (wB && eB);
+}
+
+__device__ __forceinline__ uint32_t get_byte(uint64_t V, int s) { return (uint32_t)(V >> (8 * s)) & 0xFFu; }
+
+// Runs the rule on one block held as 8 bytes (byte s = slot s; slots 0-3 top
+// layer, 4-7 bottom layer, column q = dz*2+dx).  Returns the new bytes.
+__device__ __forceinline__ uint64_t block_rule(uint64_t V, uint32_t rk, uint32_t i) {
+    uint32_t moved = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t m = get_byte(V, s);
+        if ((m != 2u && m != 3u) || ((moved >> s) & 1u)) continue;
+        const int q = s & 3;
+        int dst = -1;
+        if (s < 4) {
+            if (get_byte(V, 4 + q) == 0u) {
+                dst = 4 + q;
+            } else {
+                uint32_t cand = 0;
+#pragma unroll
+                for (int q2 = 0; q2 < 4; ++q2)
+                    if (q2 != q && get_byte(V, 4 + q2) == 0u) cand |= 1u << (4 + q2);
+                if (cand) {
+                    uint32_t r = draw_dev(__popc(cand), rk, i, (uint32_t)s);
+                    while (r--) cand &= cand - 1u;
+                    dst = __ffs(cand) - 1;
+                }
+            }
+        }
+        if (dst < 0 && m == 3u) {
+            const int base = s & 4;
+            uint32_t cand = 0;
+#pragma unroll
+            for (int q2 = 0; q2 < 4; ++q2)
+                if (q2 != q && get_byte(V, base + q2) == 0u) cand |= 1u << (base + q2);
+            if (cand) {
+                uint32_t r = draw_dev(__popc(cand), rk, i, (uint32_t)s);
+                while (r--) cand &= cand - 1u;
+                dst = __ffs(cand) - 1;
+            }
+        }
+        if (dst >= 0) {
+            V &= ~(0xFFull << (8 * s));
+            V = (V & ~(0xFFull << (8 * dst))) | ((uint64_t)m << (8 * dst));
+            moved |= 1u << dst;
+        }
+    }
+    return V;
+}
+
+
+// ---------------------------------------------------------------------------
+// Bit-sliced rule.  Each 32-bit word holds one predicate for 32 consecutive
+// blocks i = 32g .. 32g+31 of a block row (bit i & 31).  Per slot s the input
+// is (A, B): (0,0) empty, (0,1) solid, (1,0) sand, (1,1) water.
+// ---------------------------------------------------------------------------
+
+// bit-sliced u < c for the 8-bit numbers u whose bit w is plane p[w]
+template <uint32_t C>
+__device__ __forceinline__ uint32_t lt_const(const uint32_t (&p)[8]) {
+    uint32_t lt = 0, eq = 0xFFFFFFFFu;
+#pragma unroll
+    for (int w = 7; w >= 0; --w) {
+        if ((C >> w) & 1u) {
+            lt |= eq & ~p[w];
+            eq &= p[w];
+        } else {
+            eq &= ~p[w];
+        }
+    }
+    return lt;
+}
+
+// Chooses among up to three ordered candidate masks c1..c3 for the blocks in
+// `mov`; r = draw(n) from the slot's random words.  Outputs destination masks.
+__device__ __forceinline__ void bs_select(uint32_t mov, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t rk,
+                                          uint32_t g, uint32_t s, uint32_t& d1, uint32_t& d2, uint32_t& d3) {
+    const uint32_t two = (c1 & c2) | (c1 & c3) | (c2 & c3);
+    const uint32_t three = c1 & c2 & c3;
+    uint32_t r1 = 0, r2 = 0;
+    if (mov & two) {
+        const uint32_t p0 = plane(rk, g, s, 0u);
+        r1 = p0 & two & ~three;
+        if (mov & three) {
+            uint32_t p[8];
+            p[0] = p0;
+#pragma unroll
+            for (uint32_t w = 1; w < 8u; ++w) p[w] = plane(rk, g, s, w);
+            const uint32_t lt85 = lt_const<85u>(p), lt170 = lt_const<170u>(p);
+            r1 |= three & ~lt85 & lt170;
+            r2 = three & ~lt170;
+        }
+    }
+    const uint32_t r0 = ~(r1 | r2);
+    d1 = mov & r0 & c1;
+    d2 = mov & ((r0 & ~c1 & c2) | (r1 & c1 & c2));
+    d3 = mov & ((r0 & ~c1 & ~c2 & c3) | (r1 & c3 & (c1 ^ c2)) | r2);
+}
+
+// The three other columns of q, in increasing order.
+__host__ __device__ constexpr int other_col(int q, int n) { return n < q ? n : n + 1; }
+
+// Runs one step of the rule on 32 blocks.  A[s], B[s] in/out per slot s.
+// Returns the mask of blocks that changed.
+__device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], uint32_t rk, uint32_t g) {
+    uint32_t P[8], W[8], E[8], M[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        P[s] = A[s];
+        W[s] = A[s] & B[s];
+        E[s] = ~(A[s] | B[s]);
+        M[s] = 0u;
+    }
+    const uint32_t etop = E[0] | E[1] | E[2] | E[3], ebot = E[4] | E[5] | E[6] | E[7];
+    const uint32_t active = ((P[0] | P[1] | P[2] | P[3]) & ebot) | ((W[0] | W[1] | W[2] | W[3]) & etop) |
+                            ((W[4] | W[5] | W[6] | W[7]) & ebot);
+    if (!active) return 0u;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int q = s & 3, base = s & 4;
+        const uint32_t act = P[s] & ~M[s] & active;
+        if (!act) continue;
+        uint32_t fall = 0, dg1 = 0, dg2 = 0, dg3 = 0, side;
+        if (s < 4) {
+            const int b = 4 + q;
+            fall = act & E[b];
+            const uint32_t rest = act & ~E[b];
+            const uint32_t c1 = E[4 + other_col(q, 0)], c2 = E[4 + other_col(q, 1)], c3 = E[4 + other_col(q, 2)];
+            const uint32_t any = c1 | c2 | c3;
+            bs_select(rest & any, c1, c2, c3, rk, g, (uint32_t)s, dg1, dg2, dg3);
+            side = rest & ~any & W[s];
+        } else {
+            side = act & W[s];
+        }
+        const uint32_t e1 = E[base + other_col(q, 0)], e2 = E[base + other_col(q, 1)],
+                       e3 = E[base + other_col(q, 2)];
+        uint32_t sd1 = 0, sd2 = 0, sd3 = 0;
+        const uint32_t smov = side & (e1 | e2 | e3);
+        if (smov) bs_select(smov, e1, e2, e3, rk, g, (uint32_t)s, sd1, sd2, sd3);
+        const uint32_t moved = fall | dg1 | dg2 | dg3 | smov;
+        if (!moved) continue;
+        const uint32_t wat = W[s];
+        P[s] &= ~moved;
+        W[s] &= ~moved;
+        E[s] |= moved;
+        auto put = [&](int t, uint32_t m) {
+            E[t] &= ~m;
+            P[t] |= m;
+            W[t] |= m & wat;
+            M[t] |= m;
+        };
+        if (s < 4) {
+            put(4 + q, fall);
+            put(4 + other_col(q, 0), dg1);
+            put(4 + other_col(q, 1), dg2);
+            put(4 + other_col(q, 2), dg3);
+        }
+        put(base + other_col(q, 0), sd1);
+        put(base + other_col(q, 1), sd2);
+        put(base + other_col(q, 2), sd3);
+    }
+    uint32_t changed = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t nA = P[s], nB = W[s] | (~P[s] & ~E[s]);
+        changed |= (nA ^ A[s]) | (nB ^ B[s]);
+        A[s] = nA;
+        B[s] = nB;
+    }
+    return changed;
+}
+
+}  // namespace fs3d

@@ -1,0 +1,178 @@
+/*
+ * fs3d — C ABI of the GB300 falling-sand voxel engine (libfs3d.so).
+ *
+ * The upstream engine (FallingSand3D) exposes only C++ classes:
+ *   VulkanEngine::{init,run,cleanup}           src/engine/engine.h:16-35
+ *   Renderer::{init,draw,cleanup,...}          src/engine/rendering/renderer.h:81-95
+ * and has no world/step interface, no plugin layer and no FFI.  Its main loop
+ * (src/engine/engine.cpp:54-74) polls events and draws; a world step belongs
+ * between handleEvents() and draw() (engine.cpp:60-68).  This header is the
+ * boundary such a caller binds: plain pointers and sizes, status codes, no
+ * exceptions, no torch or CUDA types (streams travel as void*).
+ *
+ * The rule is FS3D-rule v1:
+ *   grid uint8, idx = x + X*(z + Z*y), gravity -y; 0 empty, 1 stone, 2 sand,
+ *   3 water, >= 4 static solid; outside the grid is solid.  Step t uses
+ *   Margolus 2x2x2 blocks with min corner (2i-o, 2j-o, 2k-o), o = t & 1.  In
+ *   each block, slots are visited top layer first; a sand/water particle that
+ *   has not moved falls straight down, else slides diagonally down into a
+ *   random empty bottom cell, else (water only) moves sideways into a random
+ *   empty cell of its layer.  Random choices come from a counter-based hash of
+ *   (seed, t, block), so every implementation is bit-identical.
+ *
+ * Threading: a handle is used by one thread at a time; different handles may
+ * be used concurrently.  Each world / batch owns one CUDA stream.
+ */
+#ifndef FS3D_H
+#define FS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS3D_ABI_VERSION 1
+
+typedef int fs3d_status;
+#define FS3D_OK 0
+#define FS3D_ERR_INVALID_ARG (-1)
+#define FS3D_ERR_OOM (-2)
+#define FS3D_ERR_BUDGET (-3)
+#define FS3D_ERR_CUDA (-4)
+#define FS3D_ERR_TIMEOUT (-5)
+#define FS3D_ERR_MISMATCH (-6)
+#define FS3D_ERR_STATE (-7)
+#define FS3D_ERR_NOT_FOUND (-8)
+#define FS3D_ERR_IO (-9)
+
+/* world storage layouts */
+#define FS3D_LAYOUT_BYTES 0  /* dense uint8, canonical index order            */
+#define FS3D_LAYOUT_PLANES 1 /* 2 bits per cell, bit planes (see fs3d_world_device_ptr) */
+
+/* render modes */
+#define FS3D_RENDER_DDA 0        /* voxel grid traversal of the world          */
+#define FS3D_RENDER_SDF_SPHERE 1 /* restatement of shaders/fs_raymarch.frag    */
+
+typedef struct fs3d_world fs3d_world;
+typedef struct fs3d_batch fs3d_batch;
+
+/* Pinhole camera.  Ray for pixel (px,py) of a W x H image (row 0 = top):
+ *   u = 1 - (px+0.5)/W, v = (py+0.5)/H, (ux,uy) = (2u-1, 2v-1)
+ *   DDA: dir = normalize(forward + right*(ux*tan_half_fov*aspect) + up*(uy*tan_half_fov))
+ *   SDF: dir = normalize(ux, uy*(1/aspect), 1), as fs_raymarch.frag:67-81. */
+typedef struct fs3d_camera {
+    float origin[3];
+    float forward[3];
+    float right[3];
+    float up[3];
+    float tan_half_fov;
+    float aspect;
+    float light_pos[3];
+    int32_t reserved;
+} fs3d_camera;
+
+typedef struct fs3d_config {
+    int steps_per_segment; /* steps per segment (graph length); default 64          */
+    int ctas_per_sm;       /* persistent grid of the step kernel; 0 = all resident  */
+    int use_graphs;        /* 1 (default) = run each segment as one CUDA graph       */
+    int reserved[13];
+} fs3d_config;
+
+/* ---- library ---- */
+int fs3d_abi_version(void);
+const char* fs3d_status_string(fs3d_status s);
+/* message of the last failing call on this thread ("" if none) */
+const char* fs3d_last_error(void);
+/* number of this library's kernels launched so far in this process */
+uint64_t fs3d_kernel_launch_count(void);
+fs3d_config fs3d_default_config(void);
+
+/* ---- drop-in step on a caller-owned device grid --------------------------
+ * Replaces the CPU update of the engine loop (engine.cpp:68 hook point):
+ * advances `grid_dev` (canonical layout, X*Y*Z bytes, device memory) in place
+ * by n_steps steps starting at step t0.  Asynchronous on `stream` (NULL =
+ * legacy default stream).  No device memory is allocated. */
+fs3d_status fs3d_step_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
+                             int n_steps, void* stream);
+/* Same contract, one thread per 2x2x2 block and byte loads: the plain
+ * reference kernel the vectorised one is checked against. */
+fs3d_status fs3d_step_device_simple(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,
+                                    uint64_t t0, int n_steps, void* stream);
+/* Whole-grid hash H = sum_i fmix64(i*256 + v_i) mod 2^64 of a device grid;
+ * synchronous (waits on `stream`). */
+fs3d_status fs3d_hash_device(const uint8_t* grid_dev, int64_t n_cells, void* stream,
+                             uint64_t* out);
+/* Smallest index where two device grids differ, -1 if equal; synchronous. */
+fs3d_status fs3d_first_diff_device(const uint8_t* a_dev, const uint8_t* b_dev, int64_t n_cells,
+                                   void* stream, int64_t* out);
+
+/* ---- world objects (library-owned device state) ---- */
+fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uint64_t seed,
+                              uint64_t start_step, int layout, fs3d_world** out);
+fs3d_status fs3d_world_step(fs3d_world* w, int n_steps);           /* async */
+fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns);     /* bounded wait */
+fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* grid_host_out); /* canonical layout */
+fs3d_status fs3d_world_write(fs3d_world* w, const uint8_t* grid_host); /* replace contents */
+fs3d_status fs3d_world_hash(fs3d_world* w, uint64_t* out);
+fs3d_status fs3d_world_info(const fs3d_world* w, int* X, int* Y, int* Z, uint64_t* seed,
+                            uint64_t* step, int* layout);
+/* Device pointer of the current state.  BYTES: X*Y*Z canonical bytes.
+ * PLANES: rows r = y*Z + z of nw = ceil(X/64) groups of four uint32 words
+ * {A even, A odd, B even, B odd}; in group g, bit m of an even word is
+ * x = 64g + 2m and of an odd word x = 64g + 2m + 1; (A,B) = (0,0) empty,
+ * (0,1) solid, (1,0) sand, (1,1) water; cells past X are solid. */
+fs3d_status fs3d_world_device_ptr(fs3d_world* w, const void** dev, int* layout);
+fs3d_status fs3d_world_stream(fs3d_world* w, void** stream);
+fs3d_status fs3d_world_destroy(fs3d_world* w);
+/* checkpoint: header {magic "FS3DCKP1", version, X, Y, Z, seed, step} + dense grid */
+fs3d_status fs3d_world_save(fs3d_world* w, const char* path);
+fs3d_status fs3d_world_load(const char* path, int layout, fs3d_world** out);
+
+/* ---- batch / serving pool ----
+ * Worlds of any size share one device pool in the PLANES layout.  Each
+ * admitted world has its own step counter and step budget; run_segment
+ * advances every live world by min(steps_per_segment, steps left).  Worlds
+ * may be admitted and retired between segments. */
+fs3d_status fs3d_batch_create(size_t hbm_budget_bytes, const fs3d_config* cfg, fs3d_batch** out);
+/* FS3D_ERR_BUDGET if the world does not fit in the budget right now */
+fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* grid_host, int X, int Y, int Z,
+                             uint64_t seed, uint64_t start_step, int64_t n_steps,
+                             uint64_t* ticket);
+fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream */
+fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
+/* done = 1 once the world has taken all its steps; hash valid when done */
+fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash);
+/* frees the world's pool space; grid_out (nullable) receives the final grid */
+fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out);
+fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells,
+                             size_t* bytes_used, size_t* bytes_budget);
+fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream);
+fs3d_status fs3d_batch_destroy(fs3d_batch* b);
+
+/* ---- render (headless) ----
+ * Writes W*H RGBA float32 pixels (row 0 = top).  out_on_device = 1: `rgba`
+ * is a device pointer (async on the world's stream); 0: host pointer
+ * (synchronous).  SDF_SPHERE ignores the world's contents (world may be NULL
+ * when out_on_device = 1 and `stream` is given via fs3d_render_sdf). */
+fs3d_status fs3d_render(fs3d_world* w, const fs3d_camera* cam, int W, int H, int mode,
+                        float* rgba, int out_on_device);
+fs3d_status fs3d_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_dev, void* stream);
+/* Camera presets: the fs_raymarch defaults (camPos (0,0,-5), aspect 1700/900,
+ * light (2,5,3)) and the large-world view (origin (-X/4, 0.9Y, -Z/4) looking
+ * at the centre, vertical FOV 70 degrees, aspect W/H). */
+void fs3d_camera_fs_raymarch(fs3d_camera* cam);
+void fs3d_camera_world_view(fs3d_camera* cam, int X, int Y, int Z, int W, int H);
+
+/* ---- synthetic worlds (seeded, bit-reproducible) ---- */
+fs3d_status fs3d_gen_parity(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);
+fs3d_status fs3d_gen_pillars(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);
+fs3d_status fs3d_gen_batch_dims(uint64_t master, int count, int* dims, uint64_t* seeds);
+fs3d_status fs3d_gen_batch_world(uint64_t world_seed, int X, int Y, int Z, uint8_t* grid_host);
+fs3d_status fs3d_gen_dunes(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FS3D_H */

@@ -1,0 +1,626 @@
+/*
+ * fs3d oracle — CPU restatement (test infrastructure only; see fs3d_oracle.h).
+ *
+ * FS3D-rule v1 — the voxel update step, stated in full
+ * ----------------------------------------------------
+ * State.  A world is a dense uint8 grid of X*Y*Z cells, idx = x + X*(z + Z*y),
+ *   gravity along -y.  0 EMPTY, 1 STONE, 2 SAND, 3 WATER; every value >= 4 is
+ *   static and solid.  Cells outside the grid are solid and never written.
+ *
+ * Partition.  Step t (a per-world 64-bit counter) uses offset o = t & 1 on all
+ *   three axes.  Blocks are 2x2x2 with lattice index (i,j,k), min corner
+ *   (bx,by,bz) = (2i-o, 2j-o, 2k-o), i in [0, (X+o+1)/2) and likewise for j
+ *   (over Y) and k (over Z).  Partial blocks at the faces are included; their
+ *   missing cells are solid.  Blocks are disjoint, so they may be visited in
+ *   any order; the canonical order is j, then k, then i.
+ *
+ * Slots.  Slot s in 0..7 is visited in increasing s.  L = s>>2 is the layer
+ *   (0 = top, dy=1; 1 = bottom, dy=0), q = s&3 the column, dz = q>>1, dx = q&1.
+ *   Every slot holding SAND or WATER that has not yet moved in this block tries:
+ *   (a) top layer only: straight down into the bottom cell of its column, if
+ *       that cell is EMPTY;
+ *   (b) top layer only: diagonal-down: candidates are the other three bottom
+ *       cells that are EMPTY, in increasing column order;
+ *   (c) WATER only, either layer, only if (a) and (b) found nothing: sideways:
+ *       candidates are the other three cells of its own layer that are EMPTY.
+ *   With n candidates the r-th is taken, r = draw(n).  A move swaps the
+ *   particle with the EMPTY cell and marks the destination as moved.  Sand
+ *   never displaces water.
+ *
+ * Randomness (counter-based, shared by CPU and GPU):
+ *   sk  = stepkey(seed, t)  = fmix32 chain over 0x243F6A88, seed_lo, seed_hi,
+ *                             t_lo, t_hi
+ *   rk  = rowkey(sk, j, k)  = fmix32(fmix32(sk ^ 0x85EBCA77*(j+1)) ^ 0xC2B2AE3D*(k+1))
+ *   P_w = plane(rk, g, s, w) = fmix32(rk + 0x9E3779B9*(1 + w + 8s + 64g))
+ *   For block i let g = i>>5, b = i&31 and p_w = bit b of P_w.
+ *   draw(1) = 0;  draw(2) = p_0;
+ *   draw(3): u = sum_w p_w << w (w = 0..7); r = u<85 ? 0 : (u<170 ? 1 : 2).
+ *   fmix32 / fmix64 are the MurmurHash3 finalizers (Appleby, public domain).
+ *   Every draw depends only on the world's seed, its step and the block, so a
+ *   world's trajectory does not depend on where or with whom it is stepped.
+ *
+ * Stability.  A block changes under a step iff some SAND/WATER slot has a
+ *   non-empty candidate set when visited; the first such slot sees the
+ *   block's initial state, so "the block does not change" does not depend on
+ *   the random draws.  (The first move puts a particle into a cell that was
+ *   EMPTY at the start; a moved particle never moves again, so the block ends
+ *   different from how it started.)
+ *
+ * Whole-grid hash: H = sum_i fmix64(i*256 + v_i) mod 2^64 (order-free).
+ */
+#include "fs3d_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* primitives                                                          */
+/* ------------------------------------------------------------------ */
+uint32_t orc_fmix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+uint64_t orc_fmix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdULL;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ULL;
+    k ^= k >> 33;
+    return k;
+}
+
+uint32_t orc_stepkey(uint64_t seed, uint64_t t) {
+    uint32_t h = orc_fmix32(0x243F6A88u ^ (uint32_t)seed);
+    h = orc_fmix32(h ^ (uint32_t)(seed >> 32));
+    h = orc_fmix32(h ^ (uint32_t)t);
+    h = orc_fmix32(h ^ (uint32_t)(t >> 32));
+    return h;
+}
+
+uint32_t orc_rowkey(uint32_t sk, uint32_t j, uint32_t k) {
+    uint32_t h = orc_fmix32(sk ^ (0x85EBCA77u * (j + 1u)));
+    return orc_fmix32(h ^ (0xC2B2AE3Du * (k + 1u)));
+}
+
+uint32_t orc_plane(uint32_t rk, uint32_t g, uint32_t s, uint32_t w) {
+    return orc_fmix32(rk + 0x9E3779B9u * (1u + w + 8u * s + 64u * g));
+}
+
+/* PCG32 XSH-RR 64/32 (O'Neill 2014, pcg32_srandom_r / pcg32_random_r /
+ * pcg32_boundedrand_r as published). */
+uint32_t orc_pcg32_next(orc_pcg32* r) {
+    uint64_t old = r->state;
+    r->state = old * 6364136223846793005ULL + r->inc;
+    uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((0u - rot) & 31u));
+}
+
+void orc_pcg32_seed(orc_pcg32* r, uint64_t initstate, uint64_t initseq) {
+    r->state = 0u;
+    r->inc = (initseq << 1u) | 1u;
+    orc_pcg32_next(r);
+    r->state += initstate;
+    orc_pcg32_next(r);
+}
+
+uint32_t orc_pcg32_bounded(orc_pcg32* r, uint32_t bound) {
+    uint32_t threshold = (0u - bound) % bound;
+    for (;;) {
+        uint32_t v = orc_pcg32_next(r);
+        if (v >= threshold) return v % bound;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* the step                                                            */
+/* ------------------------------------------------------------------ */
+static int draw(int n, uint32_t rk, int i, int s) {
+    if (n <= 1) return 0;
+    uint32_t g = (uint32_t)i >> 5, b = (uint32_t)i & 31u;
+    if (n == 2) return (int)((orc_plane(rk, g, (uint32_t)s, 0) >> b) & 1u);
+    uint32_t u = 0;
+    for (uint32_t w = 0; w < 8; ++w) u |= ((orc_plane(rk, g, (uint32_t)s, w) >> b) & 1u) << w;
+    return u < 85u ? 0 : (u < 170u ? 1 : 2);
+}
+
+/* Update block (i,j,k) of step t in place.  Returns 1 if anything moved. */
+static int block_update(uint8_t* grid, int X, int Y, int Z, int o, uint32_t rk, int i, int j,
+                        int k, int dry) {
+    const int bx = 2 * i - o, by = 2 * j - o, bz = 2 * k - o;
+    int64_t idx[8];
+    int inb[8];
+    uint8_t v[8];
+    for (int s = 0; s < 8; ++s) {
+        const int L = s >> 2, q = s & 3;
+        const int x = bx + (q & 1), y = by + (1 - L), z = bz + (q >> 1);
+        inb[s] = (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z);
+        idx[s] = inb[s] ? (int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * (int64_t)y) : -1;
+        v[s] = inb[s] ? grid[idx[s]] : (uint8_t)1; /* out of bounds acts as solid */
+    }
+    unsigned moved = 0;
+    int changed = 0;
+    for (int s = 0; s < 8; ++s) {
+        const uint8_t m = v[s];
+        if (!(m == 2 || m == 3) || ((moved >> s) & 1u)) continue;
+        const int q = s & 3;
+        int dst = -1;
+        int cand[3], n;
+        if (s < 4) {
+            if (v[4 + q] == 0 && inb[4 + q]) {
+                dst = 4 + q;
+            } else {
+                n = 0;
+                for (int q2 = 0; q2 < 4; ++q2)
+                    if (q2 != q && inb[4 + q2] && v[4 + q2] == 0) cand[n++] = 4 + q2;
+                if (n) dst = cand[draw(n, rk, i, s)];
+            }
+        }
+        if (dst < 0 && m == 3) {
+            const int base = s & 4;
+            n = 0;
+            for (int q2 = 0; q2 < 4; ++q2)
+                if (q2 != q && inb[base + q2] && v[base + q2] == 0) cand[n++] = base + q2;
+            if (n) dst = cand[draw(n, rk, i, s)];
+        }
+        if (dst >= 0) {
+            if (dry) return 1;
+            v[dst] = m;
+            v[s] = 0;
+            moved |= 1u << dst;
+            changed = 1;
+        }
+    }
+    if (changed)
+        for (int s = 0; s < 8; ++s)
+            if (inb[s]) grid[idx[s]] = v[s];
+    return changed;
+}
+
+static inline int nblocks(int n, int o) { return (n + o + 1) / 2; }
+
+void orc_step(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t) {
+    const int o = (int)(t & 1u);
+    const uint32_t sk = orc_stepkey(seed, t);
+    const int NBX = nblocks(X, o), NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
+    for (int j = 0; j < NBY; ++j)
+        for (int k = 0; k < NBZ; ++k) {
+            const uint32_t rk = orc_rowkey(sk, (uint32_t)j, (uint32_t)k);
+            for (int i = 0; i < NBX; ++i) block_update(grid, X, Y, Z, o, rk, i, j, k, 0);
+        }
+}
+
+void orc_step_shuffled(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t,
+                       uint64_t order_seed) {
+    const int o = (int)(t & 1u);
+    const uint32_t sk = orc_stepkey(seed, t);
+    const int NBX = nblocks(X, o), NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
+    const int64_t nb = (int64_t)NBX * NBY * NBZ;
+    int64_t* perm = (int64_t*)malloc(sizeof(int64_t) * (size_t)nb);
+    if (!perm) return;
+    for (int64_t a = 0; a < nb; ++a) perm[a] = a;
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, order_seed, 0x5EEDu);
+    for (int64_t a = nb - 1; a > 0; --a) {
+        uint64_t hi = orc_pcg32_next(&r), lo = orc_pcg32_next(&r);
+        int64_t b = (int64_t)(((hi << 32) | lo) % (uint64_t)(a + 1));
+        int64_t tmp = perm[a];
+        perm[a] = perm[b];
+        perm[b] = tmp;
+    }
+    for (int64_t a = 0; a < nb; ++a) {
+        const int64_t p = perm[a];
+        const int i = (int)(p % NBX);
+        const int k = (int)((p / NBX) % NBZ);
+        const int j = (int)(p / ((int64_t)NBX * NBZ));
+        block_update(grid, X, Y, Z, o, orc_rowkey(sk, (uint32_t)j, (uint32_t)k), i, j, k, 0);
+    }
+    free(perm);
+}
+
+void orc_step_omp(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t, int nthreads) {
+    const int o = (int)(t & 1u);
+    const uint32_t sk = orc_stepkey(seed, t);
+    const int NBX = nblocks(X, o), NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads) collapse(2)
+#else
+    (void)nthreads;
+#endif
+    for (int j = 0; j < NBY; ++j)
+        for (int k = 0; k < NBZ; ++k) {
+            const uint32_t rk = orc_rowkey(sk, (uint32_t)j, (uint32_t)k);
+            for (int i = 0; i < NBX; ++i) block_update(grid, X, Y, Z, o, rk, i, j, k, 0);
+        }
+}
+
+void orc_run(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t0, int n,
+             uint64_t* hashes, int nthreads) {
+    const int64_t cells = (int64_t)X * Y * Z;
+    for (int a = 0; a < n; ++a) {
+        if (nthreads == 1)
+            orc_step(grid, X, Y, Z, seed, t0 + (uint64_t)a);
+        else
+            orc_step_omp(grid, X, Y, Z, seed, t0 + (uint64_t)a, nthreads);
+        if (hashes) hashes[a] = orc_hash(grid, cells);
+    }
+}
+
+int orc_block_would_change(const uint8_t* grid, int X, int Y, int Z, uint64_t t, int i, int j,
+                           int k) {
+    /* dry run: stability does not depend on the draws, so any row key will do */
+    return block_update((uint8_t*)grid, X, Y, Z, (int)(t & 1u), 0u, i, j, k, 1);
+}
+
+/* ------------------------------------------------------------------ */
+/* hash / diff                                                         */
+/* ------------------------------------------------------------------ */
+uint64_t orc_hash(const uint8_t* grid, int64_t n) {
+    uint64_t h = 0;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : h) schedule(static)
+#endif
+    for (int64_t i = 0; i < n; ++i) h += orc_fmix64((uint64_t)i * 256u + grid[i]);
+    return h;
+}
+
+int64_t orc_first_diff(const uint8_t* a, const uint8_t* b, int64_t n) {
+    for (int64_t i = 0; i < n; ++i)
+        if (a[i] != b[i]) return i;
+    return -1;
+}
+
+/* ------------------------------------------------------------------ */
+/* generators                                                          */
+/* ------------------------------------------------------------------ */
+#define THR_P05 214748364u   /* floor(0.05 * 2^32) */
+#define THR_P10 429496729u   /* floor(0.10 * 2^32) */
+#define THR_P20 858993459u   /* floor(0.20 * 2^32) */
+#define THR_P25 1073741824u  /* floor(0.25 * 2^32) */
+#define THR_P30 1288490188u  /* floor(0.30 * 2^32) */
+#define THR_P35 1503238553u  /* floor(0.35 * 2^32) */
+#define THR_P40 1717986918u  /* floor(0.40 * 2^32) */
+
+static inline int64_t cidx(int X, int Z, int x, int y, int z) {
+    return (int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * (int64_t)y);
+}
+
+static void stone_floor(uint8_t* grid, int X, int Y, int Z) {
+    const int64_t layer = (int64_t)X * Z;
+    for (int y = 0; y < 2 && y < Y; ++y) memset(grid + layer * y, 1, (size_t)layer);
+}
+
+/* Parity workload: stone at y<2; for y >= Y/2 each cell iid, drawn in idx
+ * order: sand p=0.25, water p=0.15, else empty. */
+void orc_gen_c1(uint64_t seed, int X, int Y, int Z, uint8_t* grid) {
+    const int64_t n = (int64_t)X * Y * Z, layer = (int64_t)X * Z;
+    memset(grid, 0, (size_t)n);
+    stone_floor(grid, X, Y, Z);
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, seed, 0xC1u);
+    for (int64_t i = layer * (Y / 2); i < n; ++i) {
+        if (grid[i]) continue;
+        uint32_t u = orc_pcg32_next(&r);
+        grid[i] = u < THR_P25 ? 2 : (u < THR_P40 ? 3 : 0);
+    }
+}
+
+/* Pillar workload: stone floor, 256 stone pillars (centre uniform, radius
+ * 2..8, height 10..300), then for y >= ceil(2Y/5) every non-stone cell iid:
+ * sand p=0.30, water p=0.10. */
+void orc_gen_c2(uint64_t seed, int X, int Y, int Z, uint8_t* grid) {
+    const int64_t n = (int64_t)X * Y * Z, layer = (int64_t)X * Z;
+    memset(grid, 0, (size_t)n);
+    stone_floor(grid, X, Y, Z);
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, seed, 0xC2u);
+    for (int p = 0; p < 256; ++p) {
+        const int cx = (int)orc_pcg32_bounded(&r, (uint32_t)X);
+        const int cz = (int)orc_pcg32_bounded(&r, (uint32_t)Z);
+        const int rad = 2 + (int)orc_pcg32_bounded(&r, 7u);
+        const int h = 10 + (int)orc_pcg32_bounded(&r, 291u);
+        const int ytop = (2 + h < Y) ? 2 + h : Y;
+        for (int z = cz - rad; z <= cz + rad; ++z) {
+            if (z < 0 || z >= Z) continue;
+            for (int x = cx - rad; x <= cx + rad; ++x) {
+                if (x < 0 || x >= X) continue;
+                if ((x - cx) * (x - cx) + (z - cz) * (z - cz) > rad * rad) continue;
+                for (int y = 2; y < ytop; ++y) grid[cidx(X, Z, x, y, z)] = 1;
+            }
+        }
+    }
+    const int y0 = (2 * Y + 4) / 5;
+    for (int64_t i = layer * y0; i < n; ++i) {
+        if (grid[i]) continue;
+        uint32_t u = orc_pcg32_next(&r);
+        grid[i] = u < THR_P30 ? 2 : (u < THR_P40 ? 3 : 0);
+    }
+}
+
+/* Mixed-size batch: per world X, Y, Z drawn (in that order) uniformly from
+ * {16,24,32,48,64,96,128} with the master generator; world seed =
+ * fmix64(master ^ world index). */
+void orc_gen_c3_dims(uint64_t master, int count, int* dims, uint64_t* seeds) {
+    static const int choices[7] = {16, 24, 32, 48, 64, 96, 128};
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, master, 0xC3u);
+    for (int w = 0; w < count; ++w) {
+        for (int a = 0; a < 3; ++a) dims[3 * w + a] = choices[orc_pcg32_bounded(&r, 7u)];
+        seeds[w] = orc_fmix64(master ^ (uint64_t)w);
+    }
+}
+
+/* One batch world: sand fraction U[0.05,0.40], water U[0,0.20] (integer
+ * thresholds from two draws), stone at y<2, cells with y >= Y/2 filled iid. */
+void orc_gen_c3_world(uint64_t world_seed, int X, int Y, int Z, uint8_t* grid) {
+    const int64_t n = (int64_t)X * Y * Z, layer = (int64_t)X * Z;
+    memset(grid, 0, (size_t)n);
+    stone_floor(grid, X, Y, Z);
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, world_seed, 0xC3Du);
+    const uint32_t u1 = orc_pcg32_next(&r), u2 = orc_pcg32_next(&r);
+    const uint32_t sand_thr = THR_P05 + (uint32_t)(((uint64_t)u1 * THR_P35) >> 32);
+    const uint32_t water_thr = sand_thr + (uint32_t)(((uint64_t)u2 * THR_P20) >> 32);
+    for (int64_t i = layer * (Y / 2); i < n; ++i) {
+        if (grid[i]) continue;
+        uint32_t u = orc_pcg32_next(&r);
+        grid[i] = u < sand_thr ? 2 : (u < water_thr ? 3 : 0);
+    }
+}
+
+/* Improved noise (Perlin 2002), restated from the published algorithm. */
+static double fade(double t) { return t * t * t * (t * (t * 6.0 - 15.0) + 10.0); }
+static double lerp_d(double t, double a, double b) { return a + t * (b - a); }
+static double grad(int hash, double x, double y, double z) {
+    const int h = hash & 15;
+    const double u = h < 8 ? x : y;
+    const double v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+}
+
+double orc_perlin(const uint8_t* p, double x, double y, double z) {
+    const double fx = floor(x), fy = floor(y), fz = floor(z);
+    const int X = (int)fx & 255, Y = (int)fy & 255, Z = (int)fz & 255;
+    x -= fx;
+    y -= fy;
+    z -= fz;
+    const double u = fade(x), v = fade(y), w = fade(z);
+    const int A = p[X] + Y, AA = p[A] + Z, AB = p[A + 1] + Z;
+    const int B = p[X + 1] + Y, BA = p[B] + Z, BB = p[B + 1] + Z;
+    const double x1 = lerp_d(u, grad(p[AA], x, y, z), grad(p[BA], x - 1, y, z));
+    const double x2 = lerp_d(u, grad(p[AB], x, y - 1, z), grad(p[BB], x - 1, y - 1, z));
+    const double x3 = lerp_d(u, grad(p[AA + 1], x, y, z - 1), grad(p[BA + 1], x - 1, y, z - 1));
+    const double x4 =
+        lerp_d(u, grad(p[AB + 1], x, y - 1, z - 1), grad(p[BB + 1], x - 1, y - 1, z - 1));
+    return lerp_d(w, lerp_d(v, x1, x2), lerp_d(v, x3, x4));
+}
+
+/* Dune world: height h(x,z) = clamp(round(0.3*Y*(0.5+0.5*fbm)), 0, Y) with a
+ * 4-octave fbm (lacunarity 2, gain 0.5, normalised by the amplitude sum) of
+ * improved noise at (x/256, 0.5, z/256) over a seeded permutation; sand for
+ * y < h, water iid p=0.1 (drawn in idx order) for y >= h. */
+void orc_gen_c5(uint64_t seed, int X, int Y, int Z, uint8_t* grid) {
+    uint8_t perm[512];
+    orc_pcg32 r;
+    orc_pcg32_seed(&r, seed, 0xC5u);
+    for (int a = 0; a < 256; ++a) perm[a] = (uint8_t)a;
+    for (int a = 255; a > 0; --a) {
+        const int b = (int)orc_pcg32_bounded(&r, (uint32_t)(a + 1));
+        const uint8_t tmp = perm[a];
+        perm[a] = perm[b];
+        perm[b] = tmp;
+    }
+    for (int a = 0; a < 256; ++a) perm[256 + a] = perm[a];
+    int* hf = (int*)malloc(sizeof(int) * (size_t)X * (size_t)Z);
+    if (!hf) return;
+    for (int z = 0; z < Z; ++z)
+        for (int x = 0; x < X; ++x) {
+            double sum = 0.0, amp = 1.0, freq = 1.0, norm = 0.0;
+            for (int oct = 0; oct < 4; ++oct) {
+                sum += amp * orc_perlin(perm, (double)x / 256.0 * freq, 0.5,
+                                        (double)z / 256.0 * freq);
+                norm += amp;
+                amp *= 0.5;
+                freq *= 2.0;
+            }
+            const double fbm = sum / norm;
+            double h = round(0.3 * (double)Y * (0.5 + 0.5 * fbm));
+            if (h < 0.0) h = 0.0;
+            if (h > (double)Y) h = (double)Y;
+            hf[(size_t)z * (size_t)X + (size_t)x] = (int)h;
+        }
+    orc_pcg32 rw;
+    orc_pcg32_seed(&rw, seed, 0xC5Au);
+    for (int y = 0; y < Y; ++y)
+        for (int z = 0; z < Z; ++z) {
+            uint8_t* row = grid + cidx(X, Z, 0, y, z);
+            const int* hrow = hf + (size_t)z * (size_t)X;
+            for (int x = 0; x < X; ++x) {
+                if (y < hrow[x]) {
+                    row[x] = 2;
+                } else {
+                    const uint32_t u = orc_pcg32_next(&rw);
+                    row[x] = u < THR_P10 ? 3 : 0;
+                }
+            }
+        }
+    free(hf);
+}
+
+/* ------------------------------------------------------------------ */
+/* render (build with -ffp-contract=off: every op is a single IEEE op)  */
+/* ------------------------------------------------------------------ */
+static inline float dot3(const float* a, const float* b) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+static inline void normalize3(float* v) {
+    const float len = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] = v[0] / len;
+    v[1] = v[1] / len;
+    v[2] = v[2] / len;
+}
+
+/* pixel -> uv of the fullscreen quad (renderer.cpp:1253-1267): vertex x=+1
+ * carries u=0, x=-1 carries u=1; v grows with NDC y, which points down. */
+static inline void pixel_uv2(int px, int py, int W, int H, float* ux, float* uy) {
+    const float u = 1.0f - ((float)px + 0.5f) / (float)W;
+    const float v = ((float)py + 0.5f) / (float)H;
+    *ux = u * 2.0f - 1.0f;
+    *uy = v * 2.0f - 1.0f;
+}
+
+/* fs_raymarch.frag:10-26 — map_the_world = sphereSDF(p, 0, 0.5) */
+static inline float sdf_world(float x, float y, float z) {
+    return sqrtf(x * x + y * y + z * z) - 0.5f;
+}
+
+void orc_render_sdf(const orc_camera* cam, int W, int H, float* rgba) {
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            float ux, uy;
+            pixel_uv2(px, py, W, H, &ux, &uy);
+            uy = uy * (1.0f / cam->aspect); /* fs_raymarch.frag:72 */
+            float dir[3] = {ux, uy, 1.0f};
+            normalize3(dir);
+            const float* o = cam->origin;
+            float col = 0.0f;
+            float t = 0.0f;
+            for (int it = 0; it < 64; ++it) { /* fs_raymarch.frag:41 */
+                const float p[3] = {o[0] + t * dir[0], o[1] + t * dir[1], o[2] + t * dir[2]};
+                const float d = sdf_world(p[0], p[1], p[2]);
+                if (d < 0.001f) {
+                    const float h = 0.001f; /* calculate_normal, :28-36 */
+                    float n[3] = {
+                        sdf_world(p[0] + h, p[1], p[2]) - sdf_world(p[0] - h, p[1], p[2]),
+                        sdf_world(p[0], p[1] + h, p[2]) - sdf_world(p[0], p[1] - h, p[2]),
+                        sdf_world(p[0], p[1], p[2] + h) - sdf_world(p[0], p[1], p[2] - h)};
+                    normalize3(n);
+                    /* the upstream shader points this vector away from the light */
+                    float l[3] = {p[0] - cam->light_pos[0], p[1] - cam->light_pos[1],
+                                  p[2] - cam->light_pos[2]};
+                    normalize3(l);
+                    col = fmaxf(0.05f, dot3(n, l));
+                    break;
+                } else if (t > 1000.0f) {
+                    break;
+                }
+                t += d;
+            }
+            float* out = rgba + 4 * ((size_t)py * (size_t)W + (size_t)px);
+            out[0] = col;
+            out[1] = 0.0f;
+            out[2] = 0.0f;
+            out[3] = 1.0f;
+        }
+}
+
+static const float k_palette[5][3] = {
+    {0.0f, 0.0f, 0.0f},    /* empty (never shaded) */
+    {0.50f, 0.50f, 0.52f}, /* stone */
+    {0.86f, 0.74f, 0.46f}, /* sand */
+    {0.20f, 0.42f, 0.90f}, /* water */
+    {0.65f, 0.35f, 0.30f}, /* any static material >= 4 */
+};
+
+/* Amanatides & Woo (1987) grid traversal of the uint8 world. */
+void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* cam, int W,
+                    int H, float* rgba) {
+    const int N[3] = {X, Y, Z};
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            float ux, uy;
+            pixel_uv2(px, py, W, H, &ux, &uy);
+            const float sx = ux * cam->tan_half_fov * cam->aspect;
+            const float sy = uy * cam->tan_half_fov;
+            float d[3];
+            for (int a = 0; a < 3; ++a)
+                d[a] = cam->forward[a] + cam->right[a] * sx + cam->up[a] * sy;
+            normalize3(d);
+            const float* o = cam->origin;
+            float out4[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+            float inv[3];
+            float tmin = 0.0f, tmax = INFINITY;
+            int entry_axis = -1, miss = 0;
+            for (int a = 0; a < 3; ++a) {
+                if (d[a] == 0.0f) {
+                    inv[a] = INFINITY;
+                    if (o[a] < 0.0f || o[a] >= (float)N[a]) miss = 1;
+                    continue;
+                }
+                inv[a] = 1.0f / d[a];
+                float t0 = (0.0f - o[a]) * inv[a];
+                float t1 = ((float)N[a] - o[a]) * inv[a];
+                if (t0 > t1) {
+                    const float tmp = t0;
+                    t0 = t1;
+                    t1 = tmp;
+                }
+                if (t0 > tmin) {
+                    tmin = t0;
+                    entry_axis = a;
+                }
+                if (t1 < tmax) tmax = t1;
+            }
+            if (!miss && tmin <= tmax) {
+                int v[3], step[3];
+                float tmx[3], tdl[3];
+                for (int a = 0; a < 3; ++a) {
+                    const float p = o[a] + d[a] * tmin;
+                    int c = (int)floorf(p);
+                    if (c < 0) c = 0;
+                    if (c > N[a] - 1) c = N[a] - 1;
+                    v[a] = c;
+                    step[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
+                    if (d[a] == 0.0f) {
+                        tmx[a] = INFINITY;
+                        tdl[a] = INFINITY;
+                    } else {
+                        tmx[a] = ((float)(c + (step[a] > 0 ? 1 : 0)) - o[a]) * inv[a];
+                        tdl[a] = fabsf(inv[a]);
+                    }
+                }
+                int last = entry_axis;
+                float tcur = tmin;
+                const int max_iter = X + Y + Z + 3;
+                for (int it = 0; it < max_iter; ++it) {
+                    const uint8_t m =
+                        grid[(int64_t)v[0] + (int64_t)X * ((int64_t)v[2] + (int64_t)Z * v[1])];
+                    if (m != 0) {
+                        float n[3] = {0.0f, 0.0f, 0.0f};
+                        if (last >= 0) n[last] = step[last] > 0 ? -1.0f : 1.0f;
+                        float l[3] = {o[0] + d[0] * tcur - cam->light_pos[0],
+                                      o[1] + d[1] * tcur - cam->light_pos[1],
+                                      o[2] + d[2] * tcur - cam->light_pos[2]};
+                        normalize3(l);
+                        const float diff = fmaxf(0.05f, dot3(n, l));
+                        const float* c = k_palette[m < 4 ? m : 4];
+                        out4[0] = c[0] * diff;
+                        out4[1] = c[1] * diff;
+                        out4[2] = c[2] * diff;
+                        break;
+                    }
+                    int a;
+                    if (tmx[0] < tmx[1])
+                        a = tmx[0] < tmx[2] ? 0 : 2;
+                    else
+                        a = tmx[1] < tmx[2] ? 1 : 2;
+                    tcur = tmx[a];
+                    v[a] += step[a];
+                    if (v[a] < 0 || v[a] >= N[a]) break;
+                    tmx[a] += tdl[a];
+                    last = a;
+                }
+            }
+            memcpy(rgba + 4 * ((size_t)py * (size_t)W + (size_t)px), out4, sizeof(out4));
+        }
+}

@@ -1,0 +1,75 @@
+"""CPU checks of the C ABI: the library loads, exports every entry point that
+include/fs3d.h declares, its host-side generators match the oracle's and bad
+arguments come back as status codes (no GPU work is issued here)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    txt = open(os.path.join(ROOT, "include", "fs3d.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fs3d_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_and_binding_agree(fs3d):
+    assert declared_functions() == sorted(fs3d.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(fs3d):
+    L = fs3d.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    assert L.fs3d_abi_version() == 1
+    assert L.fs3d_status_string(-3) == b"over the memory budget"
+
+
+def test_default_config(fs3d):
+    c = fs3d.lib().fs3d_default_config()
+    assert c.steps_per_segment == 64 and c.use_graphs == 1
+
+
+def test_generators_match_oracle(fs3d, orc):
+    for seed in (1, 2):
+        assert (fs3d.gen_parity(seed) == orc.gen_c1(seed)).all()
+    assert (fs3d.gen_pillars(3, 96, 128, 80) == orc.gen_c2(3, 96, 128, 80)).all()
+    assert (fs3d.gen_dunes(4, 96, 80, 64) == orc.gen_c5(4, 96, 80, 64)).all()
+    d1, s1 = fs3d.gen_batch_dims(9, 64)
+    d2, s2 = orc.gen_c3_dims(9, 64)
+    assert (d1 == d2).all() and (s1 == s2).all()
+    for w in range(3):
+        X, Y, Z = (int(v) for v in d1[w])
+        assert (fs3d.gen_batch_world(int(s1[w]), X, Y, Z) == orc.gen_c3_world(int(s2[w]), X, Y, Z)).all()
+
+
+def test_camera_presets(fs3d):
+    c = fs3d.camera_fs_raymarch()
+    assert list(c.origin) == [0.0, 0.0, -5.0] and abs(c.aspect - 1700 / 900) < 1e-6
+    assert list(c.light_pos) == [2.0, 5.0, 3.0]
+    v = fs3d.camera_world_view(1024, 1024, 1024, 1920, 1080)
+    f = np.array(v.forward)
+    assert abs(np.linalg.norm(f) - 1) < 1e-6 and abs(v.tan_half_fov - np.tan(np.radians(35))) < 1e-6
+
+
+def test_bad_arguments_return_status(fs3d):
+    L = fs3d.lib()
+    h = C.c_void_p()
+    g = np.zeros(8, np.uint8)
+    assert L.fs3d_world_create(None, 2, 2, 2, 0, 0, 0, C.byref(h)) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_world_create(g.ctypes.data, 0, 2, 2, 0, 0, 0, C.byref(h)) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_world_create(g.ctypes.data, 2, 2, 2, 0, 0, 7, C.byref(h)) == fs3d.ERR_INVALID_ARG
+    assert b"layout" in L.fs3d_last_error()
+    assert L.fs3d_step_device(None, 2, 2, 2, 0, 0, 1, None) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_world_step(None, 1) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_world_destroy(None) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_batch_admit(None, None, 1, 1, 1, 0, 0, 1, None) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_gen_parity(1, 0, 4, 4, g.ctypes.data) == fs3d.ERR_INVALID_ARG
+    with pytest.raises(fs3d.Fs3dError) as e:
+        fs3d.check(fs3d.ERR_BUDGET)
+    assert e.value.status == fs3d.ERR_BUDGET
+    assert L.fs3d_world_load(b"/nonexistent/ckp", 0, C.byref(h)) == fs3d.ERR_IO

@@ -1,0 +1,120 @@
+"""GPU checks of the batched / served path: many mixed-size worlds in one
+pool, stepped in graph-captured segments, each bit-exact to the oracle and
+identical whether run alone or inside any mix (continuous admission)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GiB = 1 << 30
+
+
+def small_batch(fs3d, master, count, max_dim=64):
+    dims, seeds = fs3d.gen_batch_dims(master, count)
+    dims = np.minimum(dims, max_dim)
+    return [(tuple(int(v) for v in dims[w]), int(seeds[w])) for w in range(count)]
+
+
+def oracle_final(orc, fs3d, dims, seed, n, start=0):
+    X, Y, Z = dims
+    g = fs3d.gen_batch_world(seed, X, Y, Z)
+    orc.run(g, seed, start, n, nthreads=0)
+    return g
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_batch_matches_oracle(fs3d, orc, use_graphs):
+    worlds = small_batch(fs3d, 5, 24, max_dim=128)
+    rng = np.random.default_rng(1)
+    steps = [int(v) for v in rng.integers(1, 150, len(worlds))]
+    with fs3d.Batch(4 * GiB, steps_per_segment=64, use_graphs=use_graphs) as b:
+        tickets = []
+        for (dims, seed), n in zip(worlds, steps):
+            X, Y, Z = dims
+            tickets.append(b.admit(fs3d.gen_batch_world(seed, X, Y, Z), seed, n))
+        for _ in range((max(steps) + 63) // 64):
+            b.run_segment()
+        b.sync()
+        for t, (dims, seed), n in zip(tickets, worlds, steps):
+            done, h = b.poll(t)
+            assert done
+            X, Y, Z = dims
+            exp = oracle_final(orc, fs3d, dims, seed, n)
+            assert h == orc.hash(exp), (dims, seed, n)
+            got = b.retire(t, (Y, Z, X))
+            assert (got == exp).all()
+        assert b.stats()["live_worlds"] == 0 and b.stats()["bytes_used"] == 0
+
+
+def test_mix_equals_alone_with_continuous_admission(fs3d, orc):
+    worlds = small_batch(fs3d, 77, 30, max_dim=96)
+    n = 100
+    # alone: each world in its own batch
+    alone = {}
+    for dims, seed in worlds[:6]:
+        X, Y, Z = dims
+        with fs3d.Batch(GiB, steps_per_segment=32) as b:
+            t = b.admit(fs3d.gen_batch_world(seed, X, Y, Z), seed, n)
+            for _ in range(4):
+                b.run_segment()
+            b.sync()
+            alone[seed] = b.poll(t)[1]
+    # mix: worlds arrive while others are mid-flight, with a start step offset
+    with fs3d.Batch(GiB, steps_per_segment=32) as b:
+        live = {}
+        pending = list(worlds)
+        results = {}
+        seg = 0
+        while pending or live:
+            for _ in range(3):
+                if pending:
+                    dims, seed = pending.pop(0)
+                    X, Y, Z = dims
+                    live[b.admit(fs3d.gen_batch_world(seed, X, Y, Z), seed, n)] = (dims, seed)
+            b.run_segment()
+            seg += 1
+            for t in list(live):
+                done, h = b.poll(t)
+                if done:
+                    results[live.pop(t)[1]] = h
+                    b.retire(t)
+            assert seg < 100
+    for seed, h in alone.items():
+        assert results[seed] == h
+    for dims, seed in worlds[6:12]:
+        assert results[seed] == orc.hash(oracle_final(orc, fs3d, dims, seed, n))
+
+
+def test_budget_admission_and_release(fs3d):
+    g = fs3d.gen_batch_world(1, 64, 64, 64)
+    per = 64 * 64 * 16 + 64  # planes: 64 rows x 64 rows x 16 bytes, plus descriptor
+    with fs3d.Batch(2 * per + 10, steps_per_segment=8) as b:
+        t1 = b.admit(g, 1, 8)
+        t2 = b.admit(g, 2, 8)
+        assert b.try_admit(g, 3, 8) is None
+        with pytest.raises(fs3d.Fs3dError) as e:
+            b.admit(g, 3, 8)
+        assert e.value.status == fs3d.ERR_BUDGET
+        b.run_segment()
+        b.retire(t1)
+        t3 = b.admit(g, 3, 8)
+        b.run_segment()
+        b.sync()
+        assert b.poll(t2)[0] and b.poll(t3)[0]
+        with pytest.raises(fs3d.Fs3dError):
+            b.poll(t1)
+
+
+def test_start_step_offsets_parity(fs3d, orc):
+    dims, seed = (48, 40, 24), 1234
+    X, Y, Z = dims
+    g = fs3d.gen_batch_world(seed, X, Y, Z)
+    with fs3d.Batch(GiB, steps_per_segment=16) as b:
+        t = b.admit(g, seed, 37, start_step=11)
+        for _ in range(3):
+            b.run_segment()
+        b.sync()
+        h = b.poll(t)[1]
+    ref = g.copy()
+    orc.run(ref, seed, 11, 37, nthreads=0)
+    assert h == orc.hash(ref)
