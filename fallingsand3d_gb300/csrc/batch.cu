@@ -184,14 +184,32 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     return FS3D_OK;
 }
 
-fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t seed,
-                             uint64_t start_step, int64_t n_steps, uint64_t* ticket) {
-    if (!b || !g || !ticket || X <= 0 || Y <= 0 || Z <= 0 || X > kPlaneMaxX || Y > 65536 || Z > 65536 ||
-        n_steps < 0)
+}  // extern "C"
+
+namespace {
+
+// any byte >= 4 (a static material that must be kept for read-back)
+bool has_static_material(const uint8_t* g, size_t n) {
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t v;
+        memcpy(&v, g + i, 8);
+        if (v & 0xFCFCFCFCFCFCFCFCull) return true;
+    }
+    for (; i < n; ++i)
+        if (g[i] >= 4) return true;
+    return false;
+}
+
+// Admits a world given as host bytes (g != NULL) or generated on the device
+// from its seed (g == NULL: the mixed-size batch world of that seed).
+fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t seed, uint64_t start_step,
+                  int64_t n_steps, uint64_t* ticket) {
+    if (!b || !ticket || X <= 0 || Y <= 0 || Z <= 0 || X > kPlaneMaxX || Y > 65536 || Z > 65536 || n_steps < 0)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit: bad args (X must be 1..2048)");
+    if (!g && Y < 4) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_generated: needs Y >= 4");
     const size_t n = (size_t)X * Y * Z;
-    bool stat = false;
-    for (size_t i = 0; i < n && !stat; ++i) stat = g[i] >= 4;
+    const bool stat = g ? has_static_material(g, n) : false;
     BWorld w;
     w.X = X;
     w.Y = Y;
@@ -206,13 +224,19 @@ fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int 
         return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
     uint8_t* staging = nullptr;
     FS3D_CUDA(cudaMallocAsync((void**)&w.rows, plane_bytes(X, Y, Z), b->side));
-    cudaError_t e = cudaMallocAsync((void**)&staging, n, b->side);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(staging, g, n, cudaMemcpyHostToDevice, b->side);
-    fs3d_status s = e == cudaSuccess ? planes_from_bytes(staging, X, Y, Z, w.rows, b->side) : cuda_fail(e, "admit upload");
-    if (stat)
-        w.statics = staging;
-    else if (staging)
-        cudaFreeAsync(staging, b->side);
+    fs3d_status s = FS3D_OK;
+    cudaError_t e = cudaSuccess;
+    if (g) {
+        e = cudaMallocAsync((void**)&staging, n, b->side);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(staging, g, n, cudaMemcpyHostToDevice, b->side);
+        s = e == cudaSuccess ? planes_from_bytes(staging, X, Y, Z, w.rows, b->side) : cuda_fail(e, "admit upload");
+        if (stat)
+            w.statics = staging;
+        else if (staging)
+            cudaFreeAsync(staging, b->side);
+    } else {
+        s = planes_generate_batch_world(seed, X, Y, Z, w.rows, b->side);
+    }
     if (s == FS3D_OK) {
         e = cudaEventCreateWithFlags(&w.ready, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(w.ready, b->side);
@@ -228,6 +252,21 @@ fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int 
     *ticket = b->next_ticket++;
     b->worlds.emplace(*ticket, w);
     return FS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t seed,
+                             uint64_t start_step, int64_t n_steps, uint64_t* ticket) {
+    if (!g) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit: NULL grid");
+    return admit(b, g, X, Y, Z, seed, start_step, n_steps, ticket);
+}
+
+fs3d_status fs3d_batch_admit_generated(fs3d_batch* b, int X, int Y, int Z, uint64_t seed, uint64_t start_step,
+                                       int64_t n_steps, uint64_t* ticket) {
+    return admit(b, nullptr, X, Y, Z, seed, start_step, n_steps, ticket);
 }
 
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {

@@ -8,36 +8,18 @@
 #include <vector>
 
 #include "fs3d_common.h"
+#include "pcg.h"
 
 namespace {
 
-struct Pcg32 {
-    uint64_t state = 0, inc = 1;
-    Pcg32(uint64_t initstate, uint64_t initseq) {
-        inc = (initseq << 1u) | 1u;
-        next();
-        state += initstate;
-        next();
-    }
-    uint32_t next() {
-        const uint64_t old = state;
-        state = old * 6364136223846793005ULL + inc;
-        const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
-        const uint32_t rot = (uint32_t)(old >> 59);
-        return (xs >> rot) | (xs << ((0u - rot) & 31u));
-    }
-    uint32_t bounded(uint32_t bound) {
-        const uint32_t threshold = (0u - bound) % bound;
-        for (;;) {
-            const uint32_t v = next();
-            if (v >= threshold) return v % bound;
-        }
-    }
-};
-
-constexpr uint32_t kP05 = 214748364u, kP10 = 429496729u, kP20 = 858993459u,
-                   kP25 = 1073741824u, kP30 = 1288490188u, kP35 = 1503238553u,
-                   kP40 = 1717986918u;
+using fs3d::Pcg32;
+using fs3d::kP05;
+using fs3d::kP10;
+using fs3d::kP20;
+using fs3d::kP25;
+using fs3d::kP30;
+using fs3d::kP35;
+using fs3d::kP40;
 
 bool dims_ok(int X, int Y, int Z, const uint8_t* g) { return g && X > 0 && Y > 0 && Z > 0; }
 
@@ -129,10 +111,11 @@ fs3d_status fs3d_gen_batch_dims(uint64_t master, int count, int* dims, uint64_t*
 fs3d_status fs3d_gen_batch_world(uint64_t world_seed, int X, int Y, int Z, uint8_t* g) {
     if (!dims_ok(X, Y, Z, g)) return fs3d::set_error(FS3D_ERR_INVALID_ARG, "gen_batch_world: bad args");
     clear_with_floor(g, X, Y, Z);
-    Pcg32 r(world_seed, 0xC3Du);
-    const uint32_t u1 = r.next(), u2 = r.next();
-    const uint32_t sand_thr = kP05 + (uint32_t)(((uint64_t)u1 * kP35) >> 32);
-    const uint32_t water_thr = sand_thr + (uint32_t)(((uint64_t)u2 * kP20) >> 32);
+    const fs3d::BatchWorldGen p = fs3d::batch_world_gen(world_seed);
+    Pcg32 r(0, 0);
+    r.state = p.fill_state;
+    r.inc = p.inc;
+    const uint32_t sand_thr = p.sand_thr, water_thr = p.water_thr;
     const size_t n = (size_t)X * Y * Z;
     for (size_t i = (size_t)X * Z * (Y / 2); i < n; ++i) {
         if (g[i]) continue;

@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "fs3d_common.h"
+#include "pcg.h"
 #include "planes.h"
 #include "rule_device.cuh"
 
@@ -93,6 +94,45 @@ __global__ void k_hash_planes(const uint4* __restrict__ rows, const uint8_t* __r
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) h += __shfl_xor_sync(0xffffffffu, h, off);
     if ((threadIdx.x & 31) == 0 && h) atomicAdd(out, (unsigned long long)h);
+}
+
+// The mixed-size batch world generated straight into planes: stone at y < 2,
+// empty below Y/2, and above it one PCG32 draw per cell in index order; each
+// thread jumps its generator to the first draw of its 64-cell word.
+__global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p, uint4* __restrict__ rows) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    const int yf = Y / 2;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int w = (int)(u % nw);
+        const int64_t r = u / nw;
+        const int y = (int)(r / Z), z = (int)(r % Z);
+        uint32_t ae = 0, ao = 0, be = 0, bo = 0;
+        uint64_t st = 0;
+        if (y >= yf) st = pcg_jump(p.fill_state, ((uint64_t)(y - yf) * Z + z) * X + 64u * w, p.inc);
+        for (int m = 0; m < 64; ++m) {
+            const int x = 64 * w + m;
+            uint32_t v;
+            if (x >= X || y < 2) {
+                v = 1u;
+            } else if (y < yf) {
+                v = 0u;
+            } else {
+                const uint32_t d = pcg_output(st);
+                st = st * kPcgMult + p.inc;
+                v = d < p.sand_thr ? 2u : (d < p.water_thr ? 3u : 0u);
+            }
+            uint32_t a, b;
+            classify(v, a, b);
+            if (m & 1) {
+                ao |= a << (m >> 1);
+                bo |= b << (m >> 1);
+            } else {
+                ae |= a << (m >> 1);
+                be |= b << (m >> 1);
+            }
+        }
+        rows[u] = make_uint4(ae, ao, be, bo);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -238,6 +278,14 @@ fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows
     const int nw = plane_nw(X);
     k_bytes_to_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(g, X, Y, Z, nw, rows);
     FS3D_CHECK_LAUNCH("bytes->planes launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_generate_batch_world(uint64_t world_seed, int X, int Y, int Z, uint4* rows, cudaStream_t st) {
+    const int nw = plane_nw(X);
+    k_gen_batch_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(X, Y, Z, nw, batch_world_gen(world_seed),
+                                                                       rows);
+    FS3D_CHECK_LAUNCH("generate batch world launch");
     return FS3D_OK;
 }
 

@@ -35,6 +35,8 @@ int plane_items_for(int Y, int Z, int nw);
 int plane_step_grid(int64_t n_items);
 int plane_step_ctas_per_sm();
 fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows, cudaStream_t st);
+// the batch world of `world_seed` written straight into planes (needs Y >= 4)
+fs3d_status planes_generate_batch_world(uint64_t world_seed, int X, int Y, int Z, uint4* rows, cudaStream_t st);
 fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, uint8_t* g,
                             cudaStream_t st);
 fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,

@@ -140,6 +140,10 @@ fs3d_status fs3d_batch_create(size_t hbm_budget_bytes, const fs3d_config* cfg, f
 fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* grid_host, int X, int Y, int Z,
                              uint64_t seed, uint64_t start_step, int64_t n_steps,
                              uint64_t* ticket);
+/* Admits the mixed-size synthetic world of `seed` (fs3d_gen_batch_world), generated
+ * on the device straight into the pool: no host grid, no upload.  Needs Y >= 4. */
+fs3d_status fs3d_batch_admit_generated(fs3d_batch* b, int X, int Y, int Z, uint64_t seed,
+                                       uint64_t start_step, int64_t n_steps, uint64_t* ticket);
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream */
 fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
 /* done = 1 once the world has taken all its steps; hash valid when done */

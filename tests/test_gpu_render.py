@@ -28,7 +28,7 @@ def test_sdf_sphere_matches_cpu(fs3d, orc, cuda, wh):
     got = out.cpu().numpy()
     exp = orc.render_sdf(oracle_lib.camera_from(cam), W, H)
     check_img(got, exp)
-    assert (got[..., 0] > 0.04).sum() > 0.02 * W * H  # the sphere is in view
+    assert (got[..., 0] > 0.04).sum() > 0.01 * W * H  # the sphere is in view
 
 
 @pytest.mark.parametrize("layout", [0, 1])
