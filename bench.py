@@ -180,7 +180,7 @@ def cpu_sample(worlds, budget_s: float, threads: int):
         while True:
             done += sum(ex.map(run, range(len(sample))))
             rounds += 1
-            if time.perf_counter() - t0 > budget_s or rounds >= 50:
+            if time.perf_counter() - t0 > budget_s:
                 break
     dt = time.perf_counter() - t0
     return done / dt, {"worlds": len(sample), "steps_per_round": steps_each, "rounds": rounds,
@@ -404,6 +404,30 @@ def run_fs3d(args):
     return 0
 
 
+def run_only(args):
+    """One workload without the side measurements, for ncu captures:
+    `batched` runs warmup + steps segments of the 2048-world pool, `plain512`
+    runs warmup + steps x 8 steps of the drop-in byte kernel on 512^3."""
+    import torch
+    import fallingsand3d_gb300 as fs3d
+    if args.only == "batched":
+        worlds = batch_worlds(fs3d, args.master, args.worlds)
+        with fs3d.Batch(150 << 30, steps_per_segment=args.segment) as b:
+            for (X, Y, Z), seed in worlds:
+                b.admit_generated(X, Y, Z, seed, args.segment * (args.warmup + args.steps))
+            for _ in range(args.warmup + args.steps):
+                b.run_segment()
+            b.sync()
+    else:
+        g = fs3d.gen_pillars(1, 512, 512, 512)
+        d = torch.from_numpy(g).cuda()
+        fs3d.step_device(d.data_ptr(), 512, 512, 512, 1, 0, 8 * (args.warmup + args.steps),
+                         torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+    print(json.dumps({"only": args.only, "ok": True}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -417,11 +441,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--skip-512", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512"],
+                    help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.only != "all":
+        return run_only(args)
     return run_fs3d(args)
 
 

@@ -41,7 +41,7 @@ EXPORTS = (
     "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
-    "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit",
+    "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_gen_parity", "fs3d_gen_pillars",
@@ -100,6 +100,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_world_load": (S, [C.c_char_p, i32, C.POINTER(vp)]),
         "fs3d_batch_create": (S, [C.c_size_t, C.POINTER(Config), C.POINTER(vp)]),
         "fs3d_batch_admit": (S, [vp, vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
+        "fs3d_batch_admit_generated": (S, [vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
         "fs3d_batch_run_segment": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
@@ -349,6 +350,12 @@ class Batch:
         Y, Z, X = g.shape
         t = u64()
         check(lib().fs3d_batch_admit(self.handle, _ptr(g), X, Y, Z, seed, start_step, n_steps, C.byref(t)))
+        return int(t.value)
+
+    def admit_generated(self, X: int, Y: int, Z: int, seed: int, n_steps: int, start_step: int = 0) -> int:
+        """Admits the synthetic batch world of `seed`, generated on the device."""
+        t = u64()
+        check(lib().fs3d_batch_admit_generated(self.handle, X, Y, Z, seed, start_step, n_steps, C.byref(t)))
         return int(t.value)
 
     def try_admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> Optional[int]:

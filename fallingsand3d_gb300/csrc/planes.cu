@@ -138,10 +138,7 @@ __global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p,
 // ---------------------------------------------------------------------------
 // step
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t cls_byte(uint32_t a, uint32_t b) { return a ? (b ? 3u : 2u) : (b ? 1u : 0u); }
-
 // One block row-pair of one world; lane gl of a group of G lanes.
-// Returns true if any of the four rows changed.
 __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, int gl, int G,
                                               unsigned gmask) {
     const int NBZ = nblocks(w.Z, o);
@@ -149,7 +146,7 @@ __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
     const int y0 = 2 * j - o, z0 = 2 * k - o;
     const bool has = gl < w.nw;
-    uint4 q[4];
+    uint4 q[4], q0[4];
     uint4* ptr[4];
     bool in[4];
 #pragma unroll
@@ -158,72 +155,13 @@ __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32
         in[a] = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
         ptr[a] = in[a] ? w.rows + ((int64_t)y * w.Z + z) * w.nw + gl : w.rows;
         q[a] = in[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        q0[a] = q[a];
     }
-    // slot s = layer*4 + dz*2 + dx; row a = layer*2 + dz
-    uint32_t A[8], B[8];
+    rowpair_core(q, has, o, rk, gl, G, gmask, w.nw, (w.X & 63) == 0);
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
-        if (o == 0) {
-            A[s0] = q[a].x;
-            B[s0] = q[a].z;
-        } else {
-            uint32_t ua = __shfl_up_sync(gmask, q[a].y, 1, G);
-            uint32_t ub = __shfl_up_sync(gmask, q[a].w, 1, G);
-            if (gl == 0) {
-                ua = 0u;  // x = -1 lies outside: solid
-                ub = 0xFFFFFFFFu;
-            }
-            A[s0] = (q[a].y << 1) | (ua >> 31);
-            B[s0] = (q[a].w << 1) | (ub >> 31);
-        }
-        A[s0 + 1] = (o == 0) ? q[a].y : q[a].x;
-        B[s0 + 1] = (o == 0) ? q[a].w : q[a].z;
-    }
-    if (has) bs_rule(A, B, rk, (uint32_t)gl);
-    // half block at x = X-1 (odd phase, X % 64 == 0): last lane, scalar rule
-    uint32_t half = 0;
-    const bool do_half = o == 1 && has && gl == w.nw - 1 && (w.X & 63) == 0;
-    if (do_half) {
-        uint64_t V = 0;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int s0 = (a >> 1) * 4 + (a & 1) * 2;
-            V |= (uint64_t)cls_byte(q[a].y >> 31, q[a].w >> 31) << (8 * s0);
-            V |= (uint64_t)1u << (8 * (s0 + 1));
-        }
-        if (block_can_move((uint32_t)V, (uint32_t)(V >> 32))) V = block_rule(V, rk, 32u * (uint32_t)w.nw);
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const uint32_t c = get_byte(V, (a >> 1) * 4 + (a & 1) * 2);
-            half |= ((c == 2u || c == 3u) ? 1u : 0u) << a;                   // A bit
-            half |= ((c == 0u || c == 2u) ? 0u : 1u) << (4 + a);             // B bit
-        }
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
-        uint4 n;
-        if (o == 0) {
-            n = make_uint4(A[s0], A[s0 + 1], B[s0], B[s0 + 1]);
-        } else {
-            const uint32_t da = __shfl_down_sync(gmask, A[s0], 1, G);
-            const uint32_t db = __shfl_down_sync(gmask, B[s0], 1, G);
-            uint32_t ta, tb;  // new bit 31 of this lane's odd words
-            if (gl < w.nw - 1) {
-                ta = da & 1u;
-                tb = db & 1u;
-            } else if (do_half) {
-                ta = (half >> a) & 1u;
-                tb = (half >> (4 + a)) & 1u;
-            } else {
-                ta = q[a].y >> 31;
-                tb = q[a].w >> 31;
-            }
-            n = make_uint4(A[s0 + 1], (A[s0] >> 1) | (ta << 31), B[s0 + 1], (B[s0] >> 1) | (tb << 31));
-        }
-        if (in[a] && (n.x != q[a].x || n.y != q[a].y || n.z != q[a].z || n.w != q[a].w)) *ptr[a] = n;
-    }
+    for (int a = 0; a < 4; ++a)
+        if (in[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
+            *ptr[a] = q[a];
 }
 
 // One launch = one step (segment step s_seg) of every live world.  Work items

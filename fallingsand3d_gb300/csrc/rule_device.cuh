@@ -201,4 +201,81 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
     return changed;
 }
 
+
+__device__ __forceinline__ uint32_t cls_byte(uint32_t a, uint32_t b) { return a ? (b ? 3u : 2u) : (b ? 1u : 0u); }
+
+// One step of one block row-pair held as plane words.  The pair's four rows
+// (a = layer*2 + dz: top z0, top z1, bottom z0, bottom z1) cover x in
+// [64*gl, 64*gl+64) of lane gl in a group of G lanes (mask gmask); q[a] =
+// {A even, A odd, B even, B odd}, updated in place.  Rows outside the world
+// are passed as solid.  In the odd phase the dx=0 word is the odd word shifted
+// up one bit with bit 31 of the left lane's odd word carried in (x = -1 is
+// solid), and the left lane receives its new bit 31 back; when the row width
+// is a multiple of 64 (`half_at_end`) the last lane also runs the half block
+// at x = 64*nw - 1 with the scalar rule.
+__device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uint32_t rk, int gl, int G,
+                                             unsigned gmask, int nw, bool half_at_end) {
+    uint32_t A[8], B[8];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+        if (o == 0) {
+            A[s0] = q[a].x;
+            B[s0] = q[a].z;
+        } else {
+            uint32_t ua = __shfl_up_sync(gmask, q[a].y, 1, G);
+            uint32_t ub = __shfl_up_sync(gmask, q[a].w, 1, G);
+            if (gl == 0) {
+                ua = 0u;
+                ub = 0xFFFFFFFFu;
+            }
+            A[s0] = (q[a].y << 1) | (ua >> 31);
+            B[s0] = (q[a].w << 1) | (ub >> 31);
+        }
+        A[s0 + 1] = (o == 0) ? q[a].y : q[a].x;
+        B[s0 + 1] = (o == 0) ? q[a].w : q[a].z;
+    }
+    if (has) bs_rule(A, B, rk, (uint32_t)gl);
+    uint32_t half = 0;
+    const bool do_half = o == 1 && has && gl == nw - 1 && half_at_end;
+    if (do_half) {
+        uint64_t V = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+            V |= (uint64_t)cls_byte(q[a].y >> 31, q[a].w >> 31) << (8 * s0);
+            V |= (uint64_t)1u << (8 * (s0 + 1));
+        }
+        if (block_can_move((uint32_t)V, (uint32_t)(V >> 32))) V = block_rule(V, rk, 32u * (uint32_t)nw);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const uint32_t c = get_byte(V, (a >> 1) * 4 + (a & 1) * 2);
+            half |= ((c == 2u || c == 3u) ? 1u : 0u) << a;
+            half |= ((c == 0u || c == 2u) ? 0u : 1u) << (4 + a);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int s0 = (a >> 1) * 4 + (a & 1) * 2;
+        if (o == 0) {
+            q[a] = make_uint4(A[s0], A[s0 + 1], B[s0], B[s0 + 1]);
+        } else {
+            const uint32_t da = __shfl_down_sync(gmask, A[s0], 1, G);
+            const uint32_t db = __shfl_down_sync(gmask, B[s0], 1, G);
+            uint32_t ta, tb;  // new bit 31 of this lane's odd words
+            if (gl < nw - 1) {
+                ta = da & 1u;
+                tb = db & 1u;
+            } else if (do_half) {
+                ta = (half >> a) & 1u;
+                tb = (half >> (4 + a)) & 1u;
+            } else {
+                ta = q[a].y >> 31;
+                tb = q[a].w >> 31;
+            }
+            q[a] = make_uint4(A[s0 + 1], (A[s0] >> 1) | (ta << 31), B[s0 + 1], (B[s0] >> 1) | (tb << 31));
+        }
+    }
+}
+
 }  // namespace fs3d

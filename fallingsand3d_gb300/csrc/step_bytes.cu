@@ -195,6 +195,121 @@ __global__ void __launch_bounds__(256) k_step_rows16(uint8_t* __restrict__ grid,
 }
 
 // ---------------------------------------------------------------------------
+// bit-sliced byte kernel (X % 64 == 0, X <= 2048, grid 16-byte aligned)
+//
+// A lane owns 64 cells of each of the four rows of a block row-pair (16 uint4
+// loads), turns them into plane words in registers, runs the shared
+// bit-sliced row-pair step (32 blocks per 32-bit operation) and writes back
+// only the 16-byte pieces whose cells changed class.
+// ---------------------------------------------------------------------------
+
+// bits 7, 15, 23, 31 -> bits 0..3
+__device__ __forceinline__ uint32_t gather_hi4(uint32_t m) { return ((m >> 7) * 0x10204080u) >> 28; }
+// bits 0..3 -> bit 0 of bytes 0..3
+__device__ __forceinline__ uint32_t spread4(uint32_t n) { return (n * 0x00204081u) & 0x01010101u; }
+
+// four cells (one byte each) -> nibbles of A (sand or water) and B (water or solid)
+__device__ __forceinline__ void classify4(uint32_t v, uint32_t& a4, uint32_t& b4) {
+    const uint32_t ta = (v & 0xFEFEFEFEu) ^ 0x02020202u;        // byte 0 iff value in {2,3}
+    const uint32_t nza = ((ta & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | ta;  // bit 7 set iff byte != 0
+    a4 = gather_hi4(~nza & 0x80808080u);
+    const uint32_t tb = v & 0xFDFDFDFDu;                        // byte 0 iff value in {0,2}
+    const uint32_t nzb = ((tb & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | tb;
+    b4 = gather_hi4(nzb & 0x80808080u);
+}
+
+// 64 cells (16 words, x = 4k + byte) -> {A even, A odd, B even, B odd}
+__device__ __forceinline__ uint4 bytes_to_planes64(const uint32_t (&w)[16]) {
+    uint32_t ae = 0, ao = 0, be = 0, bo = 0;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        uint32_t a, b;
+        classify4(__byte_perm(w[2 * p], w[2 * p + 1], 0x6420), a, b);  // x = 8p, 8p+2, 8p+4, 8p+6
+        ae |= a << (4 * p);
+        be |= b << (4 * p);
+        classify4(__byte_perm(w[2 * p], w[2 * p + 1], 0x7531), a, b);  // x = 8p+1, +3, +5, +7
+        ao |= a << (4 * p);
+        bo |= b << (4 * p);
+    }
+    return make_uint4(ae, ao, be, bo);
+}
+
+// Writes the new class of every cell whose class changed (only empty, sand
+// and water cells can change: 0, 2, 3).  Returns a mask of changed word pairs.
+__device__ __forceinline__ uint32_t planes_to_bytes64(uint32_t (&w)[16], const uint4& n, const uint4& old) {
+    const uint32_t che = (n.x ^ old.x) | (n.z ^ old.z), cho = (n.y ^ old.y) | (n.w ^ old.w);
+    uint32_t pairs = 0;
+    if (!(che | cho)) return 0u;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        const uint32_t ce = (che >> (4 * p)) & 0xFu, co = (cho >> (4 * p)) & 0xFu;
+        if (!(ce | co)) continue;
+        pairs |= 1u << p;
+        const uint32_t sae = spread4((n.x >> (4 * p)) & 0xFu), sbe = spread4((n.z >> (4 * p)) & 0xFu);
+        const uint32_t sao = spread4((n.y >> (4 * p)) & 0xFu), sbo = spread4((n.w >> (4 * p)) & 0xFu);
+        const uint32_t ve = (sae << 1) | (sae & sbe), vo = (sao << 1) | (sao & sbo);  // 0, 2 or 3
+        const uint32_t me = spread4(ce) * 0xFFu, mo = spread4(co) * 0xFFu;
+        const uint32_t m0 = __byte_perm(me, mo, 0x5140), m1 = __byte_perm(me, mo, 0x7362);
+        w[2 * p] = (w[2 * p] & ~m0) | (__byte_perm(ve, vo, 0x5140) & m0);
+        w[2 * p + 1] = (w[2 * p + 1] & ~m1) | (__byte_perm(ve, vo, 0x7362) & m1);
+    }
+    return pairs;
+}
+
+__global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
+                                                    uint32_t sk, int lg) {
+    const int NC = X >> 6, G = 1 << lg, per = 32 >> lg;
+    const int NBZ = nblocks(Z, o), NRP = nblocks(Y, o) * NBZ;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+    const unsigned gmask = (G == 32) ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int n_items = (NRP + per - 1) / per;
+    for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += warps) {
+        const int rp = it * per + (lane >> lg);
+        if (rp >= NRP) continue;  // uniform within a lane group
+        const int j = rp / NBZ, k = rp - j * NBZ;
+        const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
+        const int y0 = 2 * j - o, z0 = 2 * k - o;
+        const bool has = gl < NC;
+        uint32_t w[4][16];
+        uint4 q[4], q0[4];
+        uint8_t* ptr[4];
+        bool in[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+            in[a] = has && y >= 0 && y < Y && z >= 0 && z < Z;
+            ptr[a] = in[a] ? grid + ((int64_t)y * Z + z) * X + 64 * gl : grid;
+            if (in[a]) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint4 v = reinterpret_cast<const uint4*>(ptr[a])[u];
+                    w[a][4 * u] = v.x;
+                    w[a][4 * u + 1] = v.y;
+                    w[a][4 * u + 2] = v.z;
+                    w[a][4 * u + 3] = v.w;
+                }
+                q[a] = bytes_to_planes64(w[a]);
+            } else {
+                q[a] = make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+            }
+            q0[a] = q[a];
+        }
+        rowpair_core(q, has, o, rk, gl, G, gmask, NC, true);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            if (!in[a]) continue;
+            const uint32_t pairs = planes_to_bytes64(w[a], q[a], q0[a]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if ((pairs >> (2 * u)) & 3u)
+                    reinterpret_cast<uint4*>(ptr[a])[u] =
+                        make_uint4(w[a][4 * u], w[a][4 * u + 1], w[a][4 * u + 2], w[a][4 * u + 3]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // hash and first difference
 // ---------------------------------------------------------------------------
 __global__ void k_hash_bytes(const uint8_t* __restrict__ g, int64_t n, unsigned long long* out) {
@@ -249,13 +364,36 @@ bool rows16_ok(const void* grid, int X) {
     return (X % 16) == 0 && (reinterpret_cast<uintptr_t>(grid) & 15u) == 0;
 }
 
+bool rows64_ok(const void* grid, int X) {
+    return (X % 64) == 0 && X <= 2048 && (reinterpret_cast<uintptr_t>(grid) & 15u) == 0;
+}
+
+static int rows64_lg(int X) {
+    int lg = 0;
+    while ((1 << lg) < (X >> 6)) ++lg;
+    return lg;
+}
+
+static int rows64_ctas_per_sm() {
+    static int n = 0;
+    if (!n && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_rows64, 128, 0) != cudaSuccess || n < 1))
+        n = 1;
+    return n;
+}
+
 fs3d_status launch_step_bytes(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t0, int n_steps,
                               cudaStream_t st) {
     for (int a = 0; a < n_steps; ++a) {
         const uint64_t t = t0 + (uint64_t)a;
         const int o = (int)(t & 1u);
         const uint32_t sk = stepkey(seed, t);
-        if (rows16_ok(grid, X)) {
+        if (rows64_ok(grid, X)) {
+            const int lg = rows64_lg(X);
+            const int per = 32 >> lg;
+            const int64_t items = ((int64_t)nblocks(Y, o) * nblocks(Z, o) + per - 1) / per;
+            k_step_rows64<<<grid_for(items * 32, 128, rows64_ctas_per_sm()), 128, 0, st>>>(grid, X, Y, Z, o, sk,
+                                                                                          lg);
+        } else if (rows16_ok(grid, X)) {
             const int64_t units = (int64_t)(X >> 4) * nblocks(Y, o) * nblocks(Z, o);
             k_step_rows16<<<grid_for(units, 256, 8), 256, 0, st>>>(grid, X, Y, Z, o, sk);
         } else {

@@ -118,3 +118,21 @@ def test_start_step_offsets_parity(fs3d, orc):
     ref = g.copy()
     orc.run(ref, seed, 11, 37, nthreads=0)
     assert h == orc.hash(ref)
+
+
+def test_device_generated_worlds_match_host_generator(fs3d, orc):
+    dims, seeds = fs3d.gen_batch_dims(31, 12)
+    with fs3d.Batch(GiB, steps_per_segment=16) as b:
+        for w in range(12):
+            X, Y, Z = (int(v) for v in dims[w])
+            seed = int(seeds[w])
+            t0 = b.admit_generated(X, Y, Z, seed, 0)
+            assert (b.retire(t0, (Y, Z, X)) == orc.gen_c3_world(seed, X, Y, Z)).all(), (X, Y, Z)
+        X, Y, Z = (int(v) for v in dims[0])
+        t = b.admit_generated(X, Y, Z, int(seeds[0]), 40)
+        for _ in range(3):
+            b.run_segment()
+        b.sync()
+        ref = orc.gen_c3_world(int(seeds[0]), X, Y, Z)
+        orc.run(ref, int(seeds[0]), 0, 40, nthreads=0)
+        assert b.poll(t)[1] == orc.hash(ref)
