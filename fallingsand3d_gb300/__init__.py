@@ -43,7 +43,7 @@ EXPORTS = (
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
-    "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_render", "fs3d_render_sdf",
+    "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_gen_parity", "fs3d_gen_pillars",
     "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
 )
@@ -61,9 +61,29 @@ class Camera(C.Structure):
                 ("light_pos", C.c_float * 3), ("reserved", C.c_int32)]
 
 
+class ServeParams(C.Structure):
+    _fields_ = [("lambda_", C.c_double), ("duration_s", C.c_double), ("max_requests", C.c_int64),
+                ("master_seed", C.c_uint64), ("hbm_budget", C.c_size_t), ("steps_per_segment", C.c_int),
+                ("min_steps", C.c_int), ("max_steps", C.c_int), ("with_hash", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("admitted_s", C.c_double), ("finished_s", C.c_double),
+                ("X", C.c_int32), ("Y", C.c_int32), ("Z", C.c_int32), ("n_steps", C.c_int32),
+                ("seed", C.c_uint64), ("hash", C.c_uint64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("requests", C.c_int64), ("completed", C.c_int64), ("segments", C.c_int64),
+                ("peak_live_worlds", C.c_int64), ("peak_bytes", C.c_size_t), ("wall_s", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("voxel_updates", C.c_double), ("voxel_updates_per_s", C.c_double),
+                ("offered_voxel_updates_per_s", C.c_double), ("reserved", C.c_double * 8)]
+
+
 class Config(C.Structure):
     _fields_ = [("steps_per_segment", C.c_int), ("ctas_per_sm", C.c_int), ("use_graphs", C.c_int),
-                ("reserved", C.c_int * 13)]
+                ("use_smem", C.c_int), ("reserved", C.c_int * 12)]
 
 
 _lib: Optional[C.CDLL] = None
@@ -109,6 +129,8 @@ def _bind(lib: C.CDLL) -> None:
                                  C.POINTER(C.c_size_t)]),
         "fs3d_batch_stream": (S, [vp, C.POINTER(vp)]),
         "fs3d_batch_destroy": (S, [vp]),
+        "fs3d_serve_plan": (S, [C.POINTER(ServeParams), i64, C.POINTER(ServeRequest), C.POINTER(i64)]),
+        "fs3d_serve_run": (S, [C.POINTER(ServeParams), i64, C.POINTER(ServeRequest), C.POINTER(ServeStats)]),
         "fs3d_render": (S, [vp, C.POINTER(Camera), i32, i32, i32, vp, i32]),
         "fs3d_render_sdf": (S, [C.POINTER(Camera), i32, i32, vp, vp]),
         "fs3d_camera_fs_raymarch": (None, [C.POINTER(Camera)]),
@@ -330,10 +352,11 @@ class Batch:
     """Pool of many worlds stepped together in graph-captured segments."""
 
     def __init__(self, budget_bytes: int, steps_per_segment: int = 64, use_graphs: bool = True,
-                 ctas_per_sm: int = 0):
+                 ctas_per_sm: int = 0, use_smem: bool = True):
         cfg = lib().fs3d_default_config()
         cfg.steps_per_segment = steps_per_segment
         cfg.use_graphs = 1 if use_graphs else 0
+        cfg.use_smem = 1 if use_smem else 0
         cfg.ctas_per_sm = ctas_per_sm
         h = vp()
         check(lib().fs3d_batch_create(budget_bytes, C.byref(cfg), C.byref(h)))
@@ -412,3 +435,31 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- serving
+def serve_params(lam: float, duration_s: float, master_seed: int = 1, max_requests: int = 0,
+                 hbm_budget: int = 0, steps_per_segment: int = 64, min_steps: int = 10, max_steps: int = 1000,
+                 with_hash: bool = True) -> ServeParams:
+    p = ServeParams()
+    p.lambda_, p.duration_s, p.max_requests, p.master_seed = lam, duration_s, max_requests, master_seed
+    p.hbm_budget, p.steps_per_segment, p.min_steps, p.max_steps = hbm_budget, steps_per_segment, min_steps, max_steps
+    p.with_hash = 1 if with_hash else 0
+    return p
+
+
+def serve_plan(p: ServeParams):
+    n = i64()
+    check(lib().fs3d_serve_plan(C.byref(p), 0, None, C.byref(n)))
+    reqs = (ServeRequest * max(n.value, 1))()
+    check(lib().fs3d_serve_plan(C.byref(p), n.value, reqs, C.byref(n)))
+    return reqs, n.value
+
+
+def serve(p: ServeParams):
+    """Plans and serves the request stream; returns (stats dict, requests)."""
+    reqs, n = serve_plan(p)
+    st = ServeStats()
+    check(lib().fs3d_serve_run(C.byref(p), n, reqs, C.byref(st)))
+    stats = {f: getattr(st, f) for f, _ in ServeStats._fields_ if f != "reserved"}
+    return stats, [reqs[i] for i in range(n)]

@@ -12,6 +12,8 @@
 // uploaded concurrently.
 #include <string.h>
 
+#include <algorithm>
+
 #include <chrono>
 #include <map>
 #include <thread>
@@ -79,13 +81,18 @@ struct fs3d_batch {
     uint64_t next_ticket = 1;
     PinnedArray<PlaneWorld> tw;
     PinnedArray<PlaneItem> ti;
-    PinnedArray<int> tn;
+    PinnedArray<int> tn;  // {per-step items, resident worlds}
+    PinnedArray<int> to;  // resident worlds (indices into tw), largest first
+    int* counter = nullptr;  // work counter of the resident kernel
+    int* err = nullptr;      // set by a kernel whose bounded wait gave up
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
     cudaEvent_t last_segment = nullptr;
     std::vector<cudaEvent_t> pending_ready;  // admissions the next segment must wait for
     cudaGraphExec_t graph = nullptr;
     void* graph_worlds = nullptr;  // table pointers baked into the graph
     void* graph_items = nullptr;
+    void* graph_order = nullptr;
     int grid = 0;
     unsigned long long* hash_dev = nullptr;
     uint64_t segments = 0;
@@ -120,28 +127,54 @@ void free_world(fs3d_batch* b, BWorld& w) {
     w.ready = w.finished = nullptr;
 }
 
+// One segment: the resident kernel (worlds that fit in shared memory, all
+// their steps in one launch) on `a`, concurrently with steps_per_segment
+// launches of the per-step kernel (the larger worlds) on `c`.
+fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, cudaStream_t c) {
+    if (a != c) {
+        FS3D_CUDA(cudaEventRecord(b->fork, a));
+        FS3D_CUDA(cudaStreamWaitEvent(c, b->fork, 0));
+    }
+    fs3d_status s = FS3D_OK;
+    if (b->cfg.use_smem) s = launch_plane_segment_smem(b->tw.d, b->to.d, b->tn.d + 1, b->counter, b->err, a);
+    for (int k = 0; k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
+        s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, c);
+    if (s != FS3D_OK) return s;
+    if (a != c) {
+        FS3D_CUDA(cudaEventRecord(b->join, c));
+        FS3D_CUDA(cudaStreamWaitEvent(a, b->join, 0));
+    }
+    return FS3D_OK;
+}
+
 fs3d_status capture_graph(fs3d_batch* b) {
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
-    cudaStream_t cs;
+    cudaStream_t cs, cs2;
     FS3D_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return cuda_fail(e, "cudaStreamCreate");
+    }
     cudaGraph_t g = nullptr;
     fs3d_status s = FS3D_OK;
-    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        for (int a = 0; a < b->cfg.steps_per_segment && s == FS3D_OK; ++a)
-            s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, a, cs);
+        s = enqueue_segment(b, cs, cs2);
         e = cudaStreamEndCapture(cs, &g);
     }
     if (e == cudaSuccess && s == FS3D_OK) e = cudaGraphInstantiate(&b->graph, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
+    cudaStreamDestroy(cs2);
     if (s != FS3D_OK) return s;
     if (e != cudaSuccess) return cuda_fail(e, "segment graph capture");
     b->graph_worlds = b->tw.d;
     b->graph_items = b->ti.d;
+    b->graph_order = b->to.d;
     return FS3D_OK;
 }
 
@@ -165,6 +198,11 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e == cudaSuccess) {
         // keep freed pool memory cached so admissions after retirements are cheap
         int dev = 0;
@@ -175,7 +213,7 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
         }
     }
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_create");
-    if (s == FS3D_OK) s = b->tn.reserve(1);
+    if (s == FS3D_OK) s = b->tn.reserve(2);
     if (s != FS3D_OK) {
         fs3d_batch_destroy(b);
         return s;
@@ -240,8 +278,9 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     if (s == FS3D_OK) {
         e = cudaEventCreateWithFlags(&w.ready, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(w.ready, b->side);
-        // the caller's buffer may be reused as soon as this returns
-        if (e == cudaSuccess) e = cudaEventSynchronize(w.ready);
+        // the caller's buffer may be reused as soon as this returns; a world
+        // generated on the device has no host buffer and is not waited for
+        if (e == cudaSuccess && g) e = cudaEventSynchronize(w.ready);
         if (e != cudaSuccess) s = cuda_fail(e, "admit event");
     }
     if (s != FS3D_OK) {
@@ -274,22 +313,25 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     const int S = b->cfg.steps_per_segment;
     // the pinned tables may be rewritten once the previous upload has run
     FS3D_CUDA(cudaEventSynchronize(b->tables_free));
-    size_t nw_ = 0, ni = 0;
+    const size_t lim = b->cfg.use_smem ? (size_t)smem_world_limit() : 0;
+    size_t nw_ = 0, ni = 0, ns = 0;
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
         ++nw_;
-        ni += (size_t)plane_items_for(w.Y, w.Z, w.nw);
+        if (plane_bytes(w.X, w.Y, w.Z) <= lim)
+            ++ns;
+        else
+            ni += (size_t)plane_items_for(w.Y, w.Z, w.nw);
     }
     if (nw_ == 0) return FS3D_OK;
-    void* old_w = b->tw.d;
-    void* old_i = b->ti.d;
     // growing the tables frees device arrays a running segment may still read
-    if (nw_ > b->tw.cap || ni > b->ti.cap) FS3D_CUDA(cudaStreamSynchronize(b->stream));
+    if (nw_ > b->tw.cap || ni > b->ti.cap || ns > b->to.cap) FS3D_CUDA(cudaStreamSynchronize(b->stream));
     fs3d_status s = b->tw.reserve(nw_);
-    if (s == FS3D_OK) s = b->ti.reserve(ni);
+    if (s == FS3D_OK) s = b->ti.reserve(ni > 0 ? ni : 1);
+    if (s == FS3D_OK) s = b->to.reserve(ns > 0 ? ns : 1);
     if (s != FS3D_OK) return s;
-    size_t wi = 0, ii = 0;
+    size_t wi = 0, ii = 0, si = 0;
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
@@ -305,11 +347,22 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         d.nw = w.nw;
         d.steps = steps;
         d.lg = plane_lg(w.nw);
-        const int per = 32 >> d.lg, items = plane_items_for(w.Y, w.Z, w.nw);
-        for (int a = 0; a < items; ++a) b->ti.h[ii++] = PlaneItem{(int32_t)wi, a * per};
+        if (plane_bytes(w.X, w.Y, w.Z) <= lim) {
+            b->to.h[si++] = (int)wi;
+        } else {
+            const int per = 32 >> d.lg, items = plane_items_for(w.Y, w.Z, w.nw);
+            for (int a = 0; a < items; ++a) b->ti.h[ii++] = PlaneItem{(int32_t)wi, a * per};
+        }
         ++wi;
     }
+    // largest resident worlds first, so the tail of the launch is short
+    std::sort(b->to.h, b->to.h + si, [&](int x, int y) {
+        const PlaneWorld &a = b->tw.h[x], &c = b->tw.h[y];
+        const int64_t ca = (int64_t)a.X * a.Y * a.Z * a.steps, cc = (int64_t)c.X * c.Y * c.Z * c.steps;
+        return ca != cc ? ca > cc : x < y;
+    });
     b->tn.h[0] = (int)ii;
+    b->tn.h[1] = (int)si;
     // admissions complete before the segment reads their planes
     for (auto& kv : b->worlds)
         if (kv.second.ready) {
@@ -318,22 +371,20 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
             kv.second.ready = nullptr;
         }
     FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * wi, cudaMemcpyHostToDevice, b->stream));
-    FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
-    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    if (ii) FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
+    if (si) FS3D_CUDA(cudaMemcpyAsync(b->to.d, b->to.h, sizeof(int) * si, cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, 2 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
     if (b->cfg.use_graphs) {
-        if (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || old_w != b->tw.d ||
-            old_i != b->ti.d) {
+        if (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d) {
             s = capture_graph(b);
             if (s != FS3D_OK) return s;
         }
         FS3D_CUDA(cudaGraphLaunch(b->graph, b->stream));
-        note_launch((uint64_t)S);
+        note_launch((uint64_t)S + 1);
     } else {
-        for (int a = 0; a < S; ++a) {
-            s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, a, b->stream);
-            if (s != FS3D_OK) return s;
-        }
+        s = enqueue_segment(b, b->stream, b->stream);
+        if (s != FS3D_OK) return s;
     }
     FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
     for (auto& kv : b->worlds) {
@@ -356,6 +407,9 @@ fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_sync: NULL batch");
     fs3d_status s = wait_stream(b->stream, timeout_ns);
     if (s != FS3D_OK) return s;
+    int err = 0;
+    FS3D_CUDA(cudaMemcpy(&err, b->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
     return wait_stream(b->side, timeout_ns);
 }
 
@@ -442,7 +496,12 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     b->tw.release();
     b->ti.release();
     b->tn.release();
+    b->to.release();
     cudaFree(b->hash_dev);
+    cudaFree(b->counter);
+    cudaFree(b->err);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
     if (b->tables_free) cudaEventDestroy(b->tables_free);
     if (b->last_segment) cudaEventDestroy(b->last_segment);
     if (b->stream) cudaStreamDestroy(b->stream);

@@ -138,14 +138,15 @@ __global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p,
 // ---------------------------------------------------------------------------
 // step
 // ---------------------------------------------------------------------------
-// One block row-pair of one world; lane gl of a group of G lanes.
-__device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, int gl, int G,
-                                              unsigned gmask) {
+// One block row-pair of one world; lane gl of a group of G lanes.  Every lane
+// of the warp calls this (valid = false for groups past the last row-pair).
+__device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, bool valid, int gl,
+                                              int G) {
     const int NBZ = nblocks(w.Z, o);
-    const int j = rp / NBZ, k = rp - j * NBZ;
+    const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
     const int y0 = 2 * j - o, z0 = 2 * k - o;
-    const bool has = gl < w.nw;
+    const bool has = valid && gl < w.nw;
     uint4 q[4], q0[4];
     uint4* ptr[4];
     bool in[4];
@@ -157,7 +158,7 @@ __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32
         q[a] = in[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
         q0[a] = q[a];
     }
-    rowpair_core(q, has, o, rk, gl, G, gmask, w.nw, (w.X & 63) == 0);
+    rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a)
         if (in[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
@@ -184,15 +185,165 @@ __global__ void __launch_bounds__(256) k_plane_step(const PlaneWorld* __restrict
         const int gl = lane & (G - 1);
         const int rp = item.rp0 + (lane >> w.lg);
         const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
-        if (rp >= nrp) continue;  // uniform within a lane group
-        const unsigned gmask = (G == 32) ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-        plane_rowpair(w, o, stepkey(w.seed, t), rp, gl, G, gmask);
+        plane_rowpair(w, o, stepkey(w.seed, t), rp, rp < nrp, gl, G);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory resident segment: one CTA steps one whole world
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Waits for the mbarrier phase with an iteration limit; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (it > 64) __nanosleep(64);
+    }
+    return false;
+}
+
+// TMA bulk copy global -> shared, completion counted in bytes on `bar`
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem_dst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// TMA bulk copy shared -> global, waited for before the buffer is reused
+__device__ __forceinline__ void bulk_store_wait(void* gdst, const void* smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(smem_src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// A block row-pair of a world held in shared memory (rows r = y*Z + z of nw
+// uint4 words).  Every lane of the warp calls this.
+__device__ __forceinline__ void smem_rowpair(uint4* rows, const PlaneWorld& w, int o, uint32_t sk, int rp,
+                                             bool valid, int gl, int G) {
+    const int NBZ = nblocks(w.Z, o);
+    const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
+    const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
+    const int y0 = 2 * j - o, z0 = 2 * k - o;
+    const bool has = valid && gl < w.nw;
+    uint4 q[4], q0[4];
+    int idx[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+        const bool in = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
+        idx[a] = in ? (y * w.Z + z) * w.nw + gl : -1;
+        q[a] = in ? rows[idx[a]] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        q0[a] = q[a];
+    }
+    rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        if (idx[a] >= 0 && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
+            rows[idx[a]] = q[a];
+}
+
+// Persistent: each CTA takes worlds in the given order from `counter`, loads
+// the world's planes into shared memory with one TMA bulk copy, runs its
+// `steps` steps (one __syncthreads per step: the next phase pairs different
+// rows), and writes the planes back with one TMA bulk store.  Worlds are
+// independent, so CTAs never wait on one another.
+__global__ void __launch_bounds__(kSmemThreads) k_plane_segment_smem(const PlaneWorld* __restrict__ worlds,
+                                                                    const int* __restrict__ order,
+                                                                    const int* __restrict__ n_p, int* counter,
+                                                                    int* err) {
+    extern __shared__ __align__(128) uint4 srows[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int item;
+    const int n = *n_p;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    uint32_t phase = 0;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = item;
+        __syncthreads();
+        if (it >= n) break;
+        const PlaneWorld w = worlds[order[it]];
+        if (w.steps <= 0) continue;
+        const uint32_t bytes = (uint32_t)w.Y * (uint32_t)w.Z * (uint32_t)w.nw * 16u;
+        if (threadIdx.x == 0) bulk_load(srows, w.rows, bytes, &bar);
+        if (!mbar_wait(&bar, phase)) {
+            if (threadIdx.x == 0) atomicExch(err, 1);
+            mbar_wait(&bar, phase);  // give a late copy a second bounded chance to land
+            return;
+        }
+        phase ^= 1u;
+        const int G = 1 << w.lg, per = kSmemThreads >> w.lg;
+        const int gl = lane & (G - 1);
+        for (int s = 0; s < w.steps; ++s) {
+            const uint64_t t = w.t + (uint64_t)s;
+            const int o = (int)(t & 1u);
+            const uint32_t sk = stepkey(w.seed, t);
+            const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
+            for (int base = 0; base < nrp; base += per) {
+                const int rp = base + (int)(threadIdx.x >> w.lg);
+                smem_rowpair(srows, w, o, sk, rp, rp < nrp, gl, G);
+            }
+            __syncthreads();
+        }
+        // make the threads' shared-memory writes visible to the bulk copy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) bulk_store_wait(w.rows, srows, bytes);
+        __syncthreads();
     }
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+int smem_world_limit() {
+    static int lim = -1;
+    if (lim < 0) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        lim = optin - 1024;  // room for the kernel's static shared memory
+        if (lim < 0) lim = 0;
+        if (cudaFuncSetAttribute(k_plane_segment_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+            cudaSuccess)
+            lim = 0;
+    }
+    return lim;
+}
+
+fs3d_status launch_plane_segment_smem(const PlaneWorld* worlds, const int* order, const int* n_dev, int* counter,
+                                      int* err, cudaStream_t st) {
+    const int lim = smem_world_limit();
+    if (lim <= 0) return set_error(FS3D_ERR_CUDA, "shared-memory segment kernel unavailable");
+    FS3D_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    k_plane_segment_smem<<<sm_count_public(), kSmemThreads, lim, st>>>(worlds, order, n_dev, counter, err);
+    FS3D_CHECK_LAUNCH("smem segment launch");
+    return FS3D_OK;
+}
 int sm_count_public();
 
 static int conv_grid(int64_t n) {

@@ -30,6 +30,15 @@ inline int plane_nw(int X) { return (X + 63) / 64; }
 inline size_t plane_bytes(int X, int Y, int Z) { return (size_t)Y * Z * plane_nw(X) * sizeof(uint4); }
 constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 
+constexpr int kSmemThreads = 512;  // threads of the shared-memory segment kernel
+// largest plane buffer (bytes) one CTA can hold; 0 if unavailable
+int smem_world_limit();
+// One launch steps every world in order[0..*n_dev) through its segment steps
+// inside shared memory (worlds must fit smem_world_limit()).  *err is set to
+// 1 if a bulk copy does not complete within the wait limit.
+fs3d_status launch_plane_segment_smem(const PlaneWorld* worlds, const int* order, const int* n_dev, int* counter,
+                                      int* err, cudaStream_t st);
+
 int plane_lg(int nw);
 int plane_items_for(int Y, int Z, int nw);
 int plane_step_grid(int64_t n_items);

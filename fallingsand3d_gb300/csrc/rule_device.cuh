@@ -202,19 +202,51 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
 }
 
 
-__device__ __forceinline__ uint32_t cls_byte(uint32_t a, uint32_t b) { return a ? (b ? 3u : 2u) : (b ? 1u : 0u); }
+// The half block at the right end of an odd-phase row (x = X-1 present,
+// x = X outside) has only its dx=0 column: cells r = layer*2 + dz with bit r
+// of P (sand or water), W (water), E (empty).  Every candidate set has at
+// most one cell there, so no random draw is ever taken.
+__device__ __forceinline__ void half_block_rule(uint32_t& P, uint32_t& W, uint32_t& E) {
+    uint32_t M = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t bit = 1u << r;
+        if (!(P & bit) || (M & bit)) continue;
+        int dst = -1;
+        if (r < 2) {
+            const int below = 2 + r, diag = 3 - r;  // straight down, then the other bottom cell
+            if (E & (1u << below))
+                dst = below;
+            else if (E & (1u << diag))
+                dst = diag;
+        }
+        if (dst < 0 && (W & bit)) {
+            const int side = r ^ 1;  // the other cell of the same layer
+            if (E & (1u << side)) dst = side;
+        }
+        if (dst >= 0) {
+            const uint32_t d = 1u << dst;
+            if (W & bit) W |= d;
+            W &= ~bit;
+            P = (P & ~bit) | d;
+            E = (E | bit) & ~d;
+            M |= d;
+        }
+    }
+}
 
 // One step of one block row-pair held as plane words.  The pair's four rows
 // (a = layer*2 + dz: top z0, top z1, bottom z0, bottom z1) cover x in
-// [64*gl, 64*gl+64) of lane gl in a group of G lanes (mask gmask); q[a] =
-// {A even, A odd, B even, B odd}, updated in place.  Rows outside the world
-// are passed as solid.  In the odd phase the dx=0 word is the odd word shifted
-// up one bit with bit 31 of the left lane's odd word carried in (x = -1 is
-// solid), and the left lane receives its new bit 31 back; when the row width
-// is a multiple of 64 (`half_at_end`) the last lane also runs the half block
-// at x = 64*nw - 1 with the scalar rule.
-__device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uint32_t rk, int gl, int G,
-                                             unsigned gmask, int nw, bool half_at_end) {
+// [64*gl, 64*gl+64): lane gl of a group of G consecutive lanes (G a power of
+// two; every lane of the warp must call this together, `has` false for lanes
+// without a word).  q[a] = {A even, A odd, B even, B odd}, updated in place;
+// rows outside the world are passed as solid.  In the odd phase the dx=0 word
+// is the odd word shifted up one bit with bit 31 of the left lane's odd word
+// carried in (x = -1 is solid), and the left lane receives its new bit 31
+// back; when the row width is a multiple of 64 (`half_at_end`) the last lane
+// also runs the half block at x = 64*nw - 1.
+__device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uint32_t rk, int gl, int G, int nw,
+                                             bool half_at_end) {
     uint32_t A[8], B[8];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -222,59 +254,60 @@ __device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uin
         if (o == 0) {
             A[s0] = q[a].x;
             B[s0] = q[a].z;
+            A[s0 + 1] = q[a].y;
+            B[s0 + 1] = q[a].w;
         } else {
-            uint32_t ua = __shfl_up_sync(gmask, q[a].y, 1, G);
-            uint32_t ub = __shfl_up_sync(gmask, q[a].w, 1, G);
-            if (gl == 0) {
-                ua = 0u;
-                ub = 0xFFFFFFFFu;
+            uint32_t ua = 0u, ub = 0xFFFFFFFFu;  // x = -1 lies outside: solid
+            if (G > 1) {
+                const uint32_t sa = __shfl_up_sync(0xFFFFFFFFu, q[a].y, 1);
+                const uint32_t sb = __shfl_up_sync(0xFFFFFFFFu, q[a].w, 1);
+                if (gl > 0) {
+                    ua = sa;
+                    ub = sb;
+                }
             }
             A[s0] = (q[a].y << 1) | (ua >> 31);
             B[s0] = (q[a].w << 1) | (ub >> 31);
+            A[s0 + 1] = q[a].x;
+            B[s0 + 1] = q[a].z;
         }
-        A[s0 + 1] = (o == 0) ? q[a].y : q[a].x;
-        B[s0 + 1] = (o == 0) ? q[a].w : q[a].z;
     }
     if (has) bs_rule(A, B, rk, (uint32_t)gl);
-    uint32_t half = 0;
-    const bool do_half = o == 1 && has && gl == nw - 1 && half_at_end;
-    if (do_half) {
-        uint64_t V = 0;
+    if (o == 0) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int s0 = (a >> 1) * 4 + (a & 1) * 2;
-            V |= (uint64_t)cls_byte(q[a].y >> 31, q[a].w >> 31) << (8 * s0);
-            V |= (uint64_t)1u << (8 * (s0 + 1));
+            q[a] = make_uint4(A[s0], A[s0 + 1], B[s0], B[s0 + 1]);
         }
-        if (block_can_move((uint32_t)V, (uint32_t)(V >> 32))) V = block_rule(V, rk, 32u * (uint32_t)nw);
+        return;
+    }
+    // new bit 31 of this lane's odd words: from the right neighbour's dx=0
+    // word, from the half block, or unchanged (padding past X)
+    uint32_t ta = 0, tb = 0;
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const uint32_t c = get_byte(V, (a >> 1) * 4 + (a & 1) * 2);
-            half |= ((c == 2u || c == 3u) ? 1u : 0u) << a;
-            half |= ((c == 0u || c == 2u) ? 0u : 1u) << (4 + a);
-        }
+    for (int a = 0; a < 4; ++a) {
+        ta |= (q[a].y >> 31) << a;
+        tb |= (q[a].w >> 31) << a;
+    }
+    if (has && gl == nw - 1 && half_at_end) {
+        uint32_t P = ta, W = ta & tb, E = ~(ta | tb) & 0xFu;
+        half_block_rule(P, W, E);
+        ta = P;
+        tb = (W | (~P & ~E)) & 0xFu;
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int s0 = (a >> 1) * 4 + (a & 1) * 2;
-        if (o == 0) {
-            q[a] = make_uint4(A[s0], A[s0 + 1], B[s0], B[s0 + 1]);
-        } else {
-            const uint32_t da = __shfl_down_sync(gmask, A[s0], 1, G);
-            const uint32_t db = __shfl_down_sync(gmask, B[s0], 1, G);
-            uint32_t ta, tb;  // new bit 31 of this lane's odd words
+        uint32_t na = (ta >> a) & 1u, nb = (tb >> a) & 1u;
+        if (G > 1) {
+            const uint32_t da = __shfl_down_sync(0xFFFFFFFFu, A[s0], 1);
+            const uint32_t db = __shfl_down_sync(0xFFFFFFFFu, B[s0], 1);
             if (gl < nw - 1) {
-                ta = da & 1u;
-                tb = db & 1u;
-            } else if (do_half) {
-                ta = (half >> a) & 1u;
-                tb = (half >> (4 + a)) & 1u;
-            } else {
-                ta = q[a].y >> 31;
-                tb = q[a].w >> 31;
+                na = da & 1u;
+                nb = db & 1u;
             }
-            q[a] = make_uint4(A[s0 + 1], (A[s0] >> 1) | (ta << 31), B[s0 + 1], (B[s0] >> 1) | (tb << 31));
         }
+        q[a] = make_uint4(A[s0 + 1], (A[s0] >> 1) | (na << 31), B[s0 + 1], (B[s0] >> 1) | (nb << 31));
     }
 }
 

@@ -261,16 +261,15 @@ __global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid,
     const int NC = X >> 6, G = 1 << lg, per = 32 >> lg;
     const int NBZ = nblocks(Z, o), NRP = nblocks(Y, o) * NBZ;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1);
-    const unsigned gmask = (G == 32) ? 0xFFFFFFFFu : (((1u << G) - 1u) << (lane & ~(G - 1)));
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int n_items = (NRP + per - 1) / per;
     for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += warps) {
         const int rp = it * per + (lane >> lg);
-        if (rp >= NRP) continue;  // uniform within a lane group
-        const int j = rp / NBZ, k = rp - j * NBZ;
+        const bool valid = rp < NRP;  // every lane takes part in the row-pair step
+        const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
         const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
         const int y0 = 2 * j - o, z0 = 2 * k - o;
-        const bool has = gl < NC;
+        const bool has = valid && gl < NC;
         uint32_t w[4][16];
         uint4 q[4], q0[4];
         uint8_t* ptr[4];
@@ -295,7 +294,7 @@ __global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid,
             }
             q0[a] = q[a];
         }
-        rowpair_core(q, has, o, rk, gl, G, gmask, NC, true);
+        rowpair_core(q, has, o, rk, gl, G, NC, true);
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             if (!in[a]) continue;

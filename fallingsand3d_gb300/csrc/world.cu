@@ -28,6 +28,7 @@ struct fs3d_world {
     PlaneItem* items = nullptr;
     int* n_items_dev = nullptr;
     int n_items = 0;
+    int* aux = nullptr;  // {1 (resident world count), 0 (order[0]), work counter, error flag}
     unsigned long long* hash_dev = nullptr;
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
@@ -69,6 +70,7 @@ void destroy(fs3d_world* w) {
     cudaFree(w->desc);
     cudaFree(w->items);
     cudaFree(w->n_items_dev);
+    cudaFree(w->aux);
     cudaFree(w->hash_dev);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
@@ -143,6 +145,9 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
         e = cudaMalloc((void**)&w->desc, sizeof(PlaneWorld));
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->items, sizeof(PlaneItem) * items.size());
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->n_items_dev, sizeof(int));
+        const int aux[4] = {1, 0, 0, 0};
+        if (e == cudaSuccess) e = cudaMalloc((void**)&w->aux, sizeof(aux));
+        if (e == cudaSuccess) e = cudaMemcpy(w->aux, aux, sizeof(aux), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
             e = cudaMemcpy(w->items, items.data(), sizeof(PlaneItem) * items.size(), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(w->n_items_dev, &w->n_items, sizeof(int), cudaMemcpyHostToDevice);
@@ -177,10 +182,15 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
         d.lg = plane_lg(nw);
         // pageable source: staged before the call returns
         FS3D_CUDA(cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream));
-        const int grid = plane_step_grid(w->n_items);
         s = FS3D_OK;
-        for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
-            s = launch_plane_step(w->desc, w->items, w->n_items_dev, grid, a, w->stream);
+        if (plane_bytes(w->X, w->Y, w->Z) <= (size_t)smem_world_limit()) {
+            // the whole world fits in one CTA's shared memory: all n steps in one launch
+            s = launch_plane_segment_smem(w->desc, w->aux + 1, w->aux, w->aux + 2, w->aux + 3, w->stream);
+        } else {
+            const int grid = plane_step_grid(w->n_items);
+            for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
+                s = launch_plane_step(w->desc, w->items, w->n_items_dev, grid, a, w->stream);
+        }
     }
     if (s == FS3D_OK) w->step += (uint64_t)n_steps;
     return s;
@@ -188,7 +198,12 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
 
 fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
     if (!w) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_sync: NULL world");
-    return bounded_wait(w->stream, timeout_ns);
+    fs3d_status s = bounded_wait(w->stream, timeout_ns);
+    if (s != FS3D_OK || !w->aux) return s;
+    int err = 0;
+    FS3D_CUDA(cudaMemcpy(&err, w->aux + 3, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
+    return FS3D_OK;
 }
 
 fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* out) {

@@ -77,7 +77,9 @@ typedef struct fs3d_config {
     int steps_per_segment; /* steps per segment (graph length); default 64          */
     int ctas_per_sm;       /* persistent grid of the step kernel; 0 = all resident  */
     int use_graphs;        /* 1 (default) = run each segment as one CUDA graph       */
-    int reserved[13];
+    int use_smem;          /* 1 (default) = worlds that fit in shared memory take all
+                              their segment steps in one resident launch             */
+    int reserved[12];
 } fs3d_config;
 
 /* ---- library ---- */
@@ -154,6 +156,48 @@ fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t*
                              size_t* bytes_used, size_t* bytes_budget);
 fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream);
 fs3d_status fs3d_batch_destroy(fs3d_batch* b);
+
+/* ---- serving ----
+ * A seeded Poisson stream of requests (dims iid from {16,24,32,48,64,96,128}^3,
+ * the synthetic batch world of the request's seed, n_steps log-uniform in
+ * [min_steps, max_steps]) served by one batch with continuous batching:
+ * arrivals are admitted (generated on the device) while a segment runs, as
+ * the memory budget allows, and join at the next segment. */
+typedef struct fs3d_serve_params {
+    double lambda;           /* mean arrivals per second                          */
+    double duration_s;       /* arrival window                                     */
+    int64_t max_requests;    /* cap on the number of requests (0 = none)           */
+    uint64_t master_seed;
+    size_t hbm_budget;       /* pool budget in bytes (0 = 150 GiB)                 */
+    int steps_per_segment;   /* 0 = 64                                             */
+    int min_steps;           /* 0 = 10                                             */
+    int max_steps;           /* 0 = 1000                                           */
+    int with_hash;           /* 1 = hash every finished world (request.hash)       */
+    int reserved[8];
+} fs3d_serve_params;
+
+typedef struct fs3d_serve_request {
+    double arrival_s, admitted_s, finished_s; /* seconds from the start of the run */
+    int32_t X, Y, Z, n_steps;
+    uint64_t seed, hash;
+} fs3d_serve_request;
+
+typedef struct fs3d_serve_stats {
+    int64_t requests, completed, segments, peak_live_worlds;
+    size_t peak_bytes;
+    double wall_s, p50_ms, p99_ms, mean_ms, max_ms;
+    double voxel_updates, voxel_updates_per_s, offered_voxel_updates_per_s;
+    double reserved[8];
+} fs3d_serve_stats;
+
+/* The request stream of `p` (no GPU work): fills up to `capacity` requests and
+ * sets *n_reqs to the stream's length. */
+fs3d_status fs3d_serve_plan(const fs3d_serve_params* p, int64_t capacity, fs3d_serve_request* reqs,
+                            int64_t* n_reqs);
+/* Serves the n planned requests in real time; fills their admitted/finished
+ * times and hashes and the summary statistics. */
+fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_request* reqs,
+                           fs3d_serve_stats* stats);
 
 /* ---- render (headless) ----
  * Writes W*H RGBA float32 pixels (row 0 = top).  out_on_device = 1: `rgba`

@@ -22,12 +22,12 @@ def oracle_final(orc, fs3d, dims, seed, n, start=0):
     return g
 
 
-@pytest.mark.parametrize("use_graphs", [True, False])
-def test_batch_matches_oracle(fs3d, orc, use_graphs):
+@pytest.mark.parametrize("use_graphs,use_smem", [(True, True), (False, True), (True, False), (False, False)])
+def test_batch_matches_oracle(fs3d, orc, use_graphs, use_smem):
     worlds = small_batch(fs3d, 5, 24, max_dim=128)
     rng = np.random.default_rng(1)
     steps = [int(v) for v in rng.integers(1, 150, len(worlds))]
-    with fs3d.Batch(4 * GiB, steps_per_segment=64, use_graphs=use_graphs) as b:
+    with fs3d.Batch(4 * GiB, steps_per_segment=64, use_graphs=use_graphs, use_smem=use_smem) as b:
         tickets = []
         for (dims, seed), n in zip(worlds, steps):
             X, Y, Z = dims
