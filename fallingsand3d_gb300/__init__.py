@@ -41,7 +41,8 @@ EXPORTS = (
     "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
-    "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated",
+    "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
+    "fs3d_batch_retire_many",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_gen_parity", "fs3d_gen_pillars",
@@ -79,6 +80,11 @@ class ServeStats(C.Structure):
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
                 ("voxel_updates", C.c_double), ("voxel_updates_per_s", C.c_double),
                 ("offered_voxel_updates_per_s", C.c_double), ("reserved", C.c_double * 8)]
+
+
+class WorldSpec(C.Structure):
+    _fields_ = [("grid", C.c_void_p), ("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int), ("pad", C.c_int),
+                ("seed", C.c_uint64), ("start_step", C.c_uint64), ("n_steps", C.c_int64)]
 
 
 class Config(C.Structure):
@@ -121,6 +127,8 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_create": (S, [C.c_size_t, C.POINTER(Config), C.POINTER(vp)]),
         "fs3d_batch_admit": (S, [vp, vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
         "fs3d_batch_admit_generated": (S, [vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
+        "fs3d_batch_admit_many": (S, [vp, i32, C.POINTER(WorldSpec), C.POINTER(u64), C.POINTER(i32)]),
+        "fs3d_batch_retire_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
         "fs3d_batch_run_segment": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
@@ -380,6 +388,39 @@ class Batch:
         t = u64()
         check(lib().fs3d_batch_admit_generated(self.handle, X, Y, Z, seed, start_step, n_steps, C.byref(t)))
         return int(t.value)
+
+    def admit_many(self, grids, seeds, n_steps, start_steps=None, ptrs=None):
+        """Admits many host grids with one host wait.  `ptrs` may give raw
+        host pointers (e.g. pinned buffers) instead of the numpy arrays'.
+        Returns the tickets of the admitted worlds (in order)."""
+        n = len(grids)
+        specs = (WorldSpec * max(n, 1))()
+        keep = []
+        for a, g in enumerate(grids):
+            Y, Z, X = g.shape
+            if ptrs is None:
+                g = np.ascontiguousarray(g, dtype=np.uint8)
+                keep.append(g)
+                p = _ptr(g)
+            else:
+                p = ptrs[a]
+            specs[a] = WorldSpec(p, X, Y, Z, 0, int(seeds[a]), int(start_steps[a]) if start_steps is not None else 0,
+                                 int(n_steps[a]) if hasattr(n_steps, "__len__") else int(n_steps))
+        tickets = (u64 * max(n, 1))()
+        done = i32()
+        st = lib().fs3d_batch_admit_many(self.handle, n, specs, tickets, C.byref(done))
+        if st not in (OK, ERR_BUDGET):
+            check(st)
+        return [int(tickets[a]) for a in range(done.value)]
+
+    def retire_many(self, tickets, out_ptrs=None) -> None:
+        """Retires worlds with one host wait; out_ptrs: host buffers (or None)."""
+        n = len(tickets)
+        ts = (u64 * max(n, 1))(*tickets)
+        outs = None
+        if out_ptrs is not None:
+            outs = (vp * max(n, 1))(*[p for p in out_ptrs])
+        check(lib().fs3d_batch_retire_many(self.handle, n, ts, outs))
 
     def try_admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> Optional[int]:
         try:

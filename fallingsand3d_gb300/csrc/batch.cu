@@ -240,9 +240,10 @@ bool has_static_material(const uint8_t* g, size_t n) {
 }
 
 // Admits a world given as host bytes (g != NULL) or generated on the device
-// from its seed (g == NULL: the mixed-size batch world of that seed).
+// from its seed (g == NULL: the mixed-size batch world of that seed).  With
+// `wait` the call returns only after the host grid has been copied.
 fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t seed, uint64_t start_step,
-                  int64_t n_steps, uint64_t* ticket) {
+                  int64_t n_steps, uint64_t* ticket, bool wait = true) {
     if (!b || !ticket || X <= 0 || Y <= 0 || Z <= 0 || X > kPlaneMaxX || Y > 65536 || Z > 65536 || n_steps < 0)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit: bad args (X must be 1..2048)");
     if (!g && Y < 4) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_generated: needs Y >= 4");
@@ -280,7 +281,7 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
         if (e == cudaSuccess) e = cudaEventRecord(w.ready, b->side);
         // the caller's buffer may be reused as soon as this returns; a world
         // generated on the device has no host buffer and is not waited for
-        if (e == cudaSuccess && g) e = cudaEventSynchronize(w.ready);
+        if (e == cudaSuccess && g && wait) e = cudaEventSynchronize(w.ready);
         if (e != cudaSuccess) s = cuda_fail(e, "admit event");
     }
     if (s != FS3D_OK) {
@@ -440,13 +441,16 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
     return FS3D_OK;
 }
 
-fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out) {
-    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire: NULL batch");
+}  // extern "C"
+
+namespace {
+
+// Enqueues the read-back (if grid_out) and the release of one world on the
+// side stream; `sync` waits for the read-back before returning.
+fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync) {
     auto it = b->worlds.find(ticket);
     if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire: unknown ticket");
     BWorld& w = it->second;
-    // the world's planes are final after its last segment (or, if retired
-    // early, after the last segment enqueued so far)
     FS3D_CUDA(cudaStreamWaitEvent(b->side, w.finished ? w.finished : b->last_segment, 0));
     if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
     fs3d_status s = FS3D_OK;
@@ -458,13 +462,50 @@ fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out)
         cudaError_t e = cudaSuccess;
         if (s == FS3D_OK) e = cudaMemcpyAsync(grid_out, staging, n, cudaMemcpyDeviceToHost, b->side);
         cudaFreeAsync(staging, b->side);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
+        if (e == cudaSuccess && sync) e = cudaStreamSynchronize(b->side);
         if (s == FS3D_OK && e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire readback");
     }
     b->used -= w.bytes;
     free_world(b, w);
     b->worlds.erase(it);
     return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
+                                  int* n_admitted) {
+    if (!b || n < 0 || (n > 0 && (!specs || !tickets)) || !n_admitted)
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: bad args");
+    *n_admitted = 0;
+    fs3d_status s = FS3D_OK;
+    for (int a = 0; a < n && s == FS3D_OK; ++a) {
+        const fs3d_world_spec& p = specs[a];
+        if (!p.grid) {
+            s = set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: NULL grid");
+            break;
+        }
+        s = admit(b, p.grid, p.X, p.Y, p.Z, p.seed, p.start_step, p.n_steps, &tickets[a], false);
+        if (s == FS3D_OK) ++*n_admitted;
+    }
+    // the callers' grids may be reused once every copy has been consumed
+    FS3D_CUDA(cudaStreamSynchronize(b->side));
+    return s == FS3D_ERR_BUDGET && *n_admitted > 0 ? FS3D_ERR_BUDGET : s;
+}
+
+fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
+    if (!b || n < 0 || (n > 0 && !tickets)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: bad args");
+    fs3d_status s = FS3D_OK;
+    for (int a = 0; a < n && s == FS3D_OK; ++a) s = retire(b, tickets[a], grids_out ? grids_out[a] : nullptr, false);
+    FS3D_CUDA(cudaStreamSynchronize(b->side));
+    return s;
+}
+
+fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire: NULL batch");
+    return retire(b, ticket, grid_out, true);
 }
 
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells, size_t* bytes_used,

@@ -146,12 +146,25 @@ fs3d_status fs3d_batch_admit(fs3d_batch* b, const uint8_t* grid_host, int X, int
  * on the device straight into the pool: no host grid, no upload.  Needs Y >= 4. */
 fs3d_status fs3d_batch_admit_generated(fs3d_batch* b, int X, int Y, int Z, uint64_t seed,
                                        uint64_t start_step, int64_t n_steps, uint64_t* ticket);
+/* Many admissions with one host wait: admits specs[0..n) in order until one
+ * does not fit (FS3D_ERR_BUDGET) or fails; *n_admitted counts the admitted. */
+typedef struct fs3d_world_spec {
+    const uint8_t* grid; /* host, canonical layout                               */
+    int X, Y, Z;
+    int pad;
+    uint64_t seed, start_step;
+    int64_t n_steps;
+} fs3d_world_spec;
+fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
+                                  int* n_admitted);
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream */
 fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
 /* done = 1 once the world has taken all its steps; hash valid when done */
 fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash);
 /* frees the world's pool space; grid_out (nullable) receives the final grid */
 fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out);
+/* retire n worlds with one host wait; grids_out (nullable) holds n host pointers (nullable each) */
+fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells,
                              size_t* bytes_used, size_t* bytes_budget);
 fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream);

@@ -136,3 +136,24 @@ def test_device_generated_worlds_match_host_generator(fs3d, orc):
         ref = orc.gen_c3_world(int(seeds[0]), X, Y, Z)
         orc.run(ref, int(seeds[0]), 0, 40, nthreads=0)
         assert b.poll(t)[1] == orc.hash(ref)
+
+
+def test_admit_many_and_retire_many(fs3d, orc):
+    worlds = small_batch(fs3d, 17, 40, max_dim=96)
+    grids = [fs3d.gen_batch_world(seed, *dims) for dims, seed in worlds]
+    n = 70
+    with fs3d.Batch(GiB, steps_per_segment=64) as b:
+        tickets = b.admit_many(grids, [s for _, s in worlds], n)
+        assert len(tickets) == len(worlds)
+        for _ in range(2):
+            b.run_segment()
+        outs = [np.empty_like(g) for g in grids]
+        b.retire_many(tickets, [o.ctypes.data for o in outs])
+        assert b.stats()["live_worlds"] == 0
+    for (dims, seed), g, o in list(zip(worlds, grids, outs))[:8]:
+        ref = g.copy()
+        orc.run(ref, seed, 0, n, nthreads=0)
+        assert (o == ref).all()
+    with fs3d.Batch(2 * 64 * 64 * 16 + 200, steps_per_segment=8) as b:
+        big = [fs3d.gen_batch_world(1, 64, 64, 64)] * 3
+        assert len(b.admit_many(big, [1, 2, 3], 8)) == 2  # the third does not fit

@@ -33,12 +33,12 @@ def test_served_results_equal_alone_and_oracle(fs3d, orc):
 
 
 def test_tight_budget_defers_but_stays_exact(fs3d):
-    p = fs3d.serve_params(4000.0, 0.1, master_seed=5, min_steps=10, max_steps=80,
-                         hbm_budget=3 << 20)
+    budget = 600 << 10  # room for one of the largest worlds (512 KiB of planes) at a time
+    p = fs3d.serve_params(4000.0, 0.1, master_seed=5, min_steps=50, max_steps=300, hbm_budget=budget)
     stats, reqs = fs3d.serve(p)
     assert stats["completed"] == len(reqs)
-    assert stats["peak_bytes"] <= 3 << 20
-    waited = [r for r in reqs if r.admitted_s - r.arrival_s > 1e-3]
+    assert stats["peak_bytes"] <= budget
+    waited = [r for r in reqs if r.admitted_s - r.arrival_s > 2e-3]
     assert waited, "the budget should have made some arrivals wait"
     for r in waited[:4]:
         assert r.hash == alone_hash(fs3d, r)
