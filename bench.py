@@ -282,18 +282,23 @@ def run_fs3d(args):
     b.close()
 
     # ---- e2e through the C ABI from pinned host buffers
+    # one step = admit every world from pinned host memory (H2D + conversion),
+    # one segment, retire every world into pinned host memory (conversion + D2H)
     e2e_ms, h2d, d2h = [], cells, cells
     outs = [torch.empty(g.shape, dtype=torch.uint8, pin_memory=True) for g in host]
-    for it in range(2):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
-            ts = [eb.admit(g.numpy(), seed, S) for g, (_, seed) in zip(host, worlds)]
+    seeds = [seed for _, seed in worlds]
+    in_ptrs = [g.data_ptr() for g in host]
+    out_ptrs = [o.data_ptr() for o in outs]
+    with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
+        for it in range(4):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ts = eb.admit_many(host, seeds, S, ptrs=in_ptrs)
             eb.run_segment()
-            for t, o in zip(ts, outs):
-                fs3d.check(fs3d.lib().fs3d_batch_retire(eb.handle, t, o.data_ptr()))
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_val = cells * S / (e2e_ms[-1] / 1e3)
+            eb.retire_many(ts, out_ptrs)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = e2e_ms[1:]  # the first call also captures the segment graph
+    e2e_val = cells * S / (float(np.mean(e2e_ms)) / 1e3)
 
     # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
     offs, off = [], 0
@@ -392,7 +397,7 @@ def run_fs3d(args):
                            "layout": "2-bit planes", "parallelism": f"replicas x{world}"},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                        "ms": round(e2e_ms[-1], 2),
+                        "ms": round(float(np.mean(e2e_ms)), 2),
                         "path": "fs3d_batch_admit (pinned) + fs3d_batch_run_segment + fs3d_batch_retire"},
                 "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
                                     "launches_per_segment": S * len(worlds),
