@@ -81,11 +81,12 @@ struct fs3d_batch {
     uint64_t next_ticket = 1;
     PinnedArray<PlaneWorld> tw;
     PinnedArray<PlaneItem> ti;
-    PinnedArray<int> tn;  // {per-step items, resident worlds}
-    PinnedArray<int> to;  // resident worlds (indices into tw), largest first
-    int* counter = nullptr;  // work counter of the resident kernel
+    PinnedArray<int> tn;  // meta: {per-step items, resident count per class, offset per class}
+    PinnedArray<int> to;  // resident worlds (indices into tw) by class, largest first
+    int* counter = nullptr;  // work counters of the resident kernels, one per class
     int* err = nullptr;      // set by a kernel whose bounded wait gave up
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join[kResidentClasses + 1] = {};
+    cudaStream_t branch[kResidentClasses + 1] = {};  // capture branches of a segment
     cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
     cudaEvent_t last_segment = nullptr;
     std::vector<cudaEvent_t> pending_ready;  // admissions the next segment must wait for
@@ -127,23 +128,28 @@ void free_world(fs3d_batch* b, BWorld& w) {
     w.ready = w.finished = nullptr;
 }
 
-// One segment: the resident kernel (worlds that fit in shared memory, all
-// their steps in one launch) on `a`, concurrently with steps_per_segment
-// launches of the per-step kernel (the larger worlds) on `c`.
-fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, cudaStream_t c) {
-    if (a != c) {
+// One segment on stream `a`: the resident kernel of every class (worlds that
+// fit in shared memory take all their steps in one launch) and
+// steps_per_segment launches of the per-step kernel (the larger worlds).
+// With `fork` each goes to its own branch stream so they run concurrently.
+fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork) {
+    if (fork) {
         FS3D_CUDA(cudaEventRecord(b->fork, a));
-        FS3D_CUDA(cudaStreamWaitEvent(c, b->fork, 0));
+        for (cudaStream_t br : b->branch) FS3D_CUDA(cudaStreamWaitEvent(br, b->fork, 0));
     }
     fs3d_status s = FS3D_OK;
-    if (b->cfg.use_smem) s = launch_plane_segment_smem(b->tw.d, b->to.d, b->tn.d + 1, b->counter, b->err, a);
+    if (b->cfg.use_smem)
+        for (int c = 0; c < kResidentClasses && s == FS3D_OK; ++c)
+            s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
+                                              fork ? b->branch[c] : a);
     for (int k = 0; k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
-        s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, c);
+        s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, fork ? b->branch[kResidentClasses] : a);
     if (s != FS3D_OK) return s;
-    if (a != c) {
-        FS3D_CUDA(cudaEventRecord(b->join, c));
-        FS3D_CUDA(cudaStreamWaitEvent(a, b->join, 0));
-    }
+    if (fork)
+        for (int c = 0; c <= kResidentClasses; ++c) {
+            FS3D_CUDA(cudaEventRecord(b->join[c], b->branch[c]));
+            FS3D_CUDA(cudaStreamWaitEvent(a, b->join[c], 0));
+        }
     return FS3D_OK;
 }
 
@@ -152,24 +158,18 @@ fs3d_status capture_graph(fs3d_batch* b) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
-    cudaStream_t cs, cs2;
+    cudaStream_t cs;
     FS3D_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    cudaError_t e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
-        cudaStreamDestroy(cs);
-        return cuda_fail(e, "cudaStreamCreate");
-    }
     cudaGraph_t g = nullptr;
     fs3d_status s = FS3D_OK;
-    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        s = enqueue_segment(b, cs, cs2);
+        s = enqueue_segment(b, cs, true);
         e = cudaStreamEndCapture(cs, &g);
     }
     if (e == cudaSuccess && s == FS3D_OK) e = cudaGraphInstantiate(&b->graph, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
-    cudaStreamDestroy(cs2);
     if (s != FS3D_OK) return s;
     if (e != cudaSuccess) return cuda_fail(e, "segment graph capture");
     b->graph_worlds = b->tw.d;
@@ -198,11 +198,14 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int) * kResidentClasses);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    for (int c = 0; c <= kResidentClasses && e == cudaSuccess; ++c) {
+        e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->branch[c], cudaStreamNonBlocking);
+    }
     if (e == cudaSuccess) {
         // keep freed pool memory cached so admissions after retirements are cheap
         int dev = 0;
@@ -213,7 +216,7 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
         }
     }
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_create");
-    if (s == FS3D_OK) s = b->tn.reserve(2);
+    if (s == FS3D_OK) s = b->tn.reserve(1 + 2 * kResidentClasses);
     if (s != FS3D_OK) {
         fs3d_batch_destroy(b);
         return s;
@@ -314,17 +317,20 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     const int S = b->cfg.steps_per_segment;
     // the pinned tables may be rewritten once the previous upload has run
     FS3D_CUDA(cudaEventSynchronize(b->tables_free));
-    const size_t lim = b->cfg.use_smem ? (size_t)smem_world_limit() : 0;
-    size_t nw_ = 0, ni = 0, ns = 0;
+    // resident class of every running world (-1: stepped by the per-step kernel)
+    std::vector<std::pair<int, BWorld*>> run;
+    size_t ni = 0, ns = 0;
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
-        ++nw_;
-        if (plane_bytes(w.X, w.Y, w.Z) <= lim)
+        const int c = b->cfg.use_smem ? resident_class(w.X, w.Y, w.Z) : -1;
+        run.emplace_back(c, &w);
+        if (c >= 0)
             ++ns;
         else
             ni += (size_t)plane_items_for(w.Y, w.Z, w.nw);
     }
+    const size_t nw_ = run.size();
     if (nw_ == 0) return FS3D_OK;
     // growing the tables frees device arrays a running segment may still read
     if (nw_ > b->tw.cap || ni > b->ti.cap || ns > b->to.cap) FS3D_CUDA(cudaStreamSynchronize(b->stream));
@@ -332,10 +338,10 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     if (s == FS3D_OK) s = b->ti.reserve(ni > 0 ? ni : 1);
     if (s == FS3D_OK) s = b->to.reserve(ns > 0 ? ns : 1);
     if (s != FS3D_OK) return s;
-    size_t wi = 0, ii = 0, si = 0;
-    for (auto& kv : b->worlds) {
-        BWorld& w = kv.second;
-        if (w.done) continue;
+    std::vector<int> by_class[kResidentClasses];
+    size_t ii = 0;
+    for (size_t wi = 0; wi < nw_; ++wi) {
+        const BWorld& w = *run[wi].second;
         const int steps = (int)(w.remaining < S ? w.remaining : S);
         PlaneWorld& d = b->tw.h[wi];
         memset(&d, 0, sizeof(d));
@@ -348,22 +354,28 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         d.nw = w.nw;
         d.steps = steps;
         d.lg = plane_lg(w.nw);
-        if (plane_bytes(w.X, w.Y, w.Z) <= lim) {
-            b->to.h[si++] = (int)wi;
+        if (run[wi].first >= 0) {
+            by_class[run[wi].first].push_back((int)wi);
         } else {
             const int per = 32 >> d.lg, items = plane_items_for(w.Y, w.Z, w.nw);
             for (int a = 0; a < items; ++a) b->ti.h[ii++] = PlaneItem{(int32_t)wi, a * per};
         }
-        ++wi;
     }
-    // largest resident worlds first, so the tail of the launch is short
-    std::sort(b->to.h, b->to.h + si, [&](int x, int y) {
-        const PlaneWorld &a = b->tw.h[x], &c = b->tw.h[y];
-        const int64_t ca = (int64_t)a.X * a.Y * a.Z * a.steps, cc = (int64_t)c.X * c.Y * c.Z * c.steps;
-        return ca != cc ? ca > cc : x < y;
-    });
-    b->tn.h[0] = (int)ii;
-    b->tn.h[1] = (int)si;
+    // per class, largest worlds first, so each launch ends with short work
+    int* meta = b->tn.h;
+    meta[0] = (int)ii;
+    size_t si = 0;
+    for (int c = 0; c < kResidentClasses; ++c) {
+        std::vector<int>& v = by_class[c];
+        std::sort(v.begin(), v.end(), [&](int x, int y) {
+            const PlaneWorld &a = b->tw.h[x], &e2 = b->tw.h[y];
+            const int64_t ca = (int64_t)a.X * a.Y * a.Z * a.steps, cc = (int64_t)e2.X * e2.Y * e2.Z * e2.steps;
+            return ca != cc ? ca > cc : x < y;
+        });
+        meta[1 + c] = (int)v.size();
+        meta[1 + kResidentClasses + c] = (int)si;
+        for (int x : v) b->to.h[si++] = x;
+    }
     // admissions complete before the segment reads their planes
     for (auto& kv : b->worlds)
         if (kv.second.ready) {
@@ -371,10 +383,11 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
             cudaEventDestroy(kv.second.ready);
             kv.second.ready = nullptr;
         }
-    FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * wi, cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * nw_, cudaMemcpyHostToDevice, b->stream));
     if (ii) FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
     if (si) FS3D_CUDA(cudaMemcpyAsync(b->to.d, b->to.h, sizeof(int) * si, cudaMemcpyHostToDevice, b->stream));
-    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, 2 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * (1 + 2 * kResidentClasses), cudaMemcpyHostToDevice,
+                              b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
     if (b->cfg.use_graphs) {
         if (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d) {
@@ -382,9 +395,9 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
             if (s != FS3D_OK) return s;
         }
         FS3D_CUDA(cudaGraphLaunch(b->graph, b->stream));
-        note_launch((uint64_t)S + 1);
+        note_launch((uint64_t)S + (b->cfg.use_smem ? kResidentClasses : 0));
     } else {
-        s = enqueue_segment(b, b->stream, b->stream);
+        s = enqueue_segment(b, b->stream, false);
         if (s != FS3D_OK) return s;
     }
     FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
@@ -542,7 +555,10 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     cudaFree(b->counter);
     cudaFree(b->err);
     if (b->fork) cudaEventDestroy(b->fork);
-    if (b->join) cudaEventDestroy(b->join);
+    for (int c = 0; c <= kResidentClasses; ++c) {
+        if (b->join[c]) cudaEventDestroy(b->join[c]);
+        if (b->branch[c]) cudaStreamDestroy(b->branch[c]);
+    }
     if (b->tables_free) cudaEventDestroy(b->tables_free);
     if (b->last_segment) cudaEventDestroy(b->last_segment);
     if (b->stream) cudaStreamDestroy(b->stream);

@@ -18,6 +18,7 @@
 // read for computation and written by exactly one lane.  When X is a multiple
 // of 64 the odd phase has one extra half block per row-pair (cells x = X-1,
 // x = X outside), which the last lane runs with the scalar rule.
+#include <cooperative_groups.h>
 #include <stdint.h>
 
 #include "fs3d_common.h"
@@ -237,113 +238,240 @@ __device__ __forceinline__ void bulk_store_wait(void* gdst, const void* smem_src
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
-// A block row-pair of a world held in shared memory (rows r = y*Z + z of nw
-// uint4 words).  Every lane of the warp calls this.
-__device__ __forceinline__ void smem_rowpair(uint4* rows, const PlaneWorld& w, int o, uint32_t sk, int rp,
-                                             bool valid, int gl, int G) {
-    const int NBZ = nblocks(w.Z, o);
-    const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
+// The rows of one world held in shared memory by the CTAs of a cluster: CTA
+// r holds rows y in [lo_r, hi_r) (lo_r even), stored as ((y - lo_r)*Z + z)*nw
+// + word.  `left` is the shared memory of CTA r-1 (null for r == 0): the only
+// row a CTA reads outside its slab is y = lo_r - 1, in the odd phase.
+template <bool CL>
+struct SlabView {
+    uint4* mine;
+    uint4* left;
+    int lo, hi, left_lo, Z, nw;
+    __device__ __forceinline__ uint4* at(int y, int z, int g) const {
+        if (!CL || y >= lo) return mine + ((y - lo) * Z + z) * nw + g;
+        return left + ((y - left_lo) * Z + z) * nw + g;
+    }
+};
+
+// A block row-pair (j, k) of a world held in shared memory.  Every lane of
+// the warp calls this.
+template <bool CL>
+__device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk, int j,
+                                             int k, bool valid, int gl, int G) {
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
     const int y0 = 2 * j - o, z0 = 2 * k - o;
     const bool has = valid && gl < w.nw;
     uint4 q[4], q0[4];
-    int idx[4];
+    uint4* ptr[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
         const bool in = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
-        idx[a] = in ? (y * w.Z + z) * w.nw + gl : -1;
-        q[a] = in ? rows[idx[a]] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        ptr[a] = in ? v.at(y, z, gl) : nullptr;
+        q[a] = in ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
         q0[a] = q[a];
     }
     rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        if (idx[a] >= 0 && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
-            rows[idx[a]] = q[a];
+        if (ptr[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
+            *ptr[a] = q[a];
 }
 
-// Persistent: each CTA takes worlds in the given order from `counter`, loads
-// the world's planes into shared memory with one TMA bulk copy, runs its
-// `steps` steps (one __syncthreads per step: the next phase pairs different
-// rows), and writes the planes back with one TMA bulk store.  Worlds are
-// independent, so CTAs never wait on one another.
-__global__ void __launch_bounds__(kSmemThreads) k_plane_segment_smem(const PlaneWorld* __restrict__ worlds,
-                                                                    const int* __restrict__ order,
-                                                                    const int* __restrict__ n_p, int* counter,
-                                                                    int* err) {
+// first row of slab r of CS slabs (even, so even-phase row-pairs never straddle)
+__device__ __forceinline__ int slab_lo(int Y, int r, int CS) { return 2 * ((r * ((Y + 1) / 2)) / CS); }
+
+// Persistent resident segment kernel.  A group of CS CTAs (a thread-block
+// cluster when CS > 1) takes worlds of its class, largest first, from
+// `counter`.  Each CTA loads its slab of the world's planes into shared
+// memory with one TMA bulk copy, the group runs the world's segment steps
+// (one CTA / cluster barrier per step: the next phase pairs different rows;
+// the one row a CTA reads from its neighbour travels through distributed
+// shared memory), and each CTA writes its slab back with one TMA bulk store.
+// Worlds are independent, so groups never wait on one another.
+// meta: [0] per-step items, [1 + c] resident worlds of class c, [1 + kResidentClasses + c] their offset in order[].
+template <int NT, bool CL>
+__global__ void __launch_bounds__(NT) k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
+                                                             const int* __restrict__ order,
+                                                             const int* __restrict__ meta, int cls, int CS,
+                                                             int* counter, int* err) {
     extern __shared__ __align__(128) uint4 srows[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int item;
-    const int n = *n_p;
+    namespace cg = cooperative_groups;
+    const int n = meta[1 + cls], off = meta[1 + kResidentClasses + cls];
+    if (!CL) CS = 1;
+    const int r = CL ? (int)cg::this_cluster().block_rank() : 0;
+    auto group_sync = [&]() {
+        if (CL)
+            cg::this_cluster().sync();
+        else
+            __syncthreads();
+    };
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     uint32_t phase = 0;
     const int lane = threadIdx.x & 31;
+    uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
     for (;;) {
-        if (threadIdx.x == 0) item = atomicAdd(counter, 1);
-        __syncthreads();
-        const int it = item;
-        __syncthreads();
+        if (r == 0 && threadIdx.x == 0) item = atomicAdd(counter, 1);
+        group_sync();
+        const int it = CL ? *cg::this_cluster().map_shared_rank(&item, 0) : item;
+        group_sync();
         if (it >= n) break;
-        const PlaneWorld w = worlds[order[it]];
+        const PlaneWorld w = worlds[order[off + it]];
         if (w.steps <= 0) continue;
-        const uint32_t bytes = (uint32_t)w.Y * (uint32_t)w.Z * (uint32_t)w.nw * 16u;
-        if (threadIdx.x == 0) bulk_load(srows, w.rows, bytes, &bar);
-        if (!mbar_wait(&bar, phase)) {
-            if (threadIdx.x == 0) atomicExch(err, 1);
-            mbar_wait(&bar, phase);  // give a late copy a second bounded chance to land
-            return;
+        SlabView<CL> v;
+        v.lo = slab_lo(w.Y, r, CS);
+        v.hi = r == CS - 1 ? w.Y : slab_lo(w.Y, r + 1, CS);
+        v.left_lo = r > 0 ? slab_lo(w.Y, r - 1, CS) : 0;
+        v.mine = srows;
+        v.left = left;
+        v.Z = w.Z;
+        v.nw = w.nw;
+        const uint32_t row_bytes = (uint32_t)w.Z * (uint32_t)w.nw * 16u;
+        const uint32_t bytes = (uint32_t)(v.hi - v.lo) * row_bytes;
+        uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
+        if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
+        if (bytes) {
+            if (!mbar_wait(&bar, phase)) {
+                if (threadIdx.x == 0) atomicExch(err, 1);
+                mbar_wait(&bar, phase);  // give a late copy a second bounded chance to land
+                return;
+            }
+            phase ^= 1u;
         }
-        phase ^= 1u;
-        const int G = 1 << w.lg, per = kSmemThreads >> w.lg;
+        group_sync();  // every slab is loaded before a neighbour reads it
+        const int G = 1 << w.lg, per = NT >> w.lg;
         const int gl = lane & (G - 1);
         for (int s = 0; s < w.steps; ++s) {
             const uint64_t t = w.t + (uint64_t)s;
             const int o = (int)(t & 1u);
             const uint32_t sk = stepkey(w.seed, t);
-            const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
+            const int NBZ = nblocks(w.Z, o);
+            const int j_lo = v.lo / 2, j_hi = (r == CS - 1) ? nblocks(w.Y, o) : v.hi / 2;
+            const int nrp = (j_hi - j_lo) * NBZ;
             for (int base = 0; base < nrp; base += per) {
                 const int rp = base + (int)(threadIdx.x >> w.lg);
-                smem_rowpair(srows, w, o, sk, rp, rp < nrp, gl, G);
+                const bool valid = rp < nrp;
+                const int jj = valid ? rp / NBZ : 0;
+                slab_rowpair(v, w, o, sk, j_lo + jj, valid ? rp - jj * NBZ : 0, valid, gl, G);
             }
-            __syncthreads();
+            group_sync();
         }
         // make the threads' shared-memory writes visible to the bulk copy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (threadIdx.x == 0) bulk_store_wait(w.rows, srows, bytes);
-        __syncthreads();
+        if (threadIdx.x == 0 && bytes) bulk_store_wait(gslab, srows, bytes);
+        group_sync();  // the slab is free again (and no neighbour still reads it)
     }
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-int smem_world_limit() {
-    static int lim = -1;
-    if (lim < 0) {
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        lim = optin - 1024;  // room for the kernel's static shared memory
-        if (lim < 0) lim = 0;
-        if (cudaFuncSetAttribute(k_plane_segment_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
-            cudaSuccess)
-            lim = 0;
-    }
-    return lim;
+namespace {
+
+struct ResidentCfg {
+    int threads, ctas_per_sm, cs;
+    int smem;  // dynamic shared memory per CTA (bytes), 0 = class unavailable
+    const void* fn;
+};
+
+ResidentCfg g_classes[kResidentClasses];
+bool g_classes_ready = false;
+
+template <int NT, bool CL>
+const void* resident_fn() {
+    return reinterpret_cast<const void*>(&k_plane_segment_resident<NT, CL>);
 }
 
-fs3d_status launch_plane_segment_smem(const PlaneWorld* worlds, const int* order, const int* n_dev, int* counter,
-                                      int* err, cudaStream_t st) {
-    const int lim = smem_world_limit();
-    if (lim <= 0) return set_error(FS3D_ERR_CUDA, "shared-memory segment kernel unavailable");
+void init_classes() {
+    if (g_classes_ready) return;
+    int dev = 0, per_sm = 0, optin = 0, reserved = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    const int kStatic = 256;  // the kernel's own shared variables, rounded up
+    const ResidentCfg base[kResidentClasses] = {
+        {128, 4, 1, 0, resident_fn<128, false>()}, {256, 2, 1, 0, resident_fn<256, false>()},
+        {512, 1, 1, 0, resident_fn<512, false>()}, {512, 1, 2, 0, resident_fn<512, true>()},
+        {512, 1, 4, 0, resident_fn<512, true>()},  {512, 1, 8, 0, resident_fn<512, true>()}};
+    for (int c = 0; c < kResidentClasses; ++c) {
+        ResidentCfg k = base[c];
+        int smem = per_sm / k.ctas_per_sm - reserved - kStatic;
+        if (smem > optin - kStatic) smem = optin - kStatic;
+        smem = smem / 16 * 16;
+        if (smem <= 0 || cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            smem = 0;
+        int fit = 0;
+        if (smem && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k.fn, k.threads, smem) != cudaSuccess ||
+                     fit < k.ctas_per_sm))
+            smem = 0;
+        k.smem = smem;
+        g_classes[c] = k;
+    }
+    cudaGetLastError();  // a refused attribute leaves the class unused, not an error
+    g_classes_ready = true;
+}
+
+}  // namespace
+
+int resident_class(int X, int Y, int Z) {
+    init_classes();
+    const int64_t row_bytes = (int64_t)Z * plane_nw(X) * 16;
+    for (int c = 0; c < kResidentClasses; ++c) {
+        const ResidentCfg& k = g_classes[c];
+        if (!k.smem) continue;
+        // every slab holds at most 2*ceil(NYP/CS) rows (NYP = row pairs); each
+        // slab must be non-empty so the row below a slab is in its neighbour
+        const int64_t nyp = (Y + 1) / 2;
+        const int64_t mx = k.cs == 1 ? Y : 2 * ((nyp + k.cs - 1) / k.cs);
+        if (mx * row_bytes <= k.smem && (k.cs == 1 || nyp >= k.cs)) return c;
+    }
+    return -1;
+}
+
+int smem_world_limit() {
+    init_classes();
+    return g_classes[2].smem;
+}
+
+fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
+                                          int* counter, int* err, cudaStream_t st) {
+    init_classes();
+    const ResidentCfg& k = g_classes[cls];
+    if (!k.smem) return set_error(FS3D_ERR_CUDA, "resident segment kernel unavailable for this class");
     FS3D_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    k_plane_segment_smem<<<sm_count_public(), kSmemThreads, lim, st>>>(worlds, order, n_dev, counter, err);
-    FS3D_CHECK_LAUNCH("smem segment launch");
+    const int groups = sm_count_public() * k.ctas_per_sm / k.cs;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)(groups * k.cs));
+    lc.blockDim = dim3((unsigned)k.threads);
+    lc.dynamicSmemBytes = (size_t)k.smem;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)k.cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    lc.attrs = attr;
+    lc.numAttrs = k.cs > 1 ? 1 : 0;
+    const int CS = k.cs;
+    cudaError_t e;
+    if (k.cs > 1)
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<512, true>, worlds, order, meta, cls, CS, counter, err);
+    else if (k.threads == 128)
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<128, false>, worlds, order, meta, cls, CS, counter, err);
+    else if (k.threads == 256)
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<256, false>, worlds, order, meta, cls, CS, counter, err);
+    else
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<512, false>, worlds, order, meta, cls, CS, counter, err);
+    if (e != cudaSuccess) return cuda_fail(e, "resident segment launch");
+    note_launch();
     return FS3D_OK;
 }
+
 int sm_count_public();
 
 static int conv_grid(int64_t n) {

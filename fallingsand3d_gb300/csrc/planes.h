@@ -30,14 +30,20 @@ inline int plane_nw(int X) { return (X + 63) / 64; }
 inline size_t plane_bytes(int X, int Y, int Z) { return (size_t)Y * Z * plane_nw(X) * sizeof(uint4); }
 constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 
-constexpr int kSmemThreads = 512;  // threads of the shared-memory segment kernel
+// Resident segment classes: worlds whose planes fit in shared memory take
+// all their segment steps in one launch.  Classes 0..2 hold a world in one CTA
+// of 128 / 256 / 512 threads (4 / 2 / 1 CTAs per SM); classes 3..5 split a
+// world into y-slabs over a cluster of 2 / 4 / 8 CTAs.
+constexpr int kResidentClasses = 6;
+// smallest class that holds a world of these dims, -1 if none does
+int resident_class(int X, int Y, int Z);
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable
 int smem_world_limit();
-// One launch steps every world in order[0..*n_dev) through its segment steps
-// inside shared memory (worlds must fit smem_world_limit()).  *err is set to
-// 1 if a bulk copy does not complete within the wait limit.
-fs3d_status launch_plane_segment_smem(const PlaneWorld* worlds, const int* order, const int* n_dev, int* counter,
-                                      int* err, cudaStream_t st);
+// One launch steps every world of class `cls` (order[meta[1+K+cls] ...],
+// meta[1+cls] of them) through its segment steps in shared memory.  *err is
+// set to 1 if a bulk copy does not complete within the wait limit.
+fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
+                                          int* counter, int* err, cudaStream_t st);
 
 int plane_lg(int nw);
 int plane_items_for(int Y, int Z, int nw);

@@ -28,12 +28,20 @@ struct fs3d_world {
     PlaneItem* items = nullptr;
     int* n_items_dev = nullptr;
     int n_items = 0;
-    int* aux = nullptr;  // {1 (resident world count), 0 (order[0]), work counter, error flag}
+    int* aux = nullptr;  // resident tables, see kAux*
+    int cls = -1;        // resident class (-1: stepped by the per-step kernel)
     unsigned long long* hash_dev = nullptr;
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
 
 namespace {
+
+// layout of fs3d_world::aux (device ints)
+constexpr int kAuxMeta = 0;                              // 1 + 2*classes ints
+constexpr int kAuxOrder = 1 + 2 * kResidentClasses;      // order[0] = 0
+constexpr int kAuxCounter = kAuxOrder + 1;
+constexpr int kAuxErr = kAuxCounter + 1;
+constexpr int kAuxInts = kAuxErr + 1;
 
 bool dims_ok(int X, int Y, int Z) {
     return X > 0 && Y > 0 && Z > 0 && X <= (1 << 16) && Y <= (1 << 16) && Z <= (1 << 16);
@@ -145,7 +153,10 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
         e = cudaMalloc((void**)&w->desc, sizeof(PlaneWorld));
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->items, sizeof(PlaneItem) * items.size());
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->n_items_dev, sizeof(int));
-        const int aux[4] = {1, 0, 0, 0};
+        // resident tables: meta (one world in its class), order {0}, work counter, error flag
+        int aux[kAuxInts] = {};
+        w->cls = resident_class(X, Y, Z);
+        if (w->cls >= 0) aux[1 + w->cls] = 1;
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->aux, sizeof(aux));
         if (e == cudaSuccess) e = cudaMemcpy(w->aux, aux, sizeof(aux), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
@@ -183,9 +194,10 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
         // pageable source: staged before the call returns
         FS3D_CUDA(cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream));
         s = FS3D_OK;
-        if (plane_bytes(w->X, w->Y, w->Z) <= (size_t)smem_world_limit()) {
-            // the whole world fits in one CTA's shared memory: all n steps in one launch
-            s = launch_plane_segment_smem(w->desc, w->aux + 1, w->aux, w->aux + 2, w->aux + 3, w->stream);
+        if (w->cls >= 0) {
+            // the world fits in shared memory (one CTA or a cluster): all n steps in one launch
+            s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
+                                              w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
         } else {
             const int grid = plane_step_grid(w->n_items);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
@@ -201,7 +213,7 @@ fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
     fs3d_status s = bounded_wait(w->stream, timeout_ns);
     if (s != FS3D_OK || !w->aux) return s;
     int err = 0;
-    FS3D_CUDA(cudaMemcpy(&err, w->aux + 3, sizeof(int), cudaMemcpyDeviceToHost));
+    FS3D_CUDA(cudaMemcpy(&err, w->aux + kAuxErr, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
     return FS3D_OK;
 }

@@ -157,3 +157,39 @@ def test_admit_many_and_retire_many(fs3d, orc):
     with fs3d.Batch(2 * 64 * 64 * 16 + 200, steps_per_segment=8) as b:
         big = [fs3d.gen_batch_world(1, 64, 64, 64)] * 3
         assert len(b.admit_many(big, [1, 2, 3], 8)) == 2  # the third does not fit
+
+
+# dims that land in each resident class (one CTA of 128/256/512 threads,
+# clusters of 2/4/8 CTAs) and one too large to be resident
+CLASS_DIMS = [(16, 16, 16), (64, 64, 64), (64, 96, 128), (96, 96, 96), (128, 128, 128), (128, 256, 128),
+              (64, 512, 128), (40, 37, 21), (130, 66, 90)]
+
+
+@pytest.mark.parametrize("use_smem", [True, False])
+def test_every_resident_class_matches_oracle(fs3d, orc, use_smem):
+    n = 67  # odd and not a multiple of the segment: phases and partial segments
+    with fs3d.Batch(8 * GiB, steps_per_segment=32, use_smem=use_smem) as b:
+        tickets = []
+        for w, (X, Y, Z) in enumerate(CLASS_DIMS):
+            g = fs3d.gen_batch_world(1000 + w, X, Y, Z)
+            tickets.append((b.admit(g, 1000 + w, n, start_step=w), g))
+        for _ in range(3):
+            b.run_segment()
+        b.sync()
+        for w, ((t, g), dims) in enumerate(zip(tickets, CLASS_DIMS)):
+            ref = g.copy()
+            orc.run(ref, 1000 + w, w, n, nthreads=0)
+            assert b.poll(t)[1] == orc.hash(ref), dims
+
+
+@pytest.mark.parametrize("dims", CLASS_DIMS[:6])
+def test_world_resident_path_matches_oracle(fs3d, orc, dims):
+    X, Y, Z = dims
+    g = fs3d.gen_batch_world(7, X, Y, Z)
+    with fs3d.World(g, 7, 3, fs3d.LAYOUT_PLANES) as w:
+        w.step(45)
+        w.step(1)
+        ref = g.copy()
+        orc.run(ref, 7, 3, 46, nthreads=0)
+        got = w.read()
+    assert (got == ref).all()
