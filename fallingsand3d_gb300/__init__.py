@@ -38,7 +38,7 @@ ERR_IO = -9
 # every entry point of include/fs3d.h (checked by the tests)
 EXPORTS = (
     "fs3d_abi_version", "fs3d_status_string", "fs3d_last_error", "fs3d_kernel_launch_count",
-    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_hash_device", "fs3d_first_diff_device",
+    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_run_device", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
@@ -109,6 +109,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_default_config": (Config, []),
         "fs3d_step_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_step_device_simple": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_run_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_hash_device": (S, [vp, i64, vp, C.POINTER(u64)]),
         "fs3d_first_diff_device": (S, [vp, vp, i64, vp, C.POINTER(i64)]),
         "fs3d_world_create": (S, [vp, i32, i32, i32, u64, u64, i32, C.POINTER(vp)]),
@@ -231,6 +232,11 @@ def camera_world_view(X: int, Y: int, Z: int, W: int, H: int) -> Camera:
 def step_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
     """Drop-in step of a device grid (pointer) in place; async on `stream`."""
     check(lib().fs3d_step_device(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
+
+
+def run_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
+    """n steps of a device grid through the bit-plane kernels (device scratch)."""
+    check(lib().fs3d_run_device(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
 
 
 def step_device_simple(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int,

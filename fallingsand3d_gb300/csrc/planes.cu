@@ -314,7 +314,8 @@ __global__ void __launch_bounds__(NT) k_plane_segment_resident(const PlaneWorld*
     const int lane = threadIdx.x & 31;
     uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
     for (;;) {
-        if (r == 0 && threadIdx.x == 0) item = atomicAdd(counter, 1);
+        // after an error every group stops taking worlds (and all of a cluster stop together)
+        if (r == 0 && threadIdx.x == 0) item = *(volatile int*)err ? n : atomicAdd(counter, 1);
         group_sync();
         const int it = CL ? *cg::this_cluster().map_shared_rank(&item, 0) : item;
         group_sync();
@@ -333,18 +334,25 @@ __global__ void __launch_bounds__(NT) k_plane_segment_resident(const PlaneWorld*
         const uint32_t bytes = (uint32_t)(v.hi - v.lo) * row_bytes;
         uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
         if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
+        bool ok = true;
         if (bytes) {
-            if (!mbar_wait(&bar, phase)) {
-                if (threadIdx.x == 0) atomicExch(err, 1);
-                mbar_wait(&bar, phase);  // give a late copy a second bounded chance to land
-                return;
-            }
+            ok = mbar_wait(&bar, phase);
+            if (!ok) ok = mbar_wait(&bar, phase);  // a second bounded chance for a late copy
             phase ^= 1u;
         }
+        // A copy that never landed poisons the world: the error flag is
+        // raised, this CTA still takes part in every barrier of its group but
+        // touches no memory, and the group stops before its next world.
+        const bool poisoned = __syncthreads_or(!ok) != 0;
+        if (poisoned && threadIdx.x == 0) atomicExch(err, 1);
         group_sync();  // every slab is loaded before a neighbour reads it
         const int G = 1 << w.lg, per = NT >> w.lg;
         const int gl = lane & (G - 1);
         for (int s = 0; s < w.steps; ++s) {
+            if (poisoned) {
+                group_sync();
+                continue;
+            }
             const uint64_t t = w.t + (uint64_t)s;
             const int o = (int)(t & 1u);
             const uint32_t sk = stepkey(w.seed, t);
@@ -362,7 +370,7 @@ __global__ void __launch_bounds__(NT) k_plane_segment_resident(const PlaneWorld*
         // make the threads' shared-memory writes visible to the bulk copy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (threadIdx.x == 0 && bytes) bulk_store_wait(gslab, srows, bytes);
+        if (threadIdx.x == 0 && bytes && !poisoned) bulk_store_wait(gslab, srows, bytes);
         group_sync();  // the slab is free again (and no neighbour still reads it)
     }
 }

@@ -203,19 +203,23 @@ __global__ void __launch_bounds__(256) k_step_rows16(uint8_t* __restrict__ grid,
 // only the 16-byte pieces whose cells changed class.
 // ---------------------------------------------------------------------------
 
-// bits 7, 15, 23, 31 -> bits 0..3
-__device__ __forceinline__ uint32_t gather_hi4(uint32_t m) { return ((m >> 7) * 0x10204080u) >> 28; }
+// bits 0, 8, 16, 24 -> bits 0..3
+__device__ __forceinline__ uint32_t gather_lo4(uint32_t m) { return (m * 0x10204080u) >> 28; }
 // bits 0..3 -> bit 0 of bytes 0..3
 __device__ __forceinline__ uint32_t spread4(uint32_t n) { return (n * 0x00204081u) & 0x01010101u; }
 
-// four cells (one byte each) -> nibbles of A (sand or water) and B (water or solid)
+// Four cells (one byte each) -> nibbles of A (sand or water) and B (water or
+// solid).  A value 0..3 is its own 2-bit code (A = bit 1, B = bit 0); any
+// value >= 4 is static and solid, code (0,1).
 __device__ __forceinline__ void classify4(uint32_t v, uint32_t& a4, uint32_t& b4) {
-    const uint32_t ta = (v & 0xFEFEFEFEu) ^ 0x02020202u;        // byte 0 iff value in {2,3}
-    const uint32_t nza = ((ta & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | ta;  // bit 7 set iff byte != 0
-    a4 = gather_hi4(~nza & 0x80808080u);
-    const uint32_t tb = v & 0xFDFDFDFDu;                        // byte 0 iff value in {0,2}
-    const uint32_t nzb = ((tb & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | tb;
-    b4 = gather_hi4(nzb & 0x80808080u);
+    const uint32_t big = v & 0xFCFCFCFCu;
+    if (big) {
+        const uint32_t nz = ((big & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | big;  // bit 7 set iff byte >= 4
+        const uint32_t m = ((nz & 0x80808080u) >> 7) * 0xFFu;
+        v = (v & ~m) | (0x01010101u & m);
+    }
+    a4 = gather_lo4((v >> 1) & 0x01010101u);
+    b4 = gather_lo4(v & 0x01010101u);
 }
 
 // 64 cells (16 words, x = 4k + byte) -> {A even, A odd, B even, B odd}
@@ -245,9 +249,9 @@ __device__ __forceinline__ uint32_t planes_to_bytes64(uint32_t (&w)[16], const u
         const uint32_t ce = (che >> (4 * p)) & 0xFu, co = (cho >> (4 * p)) & 0xFu;
         if (!(ce | co)) continue;
         pairs |= 1u << p;
-        const uint32_t sae = spread4((n.x >> (4 * p)) & 0xFu), sbe = spread4((n.z >> (4 * p)) & 0xFu);
-        const uint32_t sao = spread4((n.y >> (4 * p)) & 0xFu), sbo = spread4((n.w >> (4 * p)) & 0xFu);
-        const uint32_t ve = (sae << 1) | (sae & sbe), vo = (sao << 1) | (sao & sbo);  // 0, 2 or 3
+        // a changed cell is empty, sand or water: its byte is its code (A << 1) | B
+        const uint32_t ve = (spread4((n.x >> (4 * p)) & 0xFu) << 1) | spread4((n.z >> (4 * p)) & 0xFu);
+        const uint32_t vo = (spread4((n.y >> (4 * p)) & 0xFu) << 1) | spread4((n.w >> (4 * p)) & 0xFu);
         const uint32_t me = spread4(ce) * 0xFFu, mo = spread4(co) * 0xFFu;
         const uint32_t m0 = __byte_perm(me, mo, 0x5140), m1 = __byte_perm(me, mo, 0x7362);
         w[2 * p] = (w[2 * p] & ~m0) | (__byte_perm(ve, vo, 0x5140) & m0);
@@ -256,14 +260,17 @@ __device__ __forceinline__ uint32_t planes_to_bytes64(uint32_t (&w)[16], const u
     return pairs;
 }
 
+// `rev` walks the row-pairs from the top: consecutive steps alternate, so a
+// step starts on the rows the previous one touched last (still in L2).
 __global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
-                                                    uint32_t sk, int lg) {
+                                                    uint32_t sk, int lg, int rev) {
     const int NC = X >> 6, G = 1 << lg, per = 32 >> lg;
     const int NBZ = nblocks(Z, o), NRP = nblocks(Y, o) * NBZ;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1);
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int n_items = (NRP + per - 1) / per;
-    for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += warps) {
+    for (int it0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it0 < n_items; it0 += warps) {
+        const int it = rev ? n_items - 1 - it0 : it0;
         const int rp = it * per + (lane >> lg);
         const bool valid = rp < NRP;  // every lane takes part in the row-pair step
         const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
@@ -391,7 +398,7 @@ fs3d_status launch_step_bytes(uint8_t* grid, int X, int Y, int Z, uint64_t seed,
             const int per = 32 >> lg;
             const int64_t items = ((int64_t)nblocks(Y, o) * nblocks(Z, o) + per - 1) / per;
             k_step_rows64<<<grid_for(items * 32, 128, rows64_ctas_per_sm()), 128, 0, st>>>(grid, X, Y, Z, o, sk,
-                                                                                          lg);
+                                                                                          lg, (int)(a & 1));
         } else if (rows16_ok(grid, X)) {
             const int64_t units = (int64_t)(X >> 4) * nblocks(Y, o) * nblocks(Z, o);
             k_step_rows16<<<grid_for(units, 256, 8), 256, 0, st>>>(grid, X, Y, Z, o, sk);

@@ -98,6 +98,13 @@ fs3d_config fs3d_default_config(void);
  * legacy default stream).  No device memory is allocated. */
 fs3d_status fs3d_step_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
                              int n_steps, void* stream);
+/* Same contract as fs3d_step_device, through the bit-plane kernels: the grid is
+ * converted into 2-bit planes held in device scratch taken from the
+ * stream-ordered pool (about X*Y*Z/4 bytes, freed on `stream` when done), the
+ * n steps run there (one launch for all of them when the world fits in shared
+ * memory) and the planes are converted back.  Asynchronous on `stream`. */
+fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
+                            int n_steps, void* stream);
 /* Same contract, one thread per 2x2x2 block and byte loads: the plain
  * reference kernel the vectorised one is checked against. */
 fs3d_status fs3d_step_device_simple(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,

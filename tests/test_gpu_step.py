@@ -157,3 +157,19 @@ def test_bounded_sync_and_launch_count(fs3d, orc):
         w.sync(-1)
         w.sync(0)
         assert fs3d.kernel_launches() - before == 300
+
+
+@pytest.mark.parametrize("dims", [(64, 64, 64), (24, 40, 33), (128, 256, 128), (512, 64, 96), (3000, 5, 4)])
+def test_run_device_matches_oracle(fs3d, orc, cuda, dims):
+    X, Y, Z = dims
+    seed = X + Y + Z
+    g = mixed_grid(X, Y, Z, seed)
+    ref = g.copy()
+    orc.run(ref, seed, 9, 33, nthreads=0)
+    d = to_device(cuda, g)
+    st = stream_ptr(cuda)
+    fs3d.run_device(d.data_ptr(), X, Y, Z, seed, 9, 20, st)
+    fs3d.run_device(d.data_ptr(), X, Y, Z, seed, 29, 13, st)
+    cuda.cuda.synchronize()
+    out = d.cpu().numpy()
+    assert (out == ref).all(), describe_diff(out, ref, 32)
