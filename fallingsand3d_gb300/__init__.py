@@ -38,7 +38,8 @@ ERR_IO = -9
 # every entry point of include/fs3d.h (checked by the tests)
 EXPORTS = (
     "fs3d_abi_version", "fs3d_status_string", "fs3d_last_error", "fs3d_kernel_launch_count",
-    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_run_device", "fs3d_hash_device", "fs3d_first_diff_device",
+    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_run_device",
+    "fs3d_run_device_noalloc", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
@@ -110,6 +111,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_step_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_step_device_simple": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_run_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_run_device_noalloc": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_hash_device": (S, [vp, i64, vp, C.POINTER(u64)]),
         "fs3d_first_diff_device": (S, [vp, vp, i64, vp, C.POINTER(i64)]),
         "fs3d_world_create": (S, [vp, i32, i32, i32, u64, u64, i32, C.POINTER(vp)]),

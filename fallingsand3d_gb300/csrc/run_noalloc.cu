@@ -1,0 +1,131 @@
+// fs3d_run_device_noalloc: fs3d_run_device for callers that cannot allocate
+// device memory.
+//
+// Some embedders of the step cannot call cudaMalloc (or any allocating
+// routine) at the point where they advance the world.  Examples: an engine
+// that reserves all of the GPU's memory for its own allocator at start-up, a
+// frame loop on a real-time budget where an allocation may stall or
+// synchronise the device, and a host that gives the library a stream but no
+// allocator of its own.  This entry point runs the same bit-plane
+// computation as fs3d_run_device, but its scratch (the world's planes and the
+// step tables) lives in one file-scope static device array, so a call
+// allocates nothing.  The caller still passes the grid, in device memory.
+//
+// Limits and contract:
+//  * the world's planes must fit kNoAllocPlaneBytes (64 MiB: about 268 M
+//    cells, e.g. 512^3), and rows wider than 2048 cells are refused; larger
+//    worlds are rejected with FS3D_ERR_INVALID_ARG and a message;
+//  * every GPU that loads this library holds the array (64 MiB + 1 MiB) until
+//    the process exits;
+//  * the first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (with that device current) and caches it; make that
+//    first call before any stream capture;
+//  * every call shares the array and it keeps the last call's contents; the
+//    call clears what must start at zero itself.  Calls that overlap on the
+//    GPU (two streams, or two host threads) race on the array: serialise them.
+#include <mutex>
+
+#include "fs3d_common.h"
+#include "planes.h"
+
+namespace fs3d {
+namespace {
+
+constexpr size_t kNoAllocPlaneBytes = (size_t)64 << 20;
+constexpr size_t kNoAllocMaxItems = 1u << 17;  // per-step work items (1 MiB)
+constexpr int kMaxDevices = 64;
+
+// scratch layout: [planes][one-world descriptor][ints][work items]
+constexpr size_t kDescOff = kNoAllocPlaneBytes;
+constexpr size_t kIntsOff = kDescOff + 256;
+constexpr int kOrder = 1 + 2 * kResidentClasses, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
+constexpr size_t kItemsOff = kIntsOff + 256;
+constexpr size_t kScratchBytes = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
+static_assert(kInts * sizeof(int) <= 256, "ints region");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+
+// Writes the one-world tables into the scratch and clears the work counter
+// and the error flag (the array keeps whatever the previous call left).
+__global__ void k_noalloc_tables(PlaneWorld d, int cls, int n_items, int per, unsigned char* base) {
+    PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
+    int* ints = reinterpret_cast<int*>(base + kIntsOff);
+    PlaneItem* items = reinterpret_cast<PlaneItem*>(base + kItemsOff);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        *desc = d;
+        for (int a = 0; a < kInts; ++a) ints[a] = 0;
+        ints[0] = n_items;
+        if (cls >= 0) ints[1 + cls] = 1;
+    }
+    for (int a = tid; a < n_items; a += gridDim.x * blockDim.x) items[a] = PlaneItem{0, a * per};
+}
+
+fs3d_status scratch_base(unsigned char** out) {
+    int dev = 0;
+    FS3D_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: device index");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        FS3D_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return FS3D_OK;
+}
+
+}  // namespace
+}  // namespace fs3d
+
+using namespace fs3d;
+
+extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
+                                               int n_steps, void* stream) {
+    if (!grid_dev || X <= 0 || Y <= 0 || Z <= 0 || n_steps < 0)
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: null grid, bad dims or negative n_steps");
+    if (X > kPlaneMaxX || Y > (1 << 20) || Z > (1 << 20) || plane_bytes(X, Y, Z) > kNoAllocPlaneBytes)
+        return set_error(FS3D_ERR_INVALID_ARG,
+                         "fs3d_run_device_noalloc: world too large for the static scratch (planes of at most "
+                         "64 MiB, about 268 M cells, and rows of at most 2048 cells)");
+    const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
+    const int n_items = cls >= 0 ? 0 : plane_items_for(Y, Z, nw);
+    if ((size_t)n_items > kNoAllocMaxItems)
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: too many row-pairs for the static scratch");
+    if (n_steps == 0) return FS3D_OK;
+    unsigned char* base = nullptr;
+    fs3d_status s = scratch_base(&base);
+    if (s != FS3D_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint4* rows = reinterpret_cast<uint4*>(base);
+    PlaneWorld d{};
+    d.rows = rows;
+    d.seed = seed;
+    d.t = t0;
+    d.X = X;
+    d.Y = Y;
+    d.Z = Z;
+    d.nw = nw;
+    d.steps = n_steps;
+    d.lg = lg;
+    k_noalloc_tables<<<n_items > 0 ? (n_items + 255) / 256 : 1, 256, 0, st>>>(d, cls, n_items, 32 >> lg, base);
+    FS3D_CHECK_LAUNCH("noalloc tables launch");
+    PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
+    int* ints = reinterpret_cast<int*>(base + kIntsOff);
+    PlaneItem* items = reinterpret_cast<PlaneItem*>(base + kItemsOff);
+    s = planes_from_bytes(grid_dev, X, Y, Z, rows, st);
+    if (s == FS3D_OK) {
+        if (cls >= 0) {
+            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, ints + kErr, st);
+        } else {
+            const int grid = plane_step_grid(n_items);
+            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) s = launch_plane_step(desc, items, ints, grid, a, st);
+        }
+    }
+    // static cells never change: their values are read back from the grid itself
+    if (s == FS3D_OK) s = planes_to_bytes(rows, grid_dev, X, Y, Z, grid_dev, st);
+    return s;
+}

@@ -105,6 +105,19 @@ fs3d_status fs3d_step_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t se
  * memory) and the planes are converted back.  Asynchronous on `stream`. */
 fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
                             int n_steps, void* stream);
+/* fs3d_run_device for callers that cannot allocate device memory (an engine
+ * whose own allocator owns all GPU memory, a real-time frame loop that must
+ * not stall on an allocation): same arguments and results, but the scratch
+ * lives in one static device array (64 MiB of planes plus 1 MiB of tables)
+ * that every GPU loading this library holds until exit, so the call allocates
+ * nothing.  Worlds whose planes exceed 64 MiB (about 268 M cells) or whose
+ * rows exceed 2048 cells are rejected with FS3D_ERR_INVALID_ARG.  The first
+ * call on a device looks the array up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised.  No counterpart in the upstream
+ * project (it has no step). */
+fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,
+                                    uint64_t t0, int n_steps, void* stream);
 /* Same contract, one thread per 2x2x2 block and byte loads: the plain
  * reference kernel the vectorised one is checked against. */
 fs3d_status fs3d_step_device_simple(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,
