@@ -238,32 +238,31 @@ __device__ __forceinline__ uint4 bytes_to_planes64(const uint32_t (&w)[16]) {
     return make_uint4(ae, ao, be, bo);
 }
 
-// Writes the new class of every cell whose class changed (only empty, sand
-// and water cells can change: 0, 2, 3).  Returns a mask of changed word pairs.
-__device__ __forceinline__ uint32_t planes_to_bytes64(uint32_t (&w)[16], const uint4& n, const uint4& old) {
-    const uint32_t che = (n.x ^ old.x) | (n.z ^ old.z), cho = (n.y ^ old.y) | (n.w ^ old.w);
-    uint32_t pairs = 0;
-    if (!(che | cho)) return 0u;
+// Merges the new class of every changed cell of one 16-byte piece u (word
+// pairs 2u, 2u+1 of a 64-cell chunk) into its bytes.  Only empty, sand and
+// water cells change, and their byte is their code (A << 1) | B.
+__device__ __forceinline__ uint4 merge_piece(uint4 v, int u, uint32_t che, uint32_t cho, const uint4& n) {
+    uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int p = 0; p < 8; ++p) {
+    for (int h = 0; h < 2; ++h) {
+        const int p = 2 * u + h;
         const uint32_t ce = (che >> (4 * p)) & 0xFu, co = (cho >> (4 * p)) & 0xFu;
-        if (!(ce | co)) continue;
-        pairs |= 1u << p;
-        // a changed cell is empty, sand or water: its byte is its code (A << 1) | B
         const uint32_t ve = (spread4((n.x >> (4 * p)) & 0xFu) << 1) | spread4((n.z >> (4 * p)) & 0xFu);
         const uint32_t vo = (spread4((n.y >> (4 * p)) & 0xFu) << 1) | spread4((n.w >> (4 * p)) & 0xFu);
         const uint32_t me = spread4(ce) * 0xFFu, mo = spread4(co) * 0xFFu;
         const uint32_t m0 = __byte_perm(me, mo, 0x5140), m1 = __byte_perm(me, mo, 0x7362);
-        w[2 * p] = (w[2 * p] & ~m0) | (__byte_perm(ve, vo, 0x5140) & m0);
-        w[2 * p + 1] = (w[2 * p + 1] & ~m1) | (__byte_perm(ve, vo, 0x7362) & m1);
+        w[2 * h] = (w[2 * h] & ~m0) | (__byte_perm(ve, vo, 0x5140) & m0);
+        w[2 * h + 1] = (w[2 * h + 1] & ~m1) | (__byte_perm(ve, vo, 0x7362) & m1);
     }
-    return pairs;
+    return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // `rev` walks the row-pairs from the top: consecutive steps alternate, so a
-// step starts on the rows the previous one touched last (still in L2).
-__global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
-                                                    uint32_t sk, int lg, int rev) {
+// step starts on the rows the previous one touched last (still in L2).  The
+// loaded bytes are not kept across the rule (that would cost 64 registers);
+// the 16-byte pieces with changed cells are read again (L1) when merging.
+__global__ void __launch_bounds__(128, 5) k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
+                                                       uint32_t sk, int lg, int rev) {
     const int NC = X >> 6, G = 1 << lg, per = 32 >> lg;
     const int NBZ = nblocks(Z, o), NRP = nblocks(Y, o) * NBZ;
     const int lane = threadIdx.x & 31, gl = lane & (G - 1);
@@ -277,25 +276,25 @@ __global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid,
         const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
         const int y0 = 2 * j - o, z0 = 2 * k - o;
         const bool has = valid && gl < NC;
-        uint32_t w[4][16];
         uint4 q[4], q0[4];
-        uint8_t* ptr[4];
+        uint4* ptr[4];
         bool in[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
             in[a] = has && y >= 0 && y < Y && z >= 0 && z < Z;
-            ptr[a] = in[a] ? grid + ((int64_t)y * Z + z) * X + 64 * gl : grid;
+            ptr[a] = reinterpret_cast<uint4*>(in[a] ? grid + ((int64_t)y * Z + z) * X + 64 * gl : grid);
             if (in[a]) {
+                uint32_t w[16];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const uint4 v = reinterpret_cast<const uint4*>(ptr[a])[u];
-                    w[a][4 * u] = v.x;
-                    w[a][4 * u + 1] = v.y;
-                    w[a][4 * u + 2] = v.z;
-                    w[a][4 * u + 3] = v.w;
+                    const uint4 v = ptr[a][u];
+                    w[4 * u] = v.x;
+                    w[4 * u + 1] = v.y;
+                    w[4 * u + 2] = v.z;
+                    w[4 * u + 3] = v.w;
                 }
-                q[a] = bytes_to_planes64(w[a]);
+                q[a] = bytes_to_planes64(w);
             } else {
                 q[a] = make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
             }
@@ -305,12 +304,12 @@ __global__ void __launch_bounds__(128) k_step_rows64(uint8_t* __restrict__ grid,
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             if (!in[a]) continue;
-            const uint32_t pairs = planes_to_bytes64(w[a], q[a], q0[a]);
+            const uint32_t che = (q[a].x ^ q0[a].x) | (q[a].z ^ q0[a].z);
+            const uint32_t cho = (q[a].y ^ q0[a].y) | (q[a].w ^ q0[a].w);
+            if (!(che | cho)) continue;
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if ((pairs >> (2 * u)) & 3u)
-                    reinterpret_cast<uint4*>(ptr[a])[u] =
-                        make_uint4(w[a][4 * u], w[a][4 * u + 1], w[a][4 * u + 2], w[a][4 * u + 3]);
+                if (((che | cho) >> (8 * u)) & 0xFFu) ptr[a][u] = merge_piece(ptr[a][u], u, che, cho, q[a]);
         }
     }
 }
