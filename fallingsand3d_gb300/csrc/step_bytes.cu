@@ -261,7 +261,11 @@ __device__ __forceinline__ uint4 merge_piece(uint4 v, int u, uint32_t che, uint3
 // step starts on the rows the previous one touched last (still in L2).  The
 // loaded bytes are not kept across the rule (that would cost 64 registers);
 // the 16-byte pieces with changed cells are read again (L1) when merging.
-__global__ void __launch_bounds__(128, 5) k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
+#ifndef FS3D_ROWS64_CTAS_PER_SM
+#define FS3D_ROWS64_CTAS_PER_SM 5  // register cap: 5 CTAs of 128 threads per SM
+#endif
+__global__ void __launch_bounds__(128, FS3D_ROWS64_CTAS_PER_SM)
+    k_step_rows64(uint8_t* __restrict__ grid, int X, int Y, int Z, int o,
                                                        uint32_t sk, int lg, int rev) {
     const int NC = X >> 6, G = 1 << lg, per = 32 >> lg;
     const int NBZ = nblocks(Z, o), NRP = nblocks(Y, o) * NBZ;
