@@ -68,9 +68,12 @@ int sm_count_public();
 
 // render (render.cu)
 fs3d_status launch_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st);
-fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, const fs3d_camera* cam, int W, int H,
-                                    float* rgba_dev, cudaStream_t st);
+// the DDA kernels take a per-frame brick occupancy bitmap of brickmap_bytes() bytes
+size_t brickmap_bytes(int X, int Y, int Z);
+fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, uint32_t* bm_bits, const fs3d_camera* cam,
+                                    int W, int H, float* rgba_dev, cudaStream_t st);
 fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
-                                     const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st);
+                                     uint32_t* bm_bits, const fs3d_camera* cam, int W, int H, float* rgba_dev,
+                                     cudaStream_t st);
 
 }  // namespace fs3d

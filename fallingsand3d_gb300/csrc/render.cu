@@ -107,12 +107,64 @@ struct PlaneGrid {
     }
 };
 
+// Occupancy of 8x8x8 bricks: bit b set when brick b = bx + BX*(bz + BZ*by)
+// holds a non-empty cell.  Built per frame; the traversal skips the material
+// loads inside empty bricks but keeps every DDA step, so the visited-cell
+// sequence (and the hit) is exactly the flat traversal's.
+struct BrickMap {
+    const uint32_t* bits;
+    int BX, BY, BZ;
+    __device__ __forceinline__ bool occupied(int x, int y, int z) const {
+        const int b = (x >> 3) + BX * ((z >> 3) + BZ * (y >> 3));
+        return (__ldg(bits + (b >> 5)) >> (b & 31)) & 1u;
+    }
+};
+
+__device__ __forceinline__ void mark_brick(uint32_t* bits, int BX, int BZ, int bx, int by, int bz) {
+    const int b = bx + BX * (bz + BZ * by);
+    const uint32_t bit = 1u << (b & 31);
+    if (!(bits[b >> 5] & bit)) atomicOr(bits + (b >> 5), bit);
+}
+
+// planes: a thread per 64-cell word; each 8-cell chunk with a non-empty cell marks its brick
+__global__ void k_brickmap_planes(const uint4* __restrict__ rows, int X, int Y, int Z, int nw, uint32_t* bits,
+                                  int BX, int BZ) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(u % nw);
+        const int64_t r = u / nw;
+        const int y = (int)(r / Z), z = (int)(r % Z);
+        const uint4 q = rows[u];
+        const uint32_t ne = q.x | q.z, no = q.y | q.w;  // even / odd cells that are not empty
+        for (int c = 0; c < 8; ++c) {
+            const int x0 = 64 * g + 8 * c;
+            if (x0 >= X) break;
+            if (((ne >> (4 * c)) | (no >> (4 * c))) & 0xFu) mark_brick(bits, BX, BZ, x0 >> 3, y >> 3, z >> 3);
+        }
+    }
+}
+
+// bytes: a thread per 8-cell chunk of a row
+__global__ void k_brickmap_bytes(const uint8_t* __restrict__ g, int X, int Y, int Z, uint32_t* bits, int BX, int BZ) {
+    const int64_t n = (int64_t)Y * Z * BX;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(u % BX);
+        const int64_t r = u / BX;
+        const int y = (int)(r / Z), z = (int)(r % Z);
+        const uint8_t* row = g + r * X;
+        bool any = false;
+        for (int x = 8 * c; x < 8 * c + 8 && x < X; ++x) any |= row[x] != 0;
+        if (any) mark_brick(bits, BX, BZ, c, y >> 3, z >> 3);
+    }
+}
+
 template <class G>
-__global__ void k_render_dda(G grid, CamDev cam, int W, int H, float4* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_render_dda(G grid, BrickMap bm, CamDev cam, int W, int H,
+                                                   float4* __restrict__ out) {
     const int px = blockIdx.x * blockDim.x + threadIdx.x;
     const int py = blockIdx.y * blockDim.y + threadIdx.y;
     if (px >= W || py >= H) return;
-    const int N[3] = {grid.X, grid.Y, grid.Z};
+    const int NX = grid.X, NY = grid.Y, NZ = grid.Z;
     float ux, uy;
     pixel_uv2(px, py, W, H, ux, uy);
     const float sx = __fmul_rn(__fmul_rn(ux, cam.tan_half_fov), cam.aspect);
@@ -122,10 +174,12 @@ __global__ void k_render_dda(G grid, CamDev cam, int W, int H, float4* __restric
     for (int a = 0; a < 3; ++a) d[a] = __fadd_rn(__fadd_rn(cam.f[a], __fmul_rn(cam.r[a], sx)), __fmul_rn(cam.u[a], sy));
     normalize3(d);
     float4 res = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    // slab entry: per axis in the same order as the CPU restatement
     float inv[3];
     float tmin = 0.0f, tmax = INFINITY;
     int entry_axis = -1;
     bool miss = false;
+    const int N[3] = {NX, NY, NZ};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         if (d[a] == 0.0f) {
@@ -148,51 +202,76 @@ __global__ void k_render_dda(G grid, CamDev cam, int W, int H, float4* __restric
         if (t1 < tmax) tmax = t1;
     }
     if (!miss && tmin <= tmax) {
-        int v[3], step[3];
-        float tmx[3], tdl[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
+        // per-axis state as scalars (no local-memory arrays)
+        int v0, v1, v2, s0, s1, s2;
+        float m0, m1, m2, e0, e1, e2;  // next boundary t, t per cell
+        auto setup = [&](int a, int& v, int& st, float& tm, float& td) {
             const float p = __fadd_rn(cam.o[a], __fmul_rn(d[a], tmin));
             int c = (int)floorf(p);
             c = c < 0 ? 0 : (c > N[a] - 1 ? N[a] - 1 : c);
-            v[a] = c;
-            step[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
+            v = c;
+            st = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
             if (d[a] == 0.0f) {
-                tmx[a] = INFINITY;
-                tdl[a] = INFINITY;
+                tm = INFINITY;
+                td = INFINITY;
             } else {
-                tmx[a] = __fmul_rn(__fsub_rn((float)(c + (step[a] > 0 ? 1 : 0)), cam.o[a]), inv[a]);
-                tdl[a] = fabsf(inv[a]);
+                tm = __fmul_rn(__fsub_rn((float)(c + (st > 0 ? 1 : 0)), cam.o[a]), inv[a]);
+                td = fabsf(inv[a]);
             }
-        }
+        };
+        setup(0, v0, s0, m0, e0);
+        setup(1, v1, s1, m1, e1);
+        setup(2, v2, s2, m2, e2);
         int last = entry_axis;
         float tcur = tmin;
-        const int max_iter = N[0] + N[1] + N[2] + 3;
+        const int max_iter = NX + NY + NZ + 3;
+        int cur_brick = -1;
+        bool cur_occ = true;
         for (int it = 0; it < max_iter; ++it) {
-            const uint32_t m = grid.at(v[0], v[1], v[2]);
-            if (m != 0u) {
-                float n[3] = {0.0f, 0.0f, 0.0f};
-                if (last >= 0) n[last] = step[last] > 0 ? -1.0f : 1.0f;
-                float l[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) l[a] = __fsub_rn(__fadd_rn(cam.o[a], __fmul_rn(d[a], tcur)), cam.light[a]);
-                normalize3(l);
-                const float diff = fmaxf(0.05f, dot3(n, l));
-                const int ci = m < 4u ? (int)m : 4;
-                res = make_float4(__fmul_rn(c_palette[ci][0], diff), __fmul_rn(c_palette[ci][1], diff),
-                                  __fmul_rn(c_palette[ci][2], diff), 1.0f);
-                break;
+            const int b = (v0 >> 3) + bm.BX * ((v2 >> 3) + bm.BZ * (v1 >> 3));
+            if (b != cur_brick) {
+                cur_brick = b;
+                cur_occ = bm.occupied(v0, v1, v2);
             }
-            int a;
-            if (tmx[0] < tmx[1])
-                a = tmx[0] < tmx[2] ? 0 : 2;
-            else
-                a = tmx[1] < tmx[2] ? 1 : 2;
-            tcur = tmx[a];
-            v[a] += step[a];
-            if (v[a] < 0 || v[a] >= N[a]) break;
-            tmx[a] = __fadd_rn(tmx[a], tdl[a]);
-            last = a;
+            if (cur_occ) {
+                const uint32_t m = grid.at(v0, v1, v2);
+                if (m != 0u) {
+                    float n[3] = {0.0f, 0.0f, 0.0f};
+                    if (last == 0) n[0] = s0 > 0 ? -1.0f : 1.0f;
+                    if (last == 1) n[1] = s1 > 0 ? -1.0f : 1.0f;
+                    if (last == 2) n[2] = s2 > 0 ? -1.0f : 1.0f;
+                    float l[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+                        l[a] = __fsub_rn(__fadd_rn(cam.o[a], __fmul_rn(d[a], tcur)), cam.light[a]);
+                    normalize3(l);
+                    const float diff = fmaxf(0.05f, dot3(n, l));
+                    const int ci = m < 4u ? (int)m : 4;
+                    res = make_float4(__fmul_rn(c_palette[ci][0], diff), __fmul_rn(c_palette[ci][1], diff),
+                                      __fmul_rn(c_palette[ci][2], diff), 1.0f);
+                    break;
+                }
+            }
+            // next cell: the axis whose boundary comes first (ties: x, then y, then z)
+            if (m0 < m1 ? m0 < m2 : false) {
+                tcur = m0;
+                v0 += s0;
+                if (v0 < 0 || v0 >= NX) break;
+                m0 = __fadd_rn(m0, e0);
+                last = 0;
+            } else if (!(m0 < m1) && m1 < m2) {
+                tcur = m1;
+                v1 += s1;
+                if (v1 < 0 || v1 >= NY) break;
+                m1 = __fadd_rn(m1, e1);
+                last = 1;
+            } else {
+                tcur = m2;
+                v2 += s2;
+                if (v2 < 0 || v2 >= NZ) break;
+                m2 = __fadd_rn(m2, e2);
+                last = 2;
+            }
         }
     }
     out[(size_t)py * W + px] = res;
@@ -219,22 +298,42 @@ fs3d_status launch_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_
     return FS3D_OK;
 }
 
-fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, const fs3d_camera* cam, int W, int H,
-                                    float* rgba_dev, cudaStream_t st) {
+static int map_grid(int64_t n) {
+    const int64_t need = (n + 255) / 256, cap = (int64_t)sm_count_public() * 8;
+    return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
+// bm_bits: ceil(bricks / 32) words of device scratch the caller provides
+fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, uint32_t* bm_bits, const fs3d_camera* cam,
+                                    int W, int H, float* rgba_dev, cudaStream_t st) {
+    const int BX = (X + 7) / 8, BY = (Y + 7) / 8, BZ = (Z + 7) / 8;
+    FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
+    k_brickmap_bytes<<<map_grid((int64_t)Y * Z * BX), 256, 0, st>>>(g, X, Y, Z, bm_bits, BX, BZ);
+    FS3D_CHECK_LAUNCH("brick map (bytes) launch");
     const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
-    k_render_dda<BytesGrid><<<grd, blk, 0, st>>>(BytesGrid{g, X, Y, Z}, to_dev(cam), W, H,
-                                                 reinterpret_cast<float4*>(rgba_dev));
+    k_render_dda<BytesGrid><<<grd, blk, 0, st>>>(BytesGrid{g, X, Y, Z}, BrickMap{bm_bits, BX, BY, BZ}, to_dev(cam), W,
+                                                 H, reinterpret_cast<float4*>(rgba_dev));
     FS3D_CHECK_LAUNCH("render dda launch");
     return FS3D_OK;
 }
 
 fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
-                                     const fs3d_camera* cam, int W, int H, float* rgba_dev, cudaStream_t st) {
+                                     uint32_t* bm_bits, const fs3d_camera* cam, int W, int H, float* rgba_dev,
+                                     cudaStream_t st) {
+    const int BX = (X + 7) / 8, BY = (Y + 7) / 8, BZ = (Z + 7) / 8;
+    FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
+    k_brickmap_planes<<<map_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, X, Y, Z, nw, bm_bits, BX, BZ);
+    FS3D_CHECK_LAUNCH("brick map (planes) launch");
     const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
-    k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw}, to_dev(cam), W, H,
-                                                 reinterpret_cast<float4*>(rgba_dev));
+    k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(
+        PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw}, BrickMap{bm_bits, BX, BY, BZ},
+        to_dev(cam), W, H, reinterpret_cast<float4*>(rgba_dev));
     FS3D_CHECK_LAUNCH("render dda (planes) launch");
     return FS3D_OK;
+}
+
+size_t brickmap_bytes(int X, int Y, int Z) {
+    return ((((size_t)(X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8) + 31) / 32) * 4;
 }
 
 }  // namespace fs3d

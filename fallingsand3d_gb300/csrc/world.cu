@@ -31,6 +31,7 @@ struct fs3d_world {
     int* aux = nullptr;  // resident tables, see kAux*
     int cls = -1;        // resident class (-1: stepped by the per-step kernel)
     unsigned long long* hash_dev = nullptr;
+    uint32_t* brickmap = nullptr;  // render: per-frame occupancy of 8x8x8 bricks
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
 
@@ -80,6 +81,7 @@ void destroy(fs3d_world* w) {
     cudaFree(w->n_items_dev);
     cudaFree(w->aux);
     cudaFree(w->hash_dev);
+    cudaFree(w->brickmap);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
 }
@@ -340,14 +342,16 @@ fs3d_status fs3d_render(fs3d_world* w, const fs3d_camera* cam, int W, int H, int
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render: bad args");
     float* dst = rgba;
     const size_t bytes = (size_t)W * H * 4 * sizeof(float);
+    if (mode == FS3D_RENDER_DDA && !w->brickmap)
+        FS3D_CUDA(cudaMalloc((void**)&w->brickmap, brickmap_bytes(w->X, w->Y, w->Z)));
     if (!out_on_device) FS3D_CUDA(cudaMallocAsync((void**)&dst, bytes, w->stream));
     fs3d_status s;
     if (mode == FS3D_RENDER_SDF_SPHERE)
         s = launch_render_sdf(cam, W, H, dst, w->stream);
     else if (w->layout == FS3D_LAYOUT_BYTES)
-        s = launch_render_dda_bytes(w->bytes, w->X, w->Y, w->Z, cam, W, H, dst, w->stream);
+        s = launch_render_dda_bytes(w->bytes, w->X, w->Y, w->Z, w->brickmap, cam, W, H, dst, w->stream);
     else
-        s = launch_render_dda_planes(w->rows, w->statics, w->X, w->Y, w->Z, plane_nw(w->X), cam, W, H, dst,
+        s = launch_render_dda_planes(w->rows, w->statics, w->X, w->Y, w->Z, plane_nw(w->X), w->brickmap, cam, W, H, dst,
                                      w->stream);
     if (!out_on_device) {
         cudaError_t e = cudaSuccess;
