@@ -486,9 +486,15 @@ def run_large(fs3d, torch, dev, args, X=1024, Y=1024, Z=1024, W=1920, H=1080):
 def run_only(args):
     """One workload without the side measurements, for ncu captures:
     `batched` runs warmup + steps segments of the 2048-world pool, `plain512`
-    runs warmup + steps x 8 steps of the drop-in byte kernel on 512^3."""
+    runs warmup + steps x 8 steps of the drop-in byte kernel on 512^3, `large`
+    runs the 1024^3 dune world with a 1920x1080 frame after each of
+    --large-steps steps."""
     import torch
     import fallingsand3d_gb300 as fs3d
+    if args.only == "large":
+        out = run_large(fs3d, torch, torch.device("cuda", 0), args)
+        print(json.dumps({"only": args.only, "ok": True, "large_render": out}))
+        return 0
     if args.only == "batched":
         worlds = batch_worlds(fs3d, args.master, args.worlds)
         with fs3d.Batch(150 << 30, steps_per_segment=args.segment) as b:
@@ -524,7 +530,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -217,6 +217,13 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     }
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_create");
     if (s == FS3D_OK) s = b->tn.reserve(1 + 2 * kResidentClasses);
+    // size the tables for a few thousand worlds and capture the segment graph
+    // now, so the first segments of a run (or a server) pay neither a pinned
+    // allocation nor a capture
+    if (s == FS3D_OK) s = b->tw.reserve(4096);
+    if (s == FS3D_OK) s = b->ti.reserve(1 << 16);
+    if (s == FS3D_OK) s = b->to.reserve(4096);
+    if (s == FS3D_OK && b->cfg.use_graphs) s = capture_graph(b);
     if (s != FS3D_OK) {
         fs3d_batch_destroy(b);
         return s;
