@@ -290,8 +290,16 @@ __device__ __forceinline__ int slab_lo(int Y, int r, int CS) { return 2 * ((r * 
 // shared memory), and each CTA writes its slab back with one TMA bulk store.
 // Worlds are independent, so groups never wait on one another.
 // meta: [0] per-step items, [1 + c] resident worlds of class c, [1 + kResidentClasses + c] their offset in order[].
+// CTAs of each single-CTA class that share an SM (the register cap that lets
+// them: 24 warps of at most 80 registers per SM)
+template <int NT>
+constexpr int resident_ctas_per_sm() {
+    return NT == 128 ? 6 : (NT == 256 ? 3 : 1);
+}
+
 template <int NT, bool CL>
-__global__ void __launch_bounds__(NT) k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
+__global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
+    k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
                                                              const int* __restrict__ order,
                                                              const int* __restrict__ meta, int cls, int CS,
                                                              int* counter, int* err) {
@@ -403,9 +411,12 @@ void init_classes() {
     cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     const int kStatic = 256;  // the kernel's own shared variables, rounded up
     const ResidentCfg base[kResidentClasses] = {
-        {128, 4, 1, 0, resident_fn<128, false>()}, {256, 2, 1, 0, resident_fn<256, false>()},
-        {512, 1, 1, 0, resident_fn<512, false>()}, {512, 1, 2, 0, resident_fn<512, true>()},
-        {512, 1, 4, 0, resident_fn<512, true>()},  {512, 1, 8, 0, resident_fn<512, true>()}};
+        {128, resident_ctas_per_sm<128>(), 1, 0, resident_fn<128, false>()},
+        {256, resident_ctas_per_sm<256>(), 1, 0, resident_fn<256, false>()},
+        {768, resident_ctas_per_sm<768>(), 1, 0, resident_fn<768, false>()},
+        {512, 1, 2, 0, resident_fn<512, true>()},
+        {512, 1, 4, 0, resident_fn<512, true>()},
+        {512, 1, 8, 0, resident_fn<512, true>()}};
     for (int c = 0; c < kResidentClasses; ++c) {
         ResidentCfg k = base[c];
         int smem = per_sm / k.ctas_per_sm - reserved - kStatic;
@@ -474,7 +485,7 @@ fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, con
     else if (k.threads == 256)
         e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<256, false>, worlds, order, meta, cls, CS, counter, err);
     else
-        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<512, false>, worlds, order, meta, cls, CS, counter, err);
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<768, false>, worlds, order, meta, cls, CS, counter, err);
     if (e != cudaSuccess) return cuda_fail(e, "resident segment launch");
     note_launch();
     return FS3D_OK;

@@ -32,8 +32,8 @@ constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 
 // Resident segment classes: worlds whose planes fit in shared memory take
 // all their segment steps in one launch.  Classes 0..2 hold a world in one CTA
-// of 128 / 256 / 512 threads (4 / 2 / 1 CTAs per SM); classes 3..5 split a
-// world into y-slabs over a cluster of 2 / 4 / 8 CTAs.
+// of 128 / 256 / 768 threads (6 / 3 / 1 CTAs per SM); classes 3..5 split a
+// world into y-slabs over a cluster of 2 / 4 / 8 CTAs of 512 threads.
 constexpr int kResidentClasses = 6;
 // smallest class that holds a world of these dims, -1 if none does
 int resident_class(int X, int Y, int Z);

@@ -135,12 +135,19 @@ __global__ void k_brickmap_planes(const uint4* __restrict__ rows, int X, int Y, 
         const int64_t r = u / nw;
         const int y = (int)(r / Z), z = (int)(r % Z);
         const uint4 q = rows[u];
-        const uint32_t ne = q.x | q.z, no = q.y | q.w;  // even / odd cells that are not empty
-        for (int c = 0; c < 8; ++c) {
-            const int x0 = 64 * g + 8 * c;
-            if (x0 >= X) break;
-            if (((ne >> (4 * c)) | (no >> (4 * c))) & 0xFu) mark_brick(bits, BX, BZ, x0 >> 3, y >> 3, z >> 3);
-        }
+        const uint32_t nz = q.x | q.y | q.z | q.w;  // bit m: cell 64g+2m or 64g+2m+1 is not empty
+        if (!nz) continue;
+        // the word's 8 chunks are 8 consecutive bricks along x: one atomic per
+        // 32-bit bitmap word they fall in (at most two)
+        uint32_t m8 = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+            if (((nz >> (4 * c)) & 0xFu) && 64 * g + 8 * c < X) m8 |= 1u << c;
+        if (!m8) continue;
+        const int b0 = 8 * g + BX * ((z >> 3) + BZ * (y >> 3));
+        const int sh = b0 & 31;
+        atomicOr(bits + (b0 >> 5), m8 << sh);
+        if (sh > 24 && (m8 >> (32 - sh))) atomicOr(bits + (b0 >> 5) + 1, m8 >> (32 - sh));
     }
 }
 
