@@ -384,6 +384,11 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         for (int x : v) b->to.h[si++] = x;
     }
     // admissions complete before the segment reads their planes
+    for (cudaEvent_t ev : b->pending_ready) {
+        FS3D_CUDA(cudaStreamWaitEvent(b->stream, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    b->pending_ready.clear();
     for (auto& kv : b->worlds)
         if (kv.second.ready) {
             FS3D_CUDA(cudaStreamWaitEvent(b->stream, kv.second.ready, 0));
@@ -500,25 +505,183 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     if (!b || n < 0 || (n > 0 && (!specs || !tickets)) || !n_admitted)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: bad args");
     *n_admitted = 0;
-    fs3d_status s = FS3D_OK;
-    for (int a = 0; a < n && s == FS3D_OK; ++a) {
-        const fs3d_world_spec& p = specs[a];
-        if (!p.grid) {
-            s = set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: NULL grid");
-            break;
-        }
-        s = admit(b, p.grid, p.X, p.Y, p.Z, p.seed, p.start_step, p.n_steps, &tickets[a], false);
-        if (s == FS3D_OK) ++*n_admitted;
+    // admit in order while the budget allows (static byte copies, found on the
+    // device below, are charged on top)
+    int k = 0;
+    size_t used = b->used;
+    for (; k < n; ++k) {
+        const fs3d_world_spec& p = specs[k];
+        if (!p.grid || p.X <= 0 || p.Y <= 0 || p.Z <= 0 || p.X > kPlaneMaxX || p.Y > 65536 || p.Z > 65536 ||
+            p.n_steps < 0)
+            return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: bad world spec");
+        const size_t need = plane_bytes(p.X, p.Y, p.Z) + sizeof(PlaneWorld);
+        if (used + need > b->budget) break;
+        used += need;
     }
-    // the callers' grids may be reused once every copy has been consumed
-    FS3D_CUDA(cudaStreamSynchronize(b->side));
-    return s == FS3D_ERR_BUDGET && *n_admitted > 0 ? FS3D_ERR_BUDGET : s;
+    if (k == 0) return n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: nothing fits in the budget now") : FS3D_OK;
+    // one staging buffer, one copy per world, one conversion launch for all
+    std::vector<ConvJob> jobs((size_t)k);
+    std::vector<int64_t> unit_off((size_t)k);
+    std::vector<uint4*> rows((size_t)k, nullptr);
+    int64_t bytes_total = 0, units = 0;
+    for (int a = 0; a < k; ++a) {
+        const fs3d_world_spec& p = specs[a];
+        ConvJob& j = jobs[(size_t)a];
+        j.statics = nullptr;
+        j.byte_off = bytes_total;
+        j.X = p.X;
+        j.Y = p.Y;
+        j.Z = p.Z;
+        j.nw = plane_nw(p.X);
+        unit_off[(size_t)a] = units;
+        bytes_total += ((int64_t)p.X * p.Y * p.Z + 15) / 16 * 16;
+        units += (int64_t)p.Y * p.Z * j.nw;
+    }
+    uint8_t* staging = nullptr;
+    void* table = nullptr;
+    const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k, off_bytes = sizeof(int64_t) * (size_t)k;
+    const size_t flags_off = (jobs_bytes + off_bytes + 15) / 16 * 16;
+    fs3d_status s = FS3D_OK;
+    cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
+    if (e == cudaSuccess) e = cudaMallocAsync(&table, flags_off + sizeof(int) * (size_t)k, b->side);
+    for (int a = 0; a < k && e == cudaSuccess; ++a) {
+        const fs3d_world_spec& p = specs[a];
+        e = cudaMallocAsync((void**)&rows[(size_t)a], plane_bytes(p.X, p.Y, p.Z), b->side);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, p.grid, (size_t)p.X * p.Y * p.Z,
+                                cudaMemcpyHostToDevice, b->side);
+        jobs[(size_t)a].rows = rows[(size_t)a];
+    }
+    ConvJob* jobs_dev = static_cast<ConvJob*>(table);
+    int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
+    int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(table) + flags_off);
+    // pageable sources: staged before the calls return
+    if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(off_dev, unit_off.data(), off_bytes, cudaMemcpyHostToDevice, b->side);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags_dev, 0, sizeof(int) * (size_t)k, b->side);
+    if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many upload");
+    if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, k, units, staging, flags_dev, b->side);
+    std::vector<int> flags((size_t)k, 0);
+    if (s == FS3D_OK) {
+        e = cudaMemcpyAsync(flags.data(), flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
+        // the callers' grids may be reused once this returns
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
+        if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many conversion");
+    }
+    // worlds holding a material >= 4 keep a byte copy for read-back
+    std::vector<uint8_t*> statics((size_t)k, nullptr);
+    for (int a = 0; a < k && s == FS3D_OK; ++a) {
+        if (!flags[(size_t)a]) continue;
+        const size_t cells = (size_t)specs[a].X * specs[a].Y * specs[a].Z;
+        e = cudaMallocAsync((void**)&statics[(size_t)a], cells, b->side);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(statics[(size_t)a], staging + jobs[(size_t)a].byte_off, cells, cudaMemcpyDeviceToDevice,
+                                b->side);
+        if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many static copy");
+    }
+    if (staging) cudaFreeAsync(staging, b->side);
+    if (table) cudaFreeAsync(table, b->side);
+    if (s != FS3D_OK) {
+        for (int a = 0; a < k; ++a) {
+            if (rows[(size_t)a]) cudaFreeAsync(rows[(size_t)a], b->side);
+            if (statics[(size_t)a]) cudaFreeAsync(statics[(size_t)a], b->side);
+        }
+        return s;
+    }
+    cudaEvent_t ready = nullptr;
+    if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) == cudaSuccess) cudaEventRecord(ready, b->side);
+    for (int a = 0; a < k; ++a) {
+        const fs3d_world_spec& p = specs[a];
+        BWorld w;
+        w.X = p.X;
+        w.Y = p.Y;
+        w.Z = p.Z;
+        w.nw = plane_nw(p.X);
+        w.seed = p.seed;
+        w.t = p.start_step;
+        w.remaining = p.n_steps;
+        w.done = p.n_steps == 0;
+        w.rows = rows[(size_t)a];
+        w.statics = statics[(size_t)a];
+        w.bytes = plane_bytes(p.X, p.Y, p.Z) + sizeof(PlaneWorld) +
+                  (w.statics ? (size_t)p.X * p.Y * p.Z : 0);
+        b->used += w.bytes;
+        tickets[a] = b->next_ticket++;
+        b->worlds.emplace(tickets[a], w);
+    }
+    // the next segment runs after the static copies (side stream) are done
+    if (ready) {
+        b->pending_ready.push_back(ready);
+    }
+    *n_admitted = k;
+    return k < n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: the remaining worlds do not fit now") : FS3D_OK;
 }
 
 fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
     if (!b || n < 0 || (n > 0 && !tickets)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: bad args");
+    std::vector<std::map<uint64_t, BWorld>::iterator> its;
+    its.reserve((size_t)n);
+    for (int a = 0; a < n; ++a) {
+        auto it = b->worlds.find(tickets[a]);
+        if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire_many: unknown ticket");
+        its.push_back(it);
+    }
+    // every world's planes are final after the last segment enqueued so far
+    FS3D_CUDA(cudaStreamWaitEvent(b->side, b->last_segment, 0));
+    for (cudaEvent_t ev : b->pending_ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, ev, 0));
     fs3d_status s = FS3D_OK;
-    for (int a = 0; a < n && s == FS3D_OK; ++a) s = retire(b, tickets[a], grids_out ? grids_out[a] : nullptr, false);
+    if (grids_out) {
+        std::vector<ConvJob> jobs;
+        std::vector<int64_t> unit_off;
+        std::vector<int> who;
+        int64_t bytes_total = 0, units = 0;
+        for (int a = 0; a < n; ++a) {
+            if (!grids_out[a]) continue;
+            const BWorld& w = its[(size_t)a]->second;
+            ConvJob j;
+            j.rows = w.rows;
+            j.statics = w.statics;
+            j.byte_off = bytes_total;
+            j.X = w.X;
+            j.Y = w.Y;
+            j.Z = w.Z;
+            j.nw = w.nw;
+            jobs.push_back(j);
+            unit_off.push_back(units);
+            who.push_back(a);
+            bytes_total += ((int64_t)w.X * w.Y * w.Z + 15) / 16 * 16;
+            units += (int64_t)w.Y * w.Z * w.nw;
+        }
+        const int k = (int)jobs.size();
+        if (k) {
+            uint8_t* staging = nullptr;
+            void* table = nullptr;
+            const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k;
+            cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
+            if (e == cudaSuccess) e = cudaMallocAsync(&table, jobs_bytes + sizeof(int64_t) * (size_t)k, b->side);
+            ConvJob* jobs_dev = static_cast<ConvJob*>(table);
+            int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(off_dev, unit_off.data(), sizeof(int64_t) * (size_t)k, cudaMemcpyHostToDevice,
+                                    b->side);
+            if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
+            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, b->side);
+            for (int q = 0; q < k && s == FS3D_OK; ++q) {
+                const BWorld& w = its[(size_t)who[(size_t)q]]->second;
+                e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off,
+                                    (size_t)w.X * w.Y * w.Z, cudaMemcpyDeviceToHost, b->side);
+                if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+            }
+            if (staging) cudaFreeAsync(staging, b->side);
+            if (table) cudaFreeAsync(table, b->side);
+        }
+    }
+    for (auto it : its) {
+        b->used -= it->second.bytes;
+        free_world(b, it->second);
+        b->worlds.erase(it);
+    }
     FS3D_CUDA(cudaStreamSynchronize(b->side));
     return s;
 }
@@ -552,6 +715,8 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     if (b->side) cudaStreamSynchronize(b->side);
     for (auto& kv : b->worlds) free_world(b, kv.second);
     b->worlds.clear();
+    for (cudaEvent_t ev : b->pending_ready) cudaEventDestroy(ev);
+    b->pending_ready.clear();
     if (b->side) cudaStreamSynchronize(b->side);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->tw.release();

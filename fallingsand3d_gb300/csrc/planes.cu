@@ -97,6 +97,65 @@ __global__ void k_hash_planes(const uint4* __restrict__ rows, const uint8_t* __r
     if ((threadIdx.x & 31) == 0 && h) atomicAdd(out, (unsigned long long)h);
 }
 
+// Many worlds per launch (admission and retirement of a batch): job j covers
+// units [unit_off[j], unit_off[j+1]) of (row, word) pairs; its bytes sit at
+// byte_off in one staging buffer.
+__device__ __forceinline__ int find_job(const int64_t* __restrict__ unit_off, int njobs, int64_t u) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(unit_off + mid) <= u)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
+                                        int njobs, int64_t total, const uint8_t* __restrict__ staging, int* flags) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int j = find_job(unit_off, njobs, u);
+        const ConvJob jb = jobs[j];
+        const int64_t lu = u - unit_off[j];
+        const int w = (int)(lu % jb.nw);
+        const int64_t r = lu / jb.nw;
+        const uint8_t* row = staging + jb.byte_off + r * jb.X;
+        uint32_t ae = 0, ao = 0, be = 0, bo = 0, big = 0;
+        for (int m = 0; m < 32; ++m) {
+            const int xe = 64 * w + 2 * m, xo = xe + 1;
+            const uint32_t ve = xe < jb.X ? row[xe] : 1u, vo = xo < jb.X ? row[xo] : 1u;
+            big |= (ve | vo) & 0xFCu;
+            uint32_t a, b;
+            classify(ve, a, b);
+            ae |= a << m;
+            be |= b << m;
+            classify(vo, a, b);
+            ao |= a << m;
+            bo |= b << m;
+        }
+        jb.rows[lu] = make_uint4(ae, ao, be, bo);
+        if (big) atomicOr(flags + j, 1);  // holds a static material >= 4: keep its bytes
+    }
+}
+
+__global__ void k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
+                                        int njobs, int64_t total, uint8_t* __restrict__ staging) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int j = find_job(unit_off, njobs, u);
+        const ConvJob jb = jobs[j];
+        const int64_t lu = u - unit_off[j];
+        const int w = (int)(lu % jb.nw);
+        const int64_t r = lu / jb.nw;
+        const uint4 q = jb.rows[lu];
+        uint8_t* dst = staging + jb.byte_off;
+        for (int x = 64 * w; x < 64 * w + 64 && x < jb.X; ++x) {
+            const int64_t idx = r * jb.X + x;
+            dst[idx] = (uint8_t)cell_value(q, (x >> 1) & 31, x & 1, jb.statics, idx);
+        }
+    }
+}
+
 // The mixed-size batch world generated straight into planes: stone at y < 2,
 // empty below Y/2, and above it one PCG32 draw per cell in index order; each
 // thread jumps its generator to the first draw of its 64-cell word.
@@ -514,6 +573,23 @@ fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows
     const int nw = plane_nw(X);
     k_bytes_to_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(g, X, Y, Z, nw, rows);
     FS3D_CHECK_LAUNCH("bytes->planes launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
+                                    const uint8_t* staging, int* flags, cudaStream_t st) {
+    if (njobs <= 0 || total_units <= 0) return FS3D_OK;
+    k_bytes_to_planes_multi<<<conv_grid(total_units), 256, 0, st>>>(jobs, unit_off, njobs, total_units, staging,
+                                                                     flags);
+    FS3D_CHECK_LAUNCH("bytes->planes (many worlds) launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
+                                  uint8_t* staging, cudaStream_t st) {
+    if (njobs <= 0 || total_units <= 0) return FS3D_OK;
+    k_planes_to_bytes_multi<<<conv_grid(total_units), 256, 0, st>>>(jobs, unit_off, njobs, total_units, staging);
+    FS3D_CHECK_LAUNCH("planes->bytes (many worlds) launch");
     return FS3D_OK;
 }
 

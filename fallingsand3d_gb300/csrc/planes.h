@@ -45,6 +45,21 @@ int smem_world_limit();
 fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
                                           int* counter, int* err, cudaStream_t st);
 
+// One world of a many-world conversion: its planes, its static bytes
+// (nullable) and the offset of its canonical bytes in a shared staging buffer.
+struct ConvJob {
+    uint4* rows;
+    const uint8_t* statics;
+    int64_t byte_off;
+    int32_t X, Y, Z, nw;
+};
+// bytes -> planes for njobs worlds in one launch; unit_off[j] = sum of Y*Z*nw
+// over jobs before j; flags[j] |= 1 when world j holds a material >= 4
+fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
+                                    const uint8_t* staging, int* flags, cudaStream_t st);
+fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
+                                  uint8_t* staging, cudaStream_t st);
+
 int plane_lg(int nw);
 int plane_items_for(int Y, int Z, int nw);
 int plane_step_grid(int64_t n_items);
