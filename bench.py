@@ -235,9 +235,11 @@ def run_fs3d(args):
     # ---- headline: batched pool, device-resident
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
-    total_steps = S * (args.warmup + args.steps + 1)
+    total_steps = S * (args.warmup + args.steps + 1 + 32)
     tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
     bstream = torch.cuda.ExternalStream(b.stream())
+    # launch configuration chosen on real segments of this pool (outside the clock)
+    tune = b.autotune(trial_segments=1) if not args.no_autotune else {"segments": 0}
     for _ in range(args.warmup):
         b.run_segment()
     b.sync()
@@ -275,7 +277,7 @@ def run_fs3d(args):
         for i in range(3):
             (X, Y, Z), seed = worlds[i]
             g = host[i].numpy().copy()
-            orc.run(g, seed, 0, S * (args.warmup + args.steps), nthreads=0)
+            orc.run(g, seed, 0, S * (tune["segments"] + args.warmup + args.steps), nthreads=0)
             got = b.retire(tickets[i], (Y, Z, X))
             ok &= bool((got == g).all())
         parity = "3 worlds bit-exact after the timed segments" if ok else "MISMATCH"
@@ -294,6 +296,8 @@ def run_fs3d(args):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             ts = eb.admit_many(host, seeds, S, ptrs=in_ptrs)
+            if it == 0 and not args.no_autotune:
+                eb.autotune(trial_segments=1)  # same make-up: applies the choice made above
             eb.run_segment()
             eb.retire_many(ts, out_ptrs)
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
@@ -422,11 +426,12 @@ def run_fs3d(args):
                                        f"{S}-step CUDA-graph segments (one step = one segment)",
                            "worlds_per_gpu": args.worlds, "cells_per_gpu": cells, "steps_per_segment": S,
                            "master_seed": args.master, "l2": "flushed between timed segments (512 MB write)",
-                           "layout": "2-bit planes", "parallelism": f"replicas x{world}"},
+                           "layout": "2-bit planes", "parallelism": f"replicas x{world}",
+                           "launch_config": {k: tune.get(k) for k in ("promote", "ctas_per_sm", "trials")}},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(float(np.mean(e2e_ms)), 2),
-                        "path": "fs3d_batch_admit (pinned) + fs3d_batch_run_segment + fs3d_batch_retire"},
+                        "path": "fs3d_batch_admit_many (pinned) + fs3d_batch_run_segment + fs3d_batch_retire_many"},
                 "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
                                     "launches_per_segment": S * len(worlds),
                                     "speedup_batched_vs_plain": round(value / world / plain_val, 2)},
@@ -518,6 +523,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
     ap.add_argument("--worlds", type=int, default=2048)
     ap.add_argument("--master", type=int, default=1)

@@ -45,8 +45,9 @@ EXPORTS = (
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
     "fs3d_batch_retire_many",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
-    "fs3d_batch_stats", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
-    "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_gen_parity", "fs3d_gen_pillars",
+    "fs3d_batch_stats", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
+    "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
+    "fs3d_render_object", "fs3d_gen_parity", "fs3d_gen_pillars",
     "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
 )
 
@@ -86,6 +87,17 @@ class ServeStats(C.Structure):
 class WorldSpec(C.Structure):
     _fields_ = [("grid", C.c_void_p), ("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int), ("pad", C.c_int),
                 ("seed", C.c_uint64), ("start_step", C.c_uint64), ("n_steps", C.c_int64)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("promote", C.c_int), ("ctas_per_sm", C.c_int), ("trials", C.c_int), ("cached", C.c_int),
+                ("segments", C.c_int), ("best_vox_per_ms", C.c_double), ("trial_vox_per_ms", C.c_double * 8)]
+
+
+class ObjectView(C.Structure):
+    _fields_ = [("cam_pos", C.c_float * 3), ("cam_rot_y_deg", C.c_float), ("fovy_deg", C.c_float),
+                ("aspect", C.c_float), ("znear", C.c_float), ("zfar", C.c_float), ("model", C.c_float * 16),
+                ("clear", C.c_float * 4)]
 
 
 class Config(C.Structure):
@@ -136,6 +148,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
         "fs3d_batch_retire": (S, [vp, u64, vp]),
+        "fs3d_batch_autotune": (S, [vp, i32, C.POINTER(TuneReport)]),
         "fs3d_batch_stats": (S, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_size_t),
                                  C.POINTER(C.c_size_t)]),
         "fs3d_batch_stream": (S, [vp, C.POINTER(vp)]),
@@ -146,6 +159,9 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_render_sdf": (S, [C.POINTER(Camera), i32, i32, vp, vp]),
         "fs3d_camera_fs_raymarch": (None, [C.POINTER(Camera)]),
         "fs3d_camera_world_view": (None, [C.POINTER(Camera), i32, i32, i32, i32, i32]),
+        "fs3d_object_view_scene": (None, [C.POINTER(ObjectView)]),
+        "fs3d_mesh_cube": (C.c_int, [vp]),
+        "fs3d_render_object": (S, [C.POINTER(ObjectView), vp, i32, i32, i32, vp, vp]),
         "fs3d_gen_parity": (S, [u64, i32, i32, i32, vp]),
         "fs3d_gen_pillars": (S, [u64, i32, i32, i32, vp]),
         "fs3d_gen_batch_dims": (S, [u64, i32, vp, vp]),
@@ -228,6 +244,34 @@ def camera_world_view(X: int, Y: int, Z: int, W: int, H: int) -> Camera:
     c = Camera()
     lib().fs3d_camera_world_view(C.byref(c), X, Y, Z, W, H)
     return c
+
+
+def object_view_scene(cam_pos=None, rot_y: Optional[float] = None, model=None) -> ObjectView:
+    """The upstream scene's view of its one object, optionally moved: camPos,
+    camRot.y in degrees, a 4x4 model matrix (row-major numpy, stored
+    column-major)."""
+    v = ObjectView()
+    lib().fs3d_object_view_scene(C.byref(v))
+    if cam_pos is not None:
+        v.cam_pos[:] = [float(x) for x in cam_pos]
+    if rot_y is not None:
+        v.cam_rot_y_deg = float(rot_y)
+    if model is not None:
+        v.model[:] = [float(x) for x in np.asarray(model, np.float32).T.reshape(-1)]
+    return v
+
+
+def mesh_cube() -> np.ndarray:
+    """The scene's +-1 cube as (12, 3, 3) float32 triangles."""
+    tri = np.empty((12, 3, 3), np.float32)
+    lib().fs3d_mesh_cube(_ptr(tri))
+    return tri
+
+
+def render_object_device(view: ObjectView, tri: np.ndarray, W: int, H: int, rgba_ptr: int, stream: int = 0) -> None:
+    """The raymarch_sphere material over a triangle mesh into W*H RGBA float32 at rgba_ptr."""
+    tri = np.ascontiguousarray(tri, np.float32).reshape(-1, 9)
+    check(lib().fs3d_render_object(C.byref(view), _ptr(tri), tri.shape[0], W, H, rgba_ptr, stream))
 
 
 # ---------------------------------------------------------------- device entry points
@@ -456,6 +500,13 @@ class Batch:
         g = np.empty(shape, np.uint8)
         check(lib().fs3d_batch_retire(self.handle, ticket, _ptr(g)))
         return g
+
+    def autotune(self, trial_segments: int = 2) -> dict:
+        """Times the launch configurations on real segments and keeps the best."""
+        r = TuneReport()
+        check(lib().fs3d_batch_autotune(self.handle, trial_segments, C.byref(r)))
+        return {"promote": r.promote, "ctas_per_sm": r.ctas_per_sm, "trials": r.trials, "cached": bool(r.cached),
+                "segments": r.segments, "best_vox_per_ms": r.best_vox_per_ms, "trial_vox_per_ms": list(r.trial_vox_per_ms)[:r.trials]}
 
     def stats(self):
         w, c = i64(), i64()

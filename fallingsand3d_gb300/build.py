@@ -1,6 +1,6 @@
 """Builds libfs3d.so (the CUDA step/render library) in-tree with nvcc for sm_103a.
 
-Each translation unit compiles in parallel; the render unit gets --fmad=false
+Each translation unit compiles in parallel; the render units get --fmad=false
 so its float arithmetic is one IEEE operation per source operation.  Host code
 is built with -ffp-contract=off for the same reason (the dune generator uses
 doubles).  Usage: ``python -m fallingsand3d_gb300.build`` or ``build()``.
@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libfs3d.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall",
           "-Xptxas", "-warn-spills"]
-PER_FILE = {"render.cu": ["--fmad=false"]}
+PER_FILE = {"render.cu": ["--fmad=false"], "render_object.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:

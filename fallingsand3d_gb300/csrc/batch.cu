@@ -16,6 +16,7 @@
 
 #include <chrono>
 #include <map>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -95,6 +96,7 @@ struct fs3d_batch {
     void* graph_items = nullptr;
     void* graph_order = nullptr;
     int grid = 0;
+    int promote = 0;  // single-CTA resident worlds run this many classes wider (autotuned)
     unsigned long long* hash_dev = nullptr;
     uint64_t segments = 0;
 };
@@ -330,7 +332,8 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
-        const int c = b->cfg.use_smem ? resident_class(w.X, w.Y, w.Z) : -1;
+        int c = b->cfg.use_smem ? resident_class(w.X, w.Y, w.Z) : -1;
+        if (c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
         run.emplace_back(c, &w);
         if (c >= 0)
             ++ns;
@@ -689,6 +692,122 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
 fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire: NULL batch");
     return retire(b, ticket, grid_out, true);
+}
+
+}  // extern "C"
+
+namespace {
+
+// tuned choices per batch shape: the count of live worlds per resident class
+// (and of worlds too large to be resident), so a batch of the same make-up
+// starts from the measured best
+std::map<std::vector<int>, std::pair<int, int>> g_tuned;
+std::mutex g_tuned_mu;
+
+std::vector<int> batch_shape(const fs3d_batch* b) {
+    std::vector<int> h(kResidentClasses + 1, 0);
+    for (auto& kv : b->worlds) {
+        if (kv.second.done) continue;
+        const int c = resident_class(kv.second.X, kv.second.Y, kv.second.Z);
+        ++h[(size_t)(c < 0 ? kResidentClasses : c)];
+    }
+    return h;
+}
+
+// applies a launch configuration; the segment graph (which bakes in the
+// per-step kernel's grid) is re-captured once the stream is idle
+fs3d_status apply_tuning(fs3d_batch* b, int promote, int ctas_per_sm) {
+    FS3D_CUDA(cudaStreamSynchronize(b->stream));
+    b->promote = promote;
+    b->grid = sm_count_public() * ctas_per_sm;
+    return b->cfg.use_graphs ? capture_graph(b) : FS3D_OK;
+}
+
+// voxel-updates the next segment will perform
+double segment_work(const fs3d_batch* b) {
+    double v = 0.0;
+    const int S = b->cfg.steps_per_segment;
+    for (auto& kv : b->worlds) {
+        const BWorld& w = kv.second;
+        if (w.done) continue;
+        v += (double)w.X * w.Y * w.Z * (double)(w.remaining < S ? w.remaining : S);
+    }
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_report* out) {
+    if (!b || trial_segments <= 0) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_autotune: bad args");
+    if (out) memset(out, 0, sizeof(*out));
+    const std::vector<int> shape = batch_shape(b);
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mu);
+        auto it = g_tuned.find(shape);
+        if (it != g_tuned.end()) {
+            const fs3d_status s = apply_tuning(b, it->second.first, it->second.second);
+            if (s != FS3D_OK) return s;
+            if (out) {
+                out->promote = b->promote;
+                out->ctas_per_sm = it->second.second;
+                out->cached = 1;
+            }
+            return FS3D_OK;
+        }
+    }
+    const int resident = plane_step_ctas_per_sm();
+    std::vector<std::pair<int, int>> cand;
+    for (int p = 0; p < kSingleCtaClasses; ++p)
+        for (int cps : {resident, resident > 1 ? resident / 2 : resident})
+            if (std::find(cand.begin(), cand.end(), std::make_pair(p, cps)) == cand.end()) cand.emplace_back(p, cps);
+    cudaEvent_t e0, e1;
+    FS3D_CUDA(cudaEventCreate(&e0));
+    FS3D_CUDA(cudaEventCreate(&e1));
+    double best_rate = -1.0;
+    std::pair<int, int> best = {b->promote, b->grid / sm_count_public()};
+    fs3d_status s = FS3D_OK;
+    int trials = 0, segments = 0;
+    for (size_t ci = 0; ci < cand.size() && s == FS3D_OK; ++ci) {
+        s = apply_tuning(b, cand[ci].first, cand[ci].second);
+        double rate = 0.0;
+        for (int r = 0; r < trial_segments + 1 && s == FS3D_OK; ++r) {
+            const double work = segment_work(b);
+            if (work <= 0.0) break;
+            cudaEventRecord(e0, b->stream);
+            s = fs3d_batch_run_segment(b);
+            ++segments;
+            cudaEventRecord(e1, b->stream);
+            if (s == FS3D_OK) s = cudaEventSynchronize(e1) == cudaSuccess ? FS3D_OK : cuda_fail(cudaGetLastError(), "autotune");
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0 && ms > 0.0f) rate = std::max(rate, work / ms);  // the first is a warm-up
+        }
+        if (out && trials < 8) out->trial_vox_per_ms[trials] = rate;
+        ++trials;
+        if (rate > best_rate) {
+            best_rate = rate;
+            best = cand[ci];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const fs3d_status sa = apply_tuning(b, best.first, best.second);
+    if (s != FS3D_OK) return s;
+    if (sa != FS3D_OK) return sa;
+    if (best_rate > 0.0) {
+        std::lock_guard<std::mutex> lock(g_tuned_mu);
+        g_tuned[shape] = best;
+    }
+    if (out) {
+        out->promote = best.first;
+        out->ctas_per_sm = best.second;
+        out->trials = trials;
+        out->segments = segments;
+        out->best_vox_per_ms = best_rate;
+    }
+    return FS3D_OK;
 }
 
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells, size_t* bytes_used,

@@ -35,6 +35,7 @@ constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 // of 128 / 256 / 768 threads (6 / 3 / 1 CTAs per SM); classes 3..5 split a
 // world into y-slabs over a cluster of 2 / 4 / 8 CTAs of 512 threads.
 constexpr int kResidentClasses = 6;
+constexpr int kSingleCtaClasses = 3;  // classes 0..2 hold a world in one CTA
 // smallest class that holds a world of these dims, -1 if none does
 int resident_class(int X, int Y, int Z);
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable

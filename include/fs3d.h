@@ -185,6 +185,21 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
 fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out);
 /* retire n worlds with one host wait; grids_out (nullable) holds n host pointers (nullable each) */
 fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
+/* Autotuner: times each candidate launch configuration on trial_segments real
+ * segments of the live worlds (they advance as usual), keeps the fastest per
+ * voxel-update and remembers it for batches of the same make-up (live worlds
+ * per size class).  Knobs: worlds that fit one CTA may run in the next wider
+ * CTA class (promote), and the per-step kernel's CTAs per SM. */
+typedef struct fs3d_tune_report {
+    int promote;            /* chosen class promotion (0 = smallest fitting CTA)  */
+    int ctas_per_sm;        /* chosen CTAs per SM of the per-step kernel           */
+    int trials;             /* configurations timed                                */
+    int cached;             /* 1: taken from an earlier tuning of the same make-up */
+    int segments;           /* segments run while tuning (the worlds advanced)    */
+    double best_vox_per_ms; /* voxel-updates per ms of the choice                  */
+    double trial_vox_per_ms[8];
+} fs3d_tune_report;
+fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_report* out);
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells,
                              size_t* bytes_used, size_t* bytes_budget);
 fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream);
@@ -245,6 +260,38 @@ fs3d_status fs3d_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_de
  * at the centre, vertical FOV 70 degrees, aspect W/H). */
 void fs3d_camera_fs_raymarch(fs3d_camera* cam);
 void fs3d_camera_world_view(fs3d_camera* cam, int X, int Y, int Z, int W, int H);
+
+/* ---- the raymarch_sphere material (the object the upstream scene draws) ----
+ * Restates raymarch_sphere.vert:30-45 and .frag:18-51 with the fixed-function
+ * stages between them: the mesh (object space) is transformed by
+ * proj * rotY(cam_rot_y) * translate(cam_pos) * model (materials.cpp:531-536,
+ * OpenGL depth range, y negated), rasterised with no culling and a top-left
+ * rule at pixel centres, attributes interpolated linearly in screen space
+ * (noperspective), nearest fragment kept under LESS_OR_EQUAL against depth 1;
+ * each covered pixel marches a box SDF of half-extent 0.5 from the camera in
+ * object space, invModel * (-cam_pos), towards the interpolated position:
+ * (max(0.05, 1 - 0.05*steps), 0, 0, 1) on a hit, (0,0,0,1) on a miss; other
+ * pixels get `clear`.  W*H RGBA float32 into device memory, async on `stream`.
+ * A vertex behind the camera or outside the depth range (near/far clipping is
+ * not done) or a singular model gives FS3D_ERR_INVALID_ARG. */
+typedef struct fs3d_object_view {
+    float cam_pos[3];     /* the engine's camPos (renderer.h:148); the eye sits at -cam_pos */
+    float cam_rot_y_deg;  /* camRot.y in degrees (renderer.h:149)                            */
+    float fovy_deg;       /* vertical field of view                                          */
+    float aspect;
+    float znear, zfar;
+    float model[16];      /* column-major object transform                                  */
+    float clear[4];       /* colour of uncovered pixels                                      */
+} fs3d_object_view;
+/* the upstream scene: camPos (0,0,-5), camRot 0, 70 degrees, aspect
+ * 1700/900, depth 0.01..200, identity model, clear colour (0,0,1,1) */
+void fs3d_object_view_scene(fs3d_object_view* v);
+/* writes the scene's cube (assets/cube2.obj, +-1) as 12 triangles of 3
+ * vertices x 3 floats into tri_xyz (108 floats, may be NULL); returns 12 */
+int fs3d_mesh_cube(float* tri_xyz);
+/* ntri <= 48 triangles of 9 floats each (host memory) */
+fs3d_status fs3d_render_object(const fs3d_object_view* v, const float* tri_xyz, int ntri, int W, int H,
+                               float* rgba_dev, void* stream);
 
 /* ---- synthetic worlds (seeded, bit-reproducible) ---- */
 fs3d_status fs3d_gen_parity(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);

@@ -624,3 +624,193 @@ void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* 
             memcpy(rgba + 4 * ((size_t)py * (size_t)W + (size_t)px), out4, sizeof(out4));
         }
 }
+
+/* ---- raymarch_sphere material: the object the upstream scene draws --------
+ * Matrices follow materials.cpp:531-545 (view = rotY(camRot.y) * translate(camPos),
+ * glm::perspective with an OpenGL depth range and proj[1][1] negated) and
+ * raymarch_sphere.vert:30-45 (clip = viewproj*model*v; the fragment origin is
+ * invModel*(-camPos), the fragment position the object-space vertex, both
+ * noperspective).  Between the stages sit the fixed-function steps the
+ * pipeline configures: no culling (pipelines.cpp:114), depth LESS_OR_EQUAL
+ * against a buffer cleared to 1 (renderer.cpp:502-503, 1233), pixel centres
+ * at (px+0.5, py+0.5), and a top-left rule on shared edges.  The fragment
+ * stage is raymarch_sphere.frag:18-51.  Matrices are column-major,
+ * m[c*4 + r]; every sum runs left to right. */
+static void mat4_mul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int c = 0; c < 4; ++c)
+        for (int i = 0; i < 4; ++i)
+            r[c * 4 + i] = a[0 * 4 + i] * b[c * 4 + 0] + a[1 * 4 + i] * b[c * 4 + 1] +
+                           a[2 * 4 + i] * b[c * 4 + 2] + a[3 * 4 + i] * b[c * 4 + 3];
+    memcpy(out, r, sizeof(r));
+}
+
+/* inverse by 2x2 minors of the top and bottom row pairs (Laplace expansion,
+ * D. Eberly, "The Laplace Expansion Theorem", 2008); 0 if singular */
+static int mat4_inverse(const float* m, float* out) {
+#define A(r, c) m[(c) * 4 + (r)]
+    const float s0 = A(0, 0) * A(1, 1) - A(1, 0) * A(0, 1), s1 = A(0, 0) * A(1, 2) - A(1, 0) * A(0, 2);
+    const float s2 = A(0, 0) * A(1, 3) - A(1, 0) * A(0, 3), s3 = A(0, 1) * A(1, 2) - A(1, 1) * A(0, 2);
+    const float s4 = A(0, 1) * A(1, 3) - A(1, 1) * A(0, 3), s5 = A(0, 2) * A(1, 3) - A(1, 2) * A(0, 3);
+    const float c5 = A(2, 2) * A(3, 3) - A(3, 2) * A(2, 3), c4 = A(2, 1) * A(3, 3) - A(3, 1) * A(2, 3);
+    const float c3 = A(2, 1) * A(3, 2) - A(3, 1) * A(2, 2), c2 = A(2, 0) * A(3, 3) - A(3, 0) * A(2, 3);
+    const float c1 = A(2, 0) * A(3, 2) - A(3, 0) * A(2, 2), c0 = A(2, 0) * A(3, 1) - A(3, 0) * A(2, 1);
+    const float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    if (det == 0.0f || det != det) return 0;
+    const float k = 1.0f / det;
+    float b[16];
+#define B(r, c) b[(c) * 4 + (r)]
+    B(0, 0) = (A(1, 1) * c5 - A(1, 2) * c4 + A(1, 3) * c3) * k;
+    B(0, 1) = (-A(0, 1) * c5 + A(0, 2) * c4 - A(0, 3) * c3) * k;
+    B(0, 2) = (A(3, 1) * s5 - A(3, 2) * s4 + A(3, 3) * s3) * k;
+    B(0, 3) = (-A(2, 1) * s5 + A(2, 2) * s4 - A(2, 3) * s3) * k;
+    B(1, 0) = (-A(1, 0) * c5 + A(1, 2) * c2 - A(1, 3) * c1) * k;
+    B(1, 1) = (A(0, 0) * c5 - A(0, 2) * c2 + A(0, 3) * c1) * k;
+    B(1, 2) = (-A(3, 0) * s5 + A(3, 2) * s2 - A(3, 3) * s1) * k;
+    B(1, 3) = (A(2, 0) * s5 - A(2, 2) * s2 + A(2, 3) * s1) * k;
+    B(2, 0) = (A(1, 0) * c4 - A(1, 1) * c2 + A(1, 3) * c0) * k;
+    B(2, 1) = (-A(0, 0) * c4 + A(0, 1) * c2 - A(0, 3) * c0) * k;
+    B(2, 2) = (A(3, 0) * s4 - A(3, 1) * s2 + A(3, 3) * s0) * k;
+    B(2, 3) = (-A(2, 0) * s4 + A(2, 1) * s2 - A(2, 3) * s0) * k;
+    B(3, 0) = (-A(1, 0) * c3 + A(1, 1) * c1 - A(1, 2) * c0) * k;
+    B(3, 1) = (A(0, 0) * c3 - A(0, 1) * c1 + A(0, 2) * c0) * k;
+    B(3, 2) = (-A(3, 0) * s3 + A(3, 1) * s1 - A(3, 2) * s0) * k;
+    B(3, 3) = (A(2, 0) * s3 - A(2, 1) * s1 + A(2, 2) * s0) * k;
+#undef A
+#undef B
+    memcpy(out, b, sizeof(b));
+    return 1;
+}
+
+void orc_object_mvp(const orc_object_view* v, float* mvp) {
+    const float fovy = v->fovy_deg * 0.0174532925199432957692f;
+    const float th = tanf(fovy * 0.5f);
+    float P[16] = {0};
+    P[0] = 1.0f / (v->aspect * th);
+    P[5] = -(1.0f / th); /* proj[1][1] *= -1 */
+    P[10] = -(v->zfar + v->znear) / (v->zfar - v->znear);
+    P[11] = -1.0f;
+    P[14] = -(2.0f * v->zfar * v->znear) / (v->zfar - v->znear);
+    const float ang = v->cam_rot_y_deg * 0.0174532925199432957692f;
+    const float c = cosf(ang), s = sinf(ang);
+    float R[16] = {c, 0, -s, 0, 0, 1, 0, 0, s, 0, c, 0, 0, 0, 0, 1};
+    float T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, v->cam_pos[0], v->cam_pos[1], v->cam_pos[2], 1};
+    float V[16];
+    mat4_mul(R, T, V);
+    mat4_mul(P, V, mvp);
+    mat4_mul(mvp, v->model, mvp);
+}
+
+/* edge function of p against a->b (y down: > 0 on the interior side of a
+ * positively oriented triangle) */
+static inline float edge_fn(const float* a, const float* b, float px, float py) {
+    return (b[0] - a[0]) * (py - a[1]) - (b[1] - a[1]) * (px - a[0]);
+}
+static inline int top_left(const float* a, const float* b) {
+    return b[1] < a[1] || (b[1] == a[1] && b[0] > a[0]);
+}
+
+/* raymarch_sphere.frag:13-16 (box of half-extent 0.5) */
+static inline float box_sdf(float x, float y, float z) {
+    const float qx = fabsf(x) - 0.5f, qy = fabsf(y) - 0.5f, qz = fabsf(z) - 0.5f;
+    const float mx = fmaxf(qx, 0.0f), my = fmaxf(qy, 0.0f), mz = fmaxf(qz, 0.0f);
+    return sqrtf(mx * mx + my * my + mz * mz) + fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f);
+}
+
+int orc_render_object(const orc_object_view* v, const float* tri, int ntri, int W, int H, float* rgba) {
+    if (ntri < 0 || ntri > ORC_OBJECT_MAX_TRIS) return -1;
+    float mvp[16], inv[16];
+    orc_object_mvp(v, mvp);
+    if (!mat4_inverse(v->model, inv)) return -1;
+    const float ncp[3] = {-v->cam_pos[0], -v->cam_pos[1], -v->cam_pos[2]};
+    float o[3];
+    for (int i = 0; i < 3; ++i) o[i] = inv[0 * 4 + i] * ncp[0] + inv[1 * 4 + i] * ncp[1] + inv[2 * 4 + i] * ncp[2] + inv[3 * 4 + i];
+    /* triangle set-up: screen positions, orientation, top-left edges */
+    float sv[ORC_OBJECT_MAX_TRIS][3][3], at[ORC_OBJECT_MAX_TRIS][3][3], area[ORC_OBJECT_MAX_TRIS];
+    int tl[ORC_OBJECT_MAX_TRIS][3];
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    for (int t = 0; t < ntri; ++t) {
+        for (int k = 0; k < 3; ++k) {
+            const float* p = tri + 9 * t + 3 * k;
+            float cl[4];
+            for (int i = 0; i < 4; ++i) cl[i] = mvp[0 * 4 + i] * p[0] + mvp[1 * 4 + i] * p[1] + mvp[2 * 4 + i] * p[2] + mvp[3 * 4 + i];
+            if (!(cl[3] > 0.0f)) return -1;
+            const float nx = cl[0] / cl[3], ny = cl[1] / cl[3], nz = cl[2] / cl[3];
+            if (!(nz >= 0.0f && nz <= 1.0f)) return -1; /* clipping is not restated */
+            sv[t][k][0] = nx * hw + hw;
+            sv[t][k][1] = ny * hh + hh;
+            sv[t][k][2] = nz;
+            memcpy(at[t][k], p, 3 * sizeof(float));
+        }
+        area[t] = edge_fn(sv[t][0], sv[t][1], sv[t][2][0], sv[t][2][1]);
+        if (area[t] < 0.0f) {
+            float tmp[3];
+            memcpy(tmp, sv[t][1], sizeof(tmp));
+            memcpy(sv[t][1], sv[t][2], sizeof(tmp));
+            memcpy(sv[t][2], tmp, sizeof(tmp));
+            memcpy(tmp, at[t][1], sizeof(tmp));
+            memcpy(at[t][1], at[t][2], sizeof(tmp));
+            memcpy(at[t][2], tmp, sizeof(tmp));
+            area[t] = edge_fn(sv[t][0], sv[t][1], sv[t][2][0], sv[t][2][1]);
+        }
+        tl[t][0] = top_left(sv[t][1], sv[t][2]);
+        tl[t][1] = top_left(sv[t][2], sv[t][0]);
+        tl[t][2] = top_left(sv[t][0], sv[t][1]);
+    }
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const float fx = (float)px + 0.5f, fy = (float)py + 0.5f;
+            float best = 1.0f, pos[3];
+            int hit = 0;
+            for (int t = 0; t < ntri; ++t) {
+                if (!(area[t] > 0.0f)) continue;
+                const float w0 = edge_fn(sv[t][1], sv[t][2], fx, fy);
+                const float w1 = edge_fn(sv[t][2], sv[t][0], fx, fy);
+                const float w2 = edge_fn(sv[t][0], sv[t][1], fx, fy);
+                if (!(w0 > 0.0f || (w0 == 0.0f && tl[t][0]))) continue;
+                if (!(w1 > 0.0f || (w1 == 0.0f && tl[t][1]))) continue;
+                if (!(w2 > 0.0f || (w2 == 0.0f && tl[t][2]))) continue;
+                const float l0 = w0 / area[t], l1 = w1 / area[t], l2 = w2 / area[t];
+                const float z = l0 * sv[t][0][2] + l1 * sv[t][1][2] + l2 * sv[t][2][2];
+                if (!(z <= best)) continue;
+                best = z;
+                hit = 1;
+                for (int i = 0; i < 3; ++i) pos[i] = l0 * at[t][0][i] + l1 * at[t][1][i] + l2 * at[t][2][i];
+            }
+            float* out = rgba + 4 * ((size_t)py * (size_t)W + (size_t)px);
+            if (!hit) {
+                memcpy(out, v->clear, 4 * sizeof(float));
+                continue;
+            }
+            float d[3] = {pos[0] - o[0], pos[1] - o[1], pos[2] - o[2]};
+            normalize3(d);
+            float col = 0.0f, t = 0.0f, density = 1.0f;
+            for (int it = 0; it < 64; ++it) { /* ray_march, raymarch_sphere.frag:18-43 */
+                const float dist = box_sdf(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
+                if (dist < 0.001f) {
+                    col = fmaxf(0.05f, density);
+                    break;
+                } else if (t > 1000.0f) {
+                    break;
+                }
+                t += dist;
+                density -= 0.05f;
+            }
+            out[0] = col;
+            out[1] = 0.0f;
+            out[2] = 0.0f;
+            out[3] = 1.0f;
+        }
+    return 0;
+}
+
+/* assets/cube2.obj: the +-1 cube of the scene, its 12 faces in file order */
+int orc_mesh_cube(float* tri) {
+    static const float vtx[8][3] = {{1, 1, -1}, {1, -1, -1}, {1, 1, 1}, {1, -1, 1},
+                                    {-1, 1, -1}, {-1, -1, -1}, {-1, 1, 1}, {-1, -1, 1}};
+    static const int face[12][3] = {{5, 3, 1}, {3, 8, 4}, {7, 6, 8}, {2, 8, 6}, {1, 4, 2}, {5, 2, 6},
+                                    {5, 7, 3}, {3, 7, 8}, {7, 5, 6}, {2, 4, 8}, {1, 3, 4}, {5, 1, 2}};
+    for (int t = 0; t < 12; ++t)
+        for (int k = 0; k < 3; ++k) memcpy(tri + 9 * t + 3 * k, vtx[face[t][k] - 1], 3 * sizeof(float));
+    return 12;
+}

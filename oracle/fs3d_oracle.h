@@ -80,6 +80,21 @@ void orc_render_sdf(const orc_camera* cam, int W, int H, float* rgba);
 void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* cam,
                     int W, int H, float* rgba);
 
+/* raymarch_sphere material: a triangle mesh rasterised with noperspective
+ * attributes, each covered pixel marching a box SDF in object space */
+#define ORC_OBJECT_MAX_TRIS 48
+typedef struct {
+    float cam_pos[3];     /* engine camPos; the eye sits at -cam_pos */
+    float cam_rot_y_deg;  /* camRot.y */
+    float fovy_deg, aspect, znear, zfar;
+    float model[16];      /* column-major */
+    float clear[4];
+} orc_object_view;
+void orc_object_mvp(const orc_object_view* v, float* mvp);
+/* 0, or -1 when a vertex falls outside the depth range or the model is singular */
+int orc_render_object(const orc_object_view* v, const float* tri, int ntri, int W, int H, float* rgba);
+int orc_mesh_cube(float* tri /* 108 floats */);
+
 #ifdef __cplusplus
 }
 #endif

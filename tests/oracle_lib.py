@@ -16,6 +16,24 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "build", "liboracle.so")
 
 
+class ObjectView(C.Structure):
+    _fields_ = [("cam_pos", C.c_float * 3), ("cam_rot_y_deg", C.c_float), ("fovy_deg", C.c_float),
+                ("aspect", C.c_float), ("znear", C.c_float), ("zfar", C.c_float), ("model", C.c_float * 16),
+                ("clear", C.c_float * 4)]
+
+
+def scene_view(**kw) -> ObjectView:
+    """The upstream scene: camPos (0,0,-5), camRot 0, 70 degrees, aspect
+    1700/900, depth 0.01..200, identity model, blue clear colour."""
+    v = ObjectView()
+    v.cam_pos[:] = kw.get("cam_pos", (0.0, 0.0, -5.0))
+    v.cam_rot_y_deg = kw.get("rot_y", 0.0)
+    v.fovy_deg, v.aspect, v.znear, v.zfar = 70.0, 1700.0 / 900.0, 0.01, 200.0
+    v.model[:] = [float(x) for x in np.asarray(kw.get("model", np.eye(4)), np.float32).T.reshape(-1)]
+    v.clear[:] = (0.0, 0.0, 1.0, 1.0)
+    return v
+
+
 class Camera(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
                 ("up", C.c_float * 3), ("tan_half_fov", C.c_float), ("aspect", C.c_float),
@@ -48,6 +66,9 @@ class Oracle:
             "orc_gen_c5": (None, [u64, i32, i32, i32, vp]),
             "orc_render_sdf": (None, [C.POINTER(Camera), i32, i32, vp]),
             "orc_render_dda": (None, [vp, i32, i32, i32, C.POINTER(Camera), i32, i32, vp]),
+            "orc_render_object": (i32, [C.POINTER(ObjectView), vp, i32, i32, i32, vp]),
+            "orc_object_mvp": (None, [C.POINTER(ObjectView), vp]),
+            "orc_mesh_cube": (i32, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -113,6 +134,23 @@ class Oracle:
         img = np.empty((H, W, 4), np.float32)
         self.L.orc_render_sdf(C.byref(cam), W, H, img.ctypes.data)
         return img
+
+    def mesh_cube(self) -> np.ndarray:
+        tri = np.empty((12, 3, 3), np.float32)
+        self.L.orc_mesh_cube(tri.ctypes.data)
+        return tri
+
+    def object_mvp(self, view: ObjectView) -> np.ndarray:
+        m = np.empty(16, np.float32)
+        self.L.orc_object_mvp(C.byref(view), m.ctypes.data)
+        return m.reshape(4, 4).T  # row-major view of the column-major matrix
+
+    def render_object(self, view: ObjectView, tri: np.ndarray, W: int, H: int):
+        """RGBA image, or None when the oracle rejects the view."""
+        tri = np.ascontiguousarray(tri, np.float32)
+        img = np.empty((H, W, 4), np.float32)
+        rc = self.L.orc_render_object(C.byref(view), tri.ctypes.data, tri.shape[0], W, H, img.ctypes.data)
+        return img if rc == 0 else None
 
     def render_dda(self, g: np.ndarray, cam: Camera, W: int, H: int) -> np.ndarray:
         Y, Z, X = g.shape

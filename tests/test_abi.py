@@ -73,3 +73,19 @@ def test_bad_arguments_return_status(fs3d):
         fs3d.check(fs3d.ERR_BUDGET)
     assert e.value.status == fs3d.ERR_BUDGET
     assert L.fs3d_world_load(b"/nonexistent/ckp", 0, C.byref(h)) == fs3d.ERR_IO
+
+
+def test_object_render_rejects_before_launch(fs3d):
+    """Views the restatement does not cover are refused on the host, with no
+    device work: an eye inside the cube (a vertex behind the camera), a
+    singular model, and more than 48 triangles."""
+    tri = fs3d.mesh_cube()
+    fake = 16  # never dereferenced: every case fails in the host set-up
+    for view in (fs3d.object_view_scene(cam_pos=(0.0, 0.0, 0.0)),
+                 fs3d.object_view_scene(model=np.zeros((4, 4)))):
+        with pytest.raises(fs3d.Fs3dError) as e:
+            fs3d.render_object_device(view, tri, 64, 32, fake)
+        assert e.value.status == fs3d.ERR_INVALID_ARG
+    with pytest.raises(fs3d.Fs3dError):
+        fs3d.render_object_device(fs3d.object_view_scene(), np.concatenate([tri] * 5), 64, 32, fake)
+    assert fs3d.mesh_cube().shape == (12, 3, 3)

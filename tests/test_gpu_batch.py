@@ -193,3 +193,28 @@ def test_world_resident_path_matches_oracle(fs3d, orc, dims):
         orc.run(ref, 7, 3, 46, nthreads=0)
         got = w.read()
     assert (got == ref).all()
+
+
+def test_autotune_keeps_results_exact(fs3d, orc):
+    """Tuning runs real segments under every candidate configuration (class
+    promotion, per-step grid); the worlds must end exactly where the oracle
+    puts them, and a second batch of the same make-up reuses the choice."""
+    worlds = small_batch(fs3d, 21, 20, max_dim=160)
+    worlds += [((300, 40, 96), 991), ((512, 64, 256), 992), ((2048, 6, 4), 993)]  # cluster and per-step worlds
+    n = 600
+    for rep in range(2):
+        with fs3d.Batch(4 * GiB, steps_per_segment=32) as b:
+            tickets = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for dims, seed in worlds]
+            rpt = b.autotune(trial_segments=1)
+            assert rpt["cached"] == (rep == 1), rpt
+            if rep == 0:
+                assert rpt["trials"] >= 3 and rpt["best_vox_per_ms"] > 0, rpt
+            assert 0 <= rpt["promote"] <= 2 and rpt["ctas_per_sm"] >= 1
+            for _ in range(n // 32 + 1):
+                b.run_segment()
+            b.sync()
+            for t, (dims, seed) in zip(tickets, worlds):
+                done, h = b.poll(t)
+                assert done
+                exp = oracle_final(orc, fs3d, dims, seed, n)
+                assert h == orc.hash(exp), (rep, dims, seed, rpt)

@@ -66,3 +66,47 @@ def test_world_render_to_device(fs3d, orc, cuda):
         w.render(cam, W, H, fs3d.RENDER_DDA, out_ptr=out.data_ptr())
         w.sync()
         check_img(out.cpu().numpy(), orc.render_dda(g, oracle_lib.camera_from(cam), W, H))
+
+
+def _object_cases():
+    rx = np.eye(4)
+    c, s = np.cos(np.radians(30)), np.sin(np.radians(30))
+    rx[1:3, 1:3] = [[c, -s], [s, c]]
+    ry = np.eye(4)
+    c, s = np.cos(np.radians(40)), np.sin(np.radians(40))
+    ry[0, 0], ry[0, 2], ry[2, 0], ry[2, 2] = c, s, -s, c
+    model = rx @ ry @ np.diag([1.2, 0.8, 1.0, 1.0])
+    model[:3, 3] = (0.3, -0.2, 0.5)
+    return [("scene", {}, (850, 450)), ("scene", {}, (1920, 1080)), ("scene", {}, (333, 217)),
+            ("rot_y", {"rot_y": 25.0}, (850, 450)), ("model", {"model": model}, (640, 360)),
+            ("moved", {"cam_pos": (1.5, -1.0, -3.0), "rot_y": -20.0}, (850, 450))]
+
+
+@pytest.mark.parametrize("case", _object_cases(), ids=lambda c: f"{c[0]}-{c[2][0]}x{c[2][1]}")
+def test_object_material_matches_cpu_bit_exact(fs3d, orc, cuda, case):
+    _, kw, (W, H) = case
+    tri = fs3d.mesh_cube()
+    view = fs3d.object_view_scene(**kw)
+    out = cuda.full((H, W, 4), -1.0, dtype=cuda.float32, device="cuda")
+    fs3d.render_object_device(view, tri, W, H, out.data_ptr(), cuda.cuda.current_stream().cuda_stream)
+    got = out.cpu().numpy()
+    exp = orc.render_object(oracle_lib.scene_view(**kw), tri, W, H)
+    assert exp is not None
+    if not np.array_equal(got, exp):
+        d = np.argwhere((got != exp).any(-1))
+        y, x = d[0]
+        pytest.fail(f"{len(d)} pixels differ; first (x={x}, y={y}): got {got[y, x]} expected {exp[y, x]}")
+    assert (got[..., 0] > 0).sum() > 0.005 * W * H
+
+
+def test_object_material_custom_mesh(fs3d, orc, cuda):
+    """Two cubes (the second shifted and shrunk) and a ragged triangle count."""
+    a = fs3d.mesh_cube()
+    b = a * 0.4 + np.array([1.3, 0.2, -0.5], np.float32)
+    tri = np.concatenate([a, b, a[:5] * 0.7])
+    W, H = 512, 288
+    view = fs3d.object_view_scene(rot_y=10.0)
+    out = cuda.empty((H, W, 4), dtype=cuda.float32, device="cuda")
+    fs3d.render_object_device(view, tri, W, H, out.data_ptr(), cuda.cuda.current_stream().cuda_stream)
+    exp = orc.render_object(oracle_lib.scene_view(rot_y=10.0), tri, W, H)
+    assert np.array_equal(out.cpu().numpy(), exp)
