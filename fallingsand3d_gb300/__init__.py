@@ -45,7 +45,7 @@ EXPORTS = (
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
     "fs3d_batch_retire_many",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
-    "fs3d_batch_stats", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
+    "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
     "fs3d_render_object", "fs3d_gen_parity", "fs3d_gen_pillars",
     "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
@@ -149,6 +149,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
         "fs3d_batch_retire": (S, [vp, u64, vp]),
         "fs3d_batch_autotune": (S, [vp, i32, C.POINTER(TuneReport)]),
+        "fs3d_batch_counters": (S, [vp, C.POINTER(u64), C.POINTER(u64)]),
         "fs3d_batch_stats": (S, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_size_t),
                                  C.POINTER(C.c_size_t)]),
         "fs3d_batch_stream": (S, [vp, C.POINTER(vp)]),
@@ -500,6 +501,12 @@ class Batch:
         g = np.empty(shape, np.uint8)
         check(lib().fs3d_batch_retire(self.handle, ticket, _ptr(g)))
         return g
+
+    def counters(self) -> dict:
+        """Cell-steps since creation: all of them (dense) and those evaluated."""
+        d, p = u64(0), u64(0)
+        check(lib().fs3d_batch_counters(self.handle, C.byref(d), C.byref(p)))
+        return {"dense_cell_steps": int(d.value), "processed_cell_steps": int(p.value)}
 
     def autotune(self, trial_segments: int = 2) -> dict:
         """Times the launch configurations on real segments and keeps the best."""

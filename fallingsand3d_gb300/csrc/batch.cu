@@ -98,7 +98,10 @@ struct fs3d_batch {
     int grid = 0;
     int promote = 0;  // single-CTA resident worlds run this many classes wider (autotuned)
     unsigned long long* hash_dev = nullptr;
+    unsigned long long* processed_dev = nullptr;  // cell-steps the resident kernels evaluated
     uint64_t segments = 0;
+    uint64_t dense_cell_steps = 0;   // every cell of every stepped world, per step
+    uint64_t stepped_cell_steps = 0; // of those, taken by the per-step kernel (always evaluated)
 };
 
 namespace {
@@ -143,7 +146,7 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork) {
     if (b->cfg.use_smem)
         for (int c = 0; c < kResidentClasses && s == FS3D_OK; ++c)
             s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
-                                              fork ? b->branch[c] : a);
+                                              fork ? b->branch[c] : a, b->processed_dev);
     for (int k = 0; k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
         s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, fork ? b->branch[kResidentClasses] : a);
     if (s != FS3D_OK) return s;
@@ -200,6 +203,8 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->processed_dev, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->processed_dev, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int) * kResidentClasses);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
@@ -364,6 +369,9 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         d.nw = w.nw;
         d.steps = steps;
         d.lg = plane_lg(w.nw);
+        const uint64_t cs = (uint64_t)w.X * w.Y * w.Z * (uint64_t)steps;
+        b->dense_cell_steps += cs;
+        if (run[wi].first < 0) b->stepped_cell_steps += cs;
         if (run[wi].first >= 0) {
             by_class[run[wi].first].push_back((int)wi);
         } else {
@@ -810,6 +818,16 @@ fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_rep
     return FS3D_OK;
 }
 
+fs3d_status fs3d_batch_counters(fs3d_batch* b, uint64_t* dense_cell_steps, uint64_t* processed_cell_steps) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_counters: NULL batch");
+    FS3D_CUDA(cudaStreamSynchronize(b->stream));
+    unsigned long long dev = 0;
+    FS3D_CUDA(cudaMemcpy(&dev, b->processed_dev, sizeof(dev), cudaMemcpyDeviceToHost));
+    if (dense_cell_steps) *dense_cell_steps = b->dense_cell_steps;
+    if (processed_cell_steps) *processed_cell_steps = (uint64_t)dev + b->stepped_cell_steps;
+    return FS3D_OK;
+}
+
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells, size_t* bytes_used,
                              size_t* bytes_budget) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_stats: NULL batch");
@@ -845,6 +863,7 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     cudaFree(b->hash_dev);
     cudaFree(b->counter);
     cudaFree(b->err);
+    cudaFree(b->processed_dev);
     if (b->fork) cudaEventDestroy(b->fork);
     for (int c = 0; c <= kResidentClasses; ++c) {
         if (b->join[c]) cudaEventDestroy(b->join[c]);

@@ -299,42 +299,74 @@ __device__ __forceinline__ void bulk_store_wait(void* gdst, const void* smem_src
 
 // The rows of one world held in shared memory by the CTAs of a cluster: CTA
 // r holds rows y in [lo_r, hi_r) (lo_r even), stored as ((y - lo_r)*Z + z)*nw
-// + word.  `left` is the shared memory of CTA r-1 (null for r == 0): the only
-// row a CTA reads outside its slab is y = lo_r - 1, in the odd phase.
+// + word, followed (at the next 16-byte boundary) by one flag byte per row:
+// the low 8 bits of the last step that changed the row.  `left` is the
+// shared memory of CTA r-1 (null for r == 0): the only row a CTA touches
+// outside its slab is y = lo_r - 1, in the odd phase.
 template <bool CL>
 struct SlabView {
     uint4* mine;
     uint4* left;
+    uint8_t* fmine;
+    uint8_t* fleft;
     int lo, hi, left_lo, Z, nw;
     __device__ __forceinline__ uint4* at(int y, int z, int g) const {
         if (!CL || y >= lo) return mine + ((y - lo) * Z + z) * nw + g;
         return left + ((y - left_lo) * Z + z) * nw + g;
     }
+    __device__ __forceinline__ uint8_t* flag(int y, int z) const {
+        if (!CL || y >= lo) return fmine + (y - lo) * Z + z;
+        return fleft + (y - left_lo) * Z + z;
+    }
 };
 
+// bytes of a slab's planes, rounded up so its row flags start 16-byte aligned
+__host__ __device__ __forceinline__ uint32_t slab_flag_offset(uint32_t plane_bytes) {
+    return (plane_bytes + 15u) & ~15u;
+}
+
 // A block row-pair (j, k) of a world held in shared memory.  Every lane of
-// the warp calls this.
+// the warp calls this.  The pair is skipped when none of its rows changed in
+// the two previous steps: its cells are then those of its last evaluation in
+// the same phase, two steps back, which changed nothing, and whether a block
+// can change depends on its cells alone (the rule's activity mask), so it
+// would change nothing again.  The first two steps of a segment evaluate
+// every pair (the flags start at step t0 - 1).
 template <bool CL>
-__device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk, int j,
-                                             int k, bool valid, int gl, int G) {
-    const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
+__device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk,
+                                             uint32_t tt, int j, int k, bool valid, int gl, int G,
+                                             unsigned long long* s_processed) {
     const int y0 = 2 * j - o, z0 = 2 * k - o;
-    const bool has = valid && gl < w.nw;
-    uint4 q[4], q0[4];
-    uint4* ptr[4];
+    bool in[4], dirty = false;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
-        const bool in = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
-        ptr[a] = in ? v.at(y, z, gl) : nullptr;
-        q[a] = in ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
-        q0[a] = q[a];
+        in[a] = valid && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
+        if (in[a]) dirty |= ((tt - (uint32_t)*v.flag(y, z)) & 0xFFu) <= 2u;
     }
+    if (!__any_sync(0xFFFFFFFFu, dirty)) return;
+    const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
+    const bool has = dirty && gl < w.nw;
+    uint4 q[4], q0[4];
+    uint4* ptr[4];
+    uint32_t rows_in = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+        ptr[a] = (has && in[a]) ? v.at(y, z, gl) : nullptr;
+        q[a] = ptr[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        q0[a] = q[a];
+        rows_in += ptr[a] ? 1u : 0u;
+    }
+    const uint32_t cells = __reduce_add_sync(0xFFFFFFFFu, has ? rows_in * (uint32_t)min(64, w.X - 64 * gl) : 0u);
+    if ((threadIdx.x & 31) == 0 && cells) atomicAdd(s_processed, (unsigned long long)cells);
     rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        if (ptr[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
+        if (ptr[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w)) {
             *ptr[a] = q[a];
+            *v.flag((a < 2) ? y0 + 1 : y0, z0 + (a & 1)) = (uint8_t)tt;
+        }
 }
 
 // first row of slab r of CS slabs (even, so even-phase row-pairs never straddle)
@@ -361,7 +393,8 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
     k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
                                                              const int* __restrict__ order,
                                                              const int* __restrict__ meta, int cls, int CS,
-                                                             int* counter, int* err) {
+                                                             int* counter, int* err,
+                                                             unsigned long long* processed_cells) {
     extern __shared__ __align__(128) uint4 srows[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int item;
@@ -380,6 +413,8 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
     uint32_t phase = 0;
     const int lane = threadIdx.x & 31;
     uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
+    __shared__ unsigned long long s_processed;  // cell-steps evaluated (the rest were skipped as settled)
+    if (threadIdx.x == 0) s_processed = 0;
     for (;;) {
         // after an error every group stops taking worlds (and all of a cluster stop together)
         if (r == 0 && threadIdx.x == 0) item = *(volatile int*)err ? n : atomicAdd(counter, 1);
@@ -399,8 +434,18 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
         v.nw = w.nw;
         const uint32_t row_bytes = (uint32_t)w.Z * (uint32_t)w.nw * 16u;
         const uint32_t bytes = (uint32_t)(v.hi - v.lo) * row_bytes;
+        v.fmine = reinterpret_cast<uint8_t*>(srows) + slab_flag_offset(bytes);
+        v.fleft = left ? reinterpret_cast<uint8_t*>(left) + slab_flag_offset((uint32_t)(v.lo - v.left_lo) * row_bytes)
+                       : nullptr;
         uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
         if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
+        {
+            // every row counts as changed at step t0 - 1: the first two steps evaluate all pairs
+            const uint32_t f = ((uint32_t)(w.t - 1u) & 0xFFu) * 0x01010101u;
+            uint32_t* fw = reinterpret_cast<uint32_t*>(v.fmine);
+            const int nf = ((v.hi - v.lo) * w.Z + 3) / 4;
+            for (int i = threadIdx.x; i < nf; i += NT) fw[i] = f;
+        }
         bool ok = true;
         if (bytes) {
             ok = mbar_wait(&bar, phase);
@@ -426,11 +471,12 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
             const int NBZ = nblocks(w.Z, o);
             const int j_lo = v.lo / 2, j_hi = (r == CS - 1) ? nblocks(w.Y, o) : v.hi / 2;
             const int nrp = (j_hi - j_lo) * NBZ;
+            const uint32_t tt = (uint32_t)t & 0xFFu;
             for (int base = 0; base < nrp; base += per) {
                 const int rp = base + (int)(threadIdx.x >> w.lg);
                 const bool valid = rp < nrp;
                 const int jj = valid ? rp / NBZ : 0;
-                slab_rowpair(v, w, o, sk, j_lo + jj, valid ? rp - jj * NBZ : 0, valid, gl, G);
+                slab_rowpair(v, w, o, sk, tt, j_lo + jj, valid ? rp - jj * NBZ : 0, valid, gl, G, &s_processed);
             }
             group_sync();
         }
@@ -440,6 +486,8 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
         if (threadIdx.x == 0 && bytes && !poisoned) bulk_store_wait(gslab, srows, bytes);
         group_sync();  // the slab is free again (and no neighbour still reads it)
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && processed_cells && s_processed) atomicAdd(processed_cells, s_processed);
 }
 
 // ---------------------------------------------------------------------------
@@ -506,7 +554,9 @@ int resident_class(int X, int Y, int Z) {
         // slab must be non-empty so the row below a slab is in its neighbour
         const int64_t nyp = (Y + 1) / 2;
         const int64_t mx = k.cs == 1 ? Y : 2 * ((nyp + k.cs - 1) / k.cs);
-        if (mx * row_bytes <= k.smem && (k.cs == 1 || nyp >= k.cs)) return c;
+        // planes, then one flag byte per row (padded to whole words)
+        const int64_t need = ((mx * row_bytes + 15) & ~(int64_t)15) + ((mx * Z + 15) & ~(int64_t)15);
+        if (need <= k.smem && (k.cs == 1 || nyp >= k.cs)) return c;
     }
     return -1;
 }
@@ -517,7 +567,8 @@ int smem_world_limit() {
 }
 
 fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
-                                          int* counter, int* err, cudaStream_t st) {
+                                          int* counter, int* err, cudaStream_t st,
+                                          unsigned long long* processed_cells) {
     init_classes();
     const ResidentCfg& k = g_classes[cls];
     if (!k.smem) return set_error(FS3D_ERR_CUDA, "resident segment kernel unavailable for this class");
@@ -538,13 +589,17 @@ fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, con
     const int CS = k.cs;
     cudaError_t e;
     if (k.cs > 1)
-        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<512, true>, worlds, order, meta, cls, CS, counter, err);
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<512, true>, worlds, order, meta, cls, CS, counter, err,
+                               processed_cells);
     else if (k.threads == 128)
-        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<128, false>, worlds, order, meta, cls, CS, counter, err);
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<128, false>, worlds, order, meta, cls, CS, counter, err,
+                               processed_cells);
     else if (k.threads == 256)
-        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<256, false>, worlds, order, meta, cls, CS, counter, err);
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<256, false>, worlds, order, meta, cls, CS, counter, err,
+                               processed_cells);
     else
-        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<768, false>, worlds, order, meta, cls, CS, counter, err);
+        e = cudaLaunchKernelEx(&lc, k_plane_segment_resident<768, false>, worlds, order, meta, cls, CS, counter, err,
+                               processed_cells);
     if (e != cudaSuccess) return cuda_fail(e, "resident segment launch");
     note_launch();
     return FS3D_OK;

@@ -42,9 +42,12 @@ int resident_class(int X, int Y, int Z);
 int smem_world_limit();
 // One launch steps every world of class `cls` (order[meta[1+K+cls] ...],
 // meta[1+cls] of them) through its segment steps in shared memory.  *err is
-// set to 1 if a bulk copy does not complete within the wait limit.
+// set to 1 if a bulk copy does not complete within the wait limit.  Row
+// pairs whose rows are settled are skipped; the cell-steps actually evaluated
+// are added to *processed_cells when it is not null.
 fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
-                                          int* counter, int* err, cudaStream_t st);
+                                          int* counter, int* err, cudaStream_t st,
+                                          unsigned long long* processed_cells = nullptr);
 
 // One world of a many-world conversion: its planes, its static bytes
 // (nullable) and the offset of its canonical bytes in a shared staging buffer.

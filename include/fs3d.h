@@ -200,6 +200,11 @@ typedef struct fs3d_tune_report {
     double trial_vox_per_ms[8];
 } fs3d_tune_report;
 fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_report* out);
+/* Work counters since creation (waits for the batch stream): every cell of
+ * every stepped world once per step (dense), and the cell-steps actually
+ * evaluated: resident worlds skip block row-pairs whose rows did not change
+ * in the two previous steps (exact: such blocks cannot change). */
+fs3d_status fs3d_batch_counters(fs3d_batch* b, uint64_t* dense_cell_steps, uint64_t* processed_cell_steps);
 fs3d_status fs3d_batch_stats(const fs3d_batch* b, int64_t* live_worlds, int64_t* live_cells,
                              size_t* bytes_used, size_t* bytes_budget);
 fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream);

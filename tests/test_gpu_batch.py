@@ -159,7 +159,7 @@ def test_admit_many_and_retire_many(fs3d, orc):
         assert len(b.admit_many(big, [1, 2, 3], 8)) == 2  # the third does not fit
 
 
-# dims that land in each resident class (one CTA of 128/256/512 threads,
+# dims that land in each resident class (one CTA of 128/256/768 threads,
 # clusters of 2/4/8 CTAs) and one too large to be resident
 CLASS_DIMS = [(16, 16, 16), (64, 64, 64), (64, 96, 128), (96, 96, 96), (128, 128, 128), (128, 256, 128),
               (64, 512, 128), (40, 37, 21), (130, 66, 90)]
@@ -218,3 +218,41 @@ def test_autotune_keeps_results_exact(fs3d, orc):
                 assert done
                 exp = oracle_final(orc, fs3d, dims, seed, n)
                 assert h == orc.hash(exp), (rep, dims, seed, rpt)
+
+
+@pytest.mark.parametrize("dims", [CLASS_DIMS[0], CLASS_DIMS[2], CLASS_DIMS[3], CLASS_DIMS[5]])
+@pytest.mark.parametrize("start", [0, 250, (1 << 32) - 7])
+def test_settled_row_skip_long_segments(fs3d, orc, dims, start):
+    """Resident launches skip row pairs whose rows did not change in the two
+    previous steps, tracked by the low 8 bits of the step.  Long launches (the
+    step counter wraps those 8 bits several times, from starts on and off the
+    wrap) let most of a world settle while water keeps moving; the result must
+    be the oracle's, step for step in the hashes."""
+    X, Y, Z = dims
+    seed = 4242
+    g = fs3d.gen_batch_world(seed, X, Y, Z)
+    ref = g.copy()
+    with fs3d.World(g, seed, start, fs3d.LAYOUT_PLANES) as w:
+        for n in (700, 1, 2, 300):
+            w.step(n)
+            orc.run(ref, seed, start, n, nthreads=0)
+            start += n
+            assert w.hash() == orc.hash(ref), (dims, start)
+        assert (w.read() == ref).all()
+
+
+def test_counters_dense_and_processed(fs3d, orc):
+    """dense = every cell of every world per step; processed <= dense, and
+    below it once the worlds have settled (first two steps of each segment
+    evaluate everything)."""
+    worlds = small_batch(fs3d, 8, 10, max_dim=64)
+    n = 512
+    with fs3d.Batch(GiB, steps_per_segment=128) as b:
+        tickets = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for dims, seed in worlds]
+        for _ in range(n // 128):
+            b.run_segment()
+        c = b.counters()
+        assert c["dense_cell_steps"] == n * sum(X * Y * Z for (X, Y, Z), _ in worlds)
+        assert 0 < c["processed_cell_steps"] < c["dense_cell_steps"]
+        for t, (dims, seed) in zip(tickets[:4], worlds):
+            assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n))
