@@ -299,9 +299,10 @@ __device__ __forceinline__ void bulk_store_wait(void* gdst, const void* smem_src
 
 // The rows of one world held in shared memory by the CTAs of a cluster: CTA
 // r holds rows y in [lo_r, hi_r) (lo_r even), stored as ((y - lo_r)*Z + z)*nw
-// + word, followed (at the next 16-byte boundary) by one flag byte per row:
-// the low 8 bits of the last step that changed the row.  `left` is the
-// shared memory of CTA r-1 (null for r == 0): the only row a CTA touches
+// + word, followed (at the next 16-byte boundary) by one flag byte per layer
+// y: the low 8 bits of the last step that changed a row of the layer, and a
+// list of up to (hi_r - lo_r)/2 + 2 16-bit layer-pair indices.  `left` is the
+// shared memory of CTA r-1 (null for r == 0): the only layer a CTA touches
 // outside its slab is y = lo_r - 1, in the odd phase.
 template <bool CL>
 struct SlabView {
@@ -314,46 +315,59 @@ struct SlabView {
         if (!CL || y >= lo) return mine + ((y - lo) * Z + z) * nw + g;
         return left + ((y - left_lo) * Z + z) * nw + g;
     }
-    __device__ __forceinline__ uint8_t* flag(int y, int z) const {
-        if (!CL || y >= lo) return fmine + (y - lo) * Z + z;
-        return fleft + (y - left_lo) * Z + z;
+    __device__ __forceinline__ uint8_t* flag(int y) const {
+        if (!CL || y >= lo) return fmine + (y - lo);
+        return fleft + (y - left_lo);
     }
 };
+
+// shared-memory bytes after a slab's planes: layer flags and the layer list
+__host__ __device__ __forceinline__ uint32_t slab_aux_bytes(uint32_t layers) {
+    return ((layers + 15u) & ~15u) + ((2u * (layers / 2u + 2u) + 15u) & ~15u);
+}
 
 // bytes of a slab's planes, rounded up so its row flags start 16-byte aligned
 __host__ __device__ __forceinline__ uint32_t slab_flag_offset(uint32_t plane_bytes) {
     return (plane_bytes + 15u) & ~15u;
 }
 
-// A block row-pair (j, k) of a world held in shared memory.  Every lane of
-// the warp calls this.  The pair is skipped when none of its rows changed in
-// the two previous steps: its cells are then those of its last evaluation in
-// the same phase, two steps back, which changed nothing, and whether a block
-// can change depends on its cells alone (the rule's activity mask), so it
-// would change nothing again.  The first two steps of a segment evaluate
-// every pair (the flags start at step t0 - 1).
+// Whether the block row-pairs of layer pair j (all k) must be evaluated: a
+// row of layer 2j - o or 2j - o + 1 changed in one of the two previous steps.
+// Otherwise every pair's cells are those of its last evaluation in the same
+// phase, two steps back, which changed nothing, and whether a block can
+// change depends on its cells alone (the rule's activity mask), so it would
+// change nothing again.  The first two steps of a segment evaluate every
+// pair (the flags start at step t0 - 1).
+template <bool CL>
+__device__ __forceinline__ bool layer_dirty(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t tt, int j) {
+    bool dirty = false;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int y = 2 * j - o + a;
+        if (y >= 0 && y < w.Y) dirty |= ((tt - (uint32_t)*v.flag(y)) & 0xFFu) <= 2u;
+    }
+    return dirty;
+}
+
+// Evaluates block row-pair (j, k) of a world held in shared memory when `run`
+// is set.  Every lane of the warp calls this together (the odd phase passes
+// carry bits between lanes).  Layers with a changed row get the step's flag;
+// the cells evaluated are added to *s_processed.
 template <bool CL>
 __device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk,
-                                             uint32_t tt, int j, int k, bool valid, int gl, int G,
+                                             uint32_t tt, int j, int k, bool run, int gl, int G,
                                              unsigned long long* s_processed) {
+    if (!__any_sync(0xFFFFFFFFu, run)) return;
     const int y0 = 2 * j - o, z0 = 2 * k - o;
-    bool in[4], dirty = false;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
-        in[a] = valid && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
-        if (in[a]) dirty |= ((tt - (uint32_t)*v.flag(y, z)) & 0xFFu) <= 2u;
-    }
-    if (!__any_sync(0xFFFFFFFFu, dirty)) return;
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
-    const bool has = dirty && gl < w.nw;
+    const bool has = run && gl < w.nw;
     uint4 q[4], q0[4];
     uint4* ptr[4];
     uint32_t rows_in = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
-        ptr[a] = (has && in[a]) ? v.at(y, z, gl) : nullptr;
+        ptr[a] = (has && y >= 0 && y < w.Y && z >= 0 && z < w.Z) ? v.at(y, z, gl) : nullptr;
         q[a] = ptr[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
         q0[a] = q[a];
         rows_in += ptr[a] ? 1u : 0u;
@@ -365,7 +379,7 @@ __device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneW
     for (int a = 0; a < 4; ++a)
         if (ptr[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w)) {
             *ptr[a] = q[a];
-            *v.flag((a < 2) ? y0 + 1 : y0, z0 + (a & 1)) = (uint8_t)tt;
+            *v.flag((a < 2) ? y0 + 1 : y0) = (uint8_t)tt;
         }
 }
 
@@ -414,7 +428,11 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
     const int lane = threadIdx.x & 31;
     uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
     __shared__ unsigned long long s_processed;  // cell-steps evaluated (the rest were skipped as settled)
-    if (threadIdx.x == 0) s_processed = 0;
+    __shared__ int s_count[2];                   // work-list length, by step parity
+    if (threadIdx.x == 0) {
+        s_processed = 0;
+        s_count[0] = s_count[1] = 0;
+    }
     for (;;) {
         // after an error every group stops taking worlds (and all of a cluster stop together)
         if (r == 0 && threadIdx.x == 0) item = *(volatile int*)err ? n : atomicAdd(counter, 1);
@@ -439,13 +457,8 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
                        : nullptr;
         uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
         if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
-        {
-            // every row counts as changed at step t0 - 1: the first two steps evaluate all pairs
-            const uint32_t f = ((uint32_t)(w.t - 1u) & 0xFFu) * 0x01010101u;
-            uint32_t* fw = reinterpret_cast<uint32_t*>(v.fmine);
-            const int nf = ((v.hi - v.lo) * w.Z + 3) / 4;
-            for (int i = threadIdx.x; i < nf; i += NT) fw[i] = f;
-        }
+        // every layer counts as changed at step t0 - 1: the first two steps evaluate all pairs
+        for (int i = threadIdx.x; i < v.hi - v.lo; i += NT) v.fmine[i] = (uint8_t)(w.t - 1u);
         bool ok = true;
         if (bytes) {
             ok = mbar_wait(&bar, phase);
@@ -460,6 +473,8 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
         group_sync();  // every slab is loaded before a neighbour reads it
         const int G = 1 << w.lg, per = NT >> w.lg;
         const int gl = lane & (G - 1);
+        // layer pairs to evaluate in a step (16-bit offsets from j_lo), after the flags
+        uint16_t* jlist = reinterpret_cast<uint16_t*>(v.fmine + (((v.hi - v.lo) + 15) & ~15));
         for (int s = 0; s < w.steps; ++s) {
             if (poisoned) {
                 group_sync();
@@ -470,13 +485,34 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
             const uint32_t sk = stepkey(w.seed, t);
             const int NBZ = nblocks(w.Z, o);
             const int j_lo = v.lo / 2, j_hi = (r == CS - 1) ? nblocks(w.Y, o) : v.hi / 2;
-            const int nrp = (j_hi - j_lo) * NBZ;
+            const int nj = j_hi - j_lo;
             const uint32_t tt = (uint32_t)t & 0xFFu;
-            for (int base = 0; base < nrp; base += per) {
-                const int rp = base + (int)(threadIdx.x >> w.lg);
-                const bool valid = rp < nrp;
-                const int jj = valid ? rp / NBZ : 0;
-                slab_rowpair(v, w, o, sk, tt, j_lo + jj, valid ? rp - jj * NBZ : 0, valid, gl, G, &s_processed);
+            int n_layers = nj;
+            const bool listed = s >= 2;  // the first two steps evaluate every layer pair
+            if (listed) {
+                int* cnt = &s_count[s & 1];
+                for (int base = 0; base < nj; base += NT) {
+                    const int i = base + (int)threadIdx.x;
+                    const bool add = i < nj && layer_dirty(v, w, o, tt, j_lo + i);
+                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, add);
+                    if (m) {
+                        int pos = 0;
+                        if (lane == __ffs(m) - 1) pos = atomicAdd(cnt, __popc(m));
+                        pos = __shfl_sync(0xFFFFFFFFu, pos, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1u));
+                        if (add) jlist[pos] = (uint16_t)i;
+                    }
+                }
+                __syncthreads();
+                n_layers = *cnt;
+            }
+            if (threadIdx.x == 0) s_count[(s + 1) & 1] = 0;  // the next step's counter (read before this step)
+            const int npairs = n_layers * NBZ;
+            for (int base = 0; base < npairs; base += per) {
+                const int e = base + (int)(threadIdx.x >> w.lg);
+                const bool valid = e < npairs;
+                const int jd = valid ? e / NBZ : 0, kk = valid ? e - jd * NBZ : 0;
+                const int jj = listed ? (valid ? (int)jlist[jd] : 0) : jd;
+                slab_rowpair(v, w, o, sk, tt, j_lo + jj, kk, valid, gl, G, &s_processed);
             }
             group_sync();
         }
@@ -554,8 +590,8 @@ int resident_class(int X, int Y, int Z) {
         // slab must be non-empty so the row below a slab is in its neighbour
         const int64_t nyp = (Y + 1) / 2;
         const int64_t mx = k.cs == 1 ? Y : 2 * ((nyp + k.cs - 1) / k.cs);
-        // planes, then one flag byte per row (padded to whole words)
-        const int64_t need = ((mx * row_bytes + 15) & ~(int64_t)15) + ((mx * Z + 15) & ~(int64_t)15);
+        // planes, then the layer flags and the layer list
+        const int64_t need = ((mx * row_bytes + 15) & ~(int64_t)15) + (int64_t)slab_aux_bytes((uint32_t)mx);
         if (need <= k.smem && (k.cs == 1 || nyp >= k.cs)) return c;
     }
     return -1;
