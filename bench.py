@@ -235,14 +235,19 @@ def run_fs3d(args):
     # ---- headline: batched pool, device-resident
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
-    total_steps = S * (args.warmup + args.steps + 1 + 32)
+    # untimed: warm-up segments (at least five, so the worlds are past their
+    # first 256 steps, the phase where everything still falls), then the
+    # launch configuration is chosen on real segments, then one more segment
+    pre = max(args.warmup, 5)
+    total_steps = S * (pre + 1 + args.steps + 1 + 32)
     tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
     bstream = torch.cuda.ExternalStream(b.stream())
-    # launch configuration chosen on real segments of this pool (outside the clock)
-    tune = b.autotune(trial_segments=1) if not args.no_autotune else {"segments": 0}
-    for _ in range(args.warmup):
+    for _ in range(pre):
         b.run_segment()
+    tune = b.autotune(trial_segments=1) if not args.no_autotune else {"segments": 0}
+    b.run_segment()
     b.sync()
+    untimed = pre + tune["segments"] + 1
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -282,7 +287,7 @@ def run_fs3d(args):
         for i in range(3):
             (X, Y, Z), seed = worlds[i]
             g = host[i].numpy().copy()
-            orc.run(g, seed, 0, S * (tune["segments"] + args.warmup + args.steps), nthreads=0)
+            orc.run(g, seed, 0, S * (untimed + args.steps), nthreads=0)
             got = b.retire(tickets[i], (Y, Z, X))
             ok &= bool((got == g).all())
         parity = "3 worlds bit-exact after the timed segments" if ok else "MISMATCH"
@@ -435,7 +440,8 @@ def run_fs3d(args):
                            "worlds_per_gpu": args.worlds, "cells_per_gpu": cells, "steps_per_segment": S,
                            "master_seed": args.master, "l2": "flushed between timed segments (512 MB write)",
                            "layout": "2-bit planes", "parallelism": f"replicas x{world}",
-                           "launch_config": {k: tune.get(k) for k in ("promote", "ctas_per_sm", "trials")}},
+                           "launch_config": {k: tune.get(k) for k in ("mode", "promote", "ctas_per_sm", "trials")},
+                           "untimed_segments": untimed},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(float(np.mean(e2e_ms)), 2),

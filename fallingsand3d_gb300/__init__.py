@@ -90,7 +90,7 @@ class WorldSpec(C.Structure):
 
 
 class TuneReport(C.Structure):
-    _fields_ = [("promote", C.c_int), ("ctas_per_sm", C.c_int), ("trials", C.c_int), ("cached", C.c_int),
+    _fields_ = [("mode", C.c_int), ("promote", C.c_int), ("ctas_per_sm", C.c_int), ("trials", C.c_int), ("cached", C.c_int),
                 ("segments", C.c_int), ("best_vox_per_ms", C.c_double), ("trial_vox_per_ms", C.c_double * 8)]
 
 
@@ -413,11 +413,15 @@ class Batch:
     """Pool of many worlds stepped together in graph-captured segments."""
 
     def __init__(self, budget_bytes: int, steps_per_segment: int = 64, use_graphs: bool = True,
-                 ctas_per_sm: int = 0, use_smem: bool = True):
+                 ctas_per_sm: int = 0, use_smem=None):
+        """use_smem: None = the library default; False/0 = per-step kernel only;
+        True/1 = shared-memory resident segments; 2 = global-memory segments;
+        3 = shared memory for a world's first 256 steps, then global memory."""
         cfg = lib().fs3d_default_config()
         cfg.steps_per_segment = steps_per_segment
         cfg.use_graphs = 1 if use_graphs else 0
-        cfg.use_smem = 1 if use_smem else 0
+        if use_smem is not None:
+            cfg.use_smem = int(use_smem)
         cfg.ctas_per_sm = ctas_per_sm
         h = vp()
         check(lib().fs3d_batch_create(budget_bytes, C.byref(cfg), C.byref(h)))
@@ -512,7 +516,7 @@ class Batch:
         """Times the launch configurations on real segments and keeps the best."""
         r = TuneReport()
         check(lib().fs3d_batch_autotune(self.handle, trial_segments, C.byref(r)))
-        return {"promote": r.promote, "ctas_per_sm": r.ctas_per_sm, "trials": r.trials, "cached": bool(r.cached),
+        return {"mode": r.mode, "promote": r.promote, "ctas_per_sm": r.ctas_per_sm, "trials": r.trials, "cached": bool(r.cached),
                 "segments": r.segments, "best_vox_per_ms": r.best_vox_per_ms, "trial_vox_per_ms": list(r.trial_vox_per_ms)[:r.trials]}
 
     def stats(self):

@@ -57,7 +57,7 @@ fs3d_config fs3d_default_config(void) {
     memset(&c, 0, sizeof(c));
     c.steps_per_segment = 64;
     c.use_graphs = 1;
-    c.use_smem = 1;
+    c.use_smem = 3;
     return c;
 }
 

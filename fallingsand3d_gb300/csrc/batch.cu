@@ -30,9 +30,12 @@ namespace {
 struct BWorld {
     int X = 0, Y = 0, Z = 0, nw = 0;
     uint64_t seed = 0, t = 0;
+    uint64_t t0 = 0;  // step at admission
     int64_t remaining = 0;
     uint4* rows = nullptr;
     uint8_t* statics = nullptr;
+    uint8_t* lflags = nullptr;  // layer flags after the planes (same allocation)
+    bool flags_valid = false;   // kept up to date by every segment that stepped the world
     size_t bytes = 0;
     bool done = false;
     cudaEvent_t ready = nullptr;     // admission finished (side stream)
@@ -86,13 +89,15 @@ struct fs3d_batch {
     PinnedArray<int> to;  // resident worlds (indices into tw) by class, largest first
     int* counter = nullptr;  // work counters of the resident kernels, one per class
     int* err = nullptr;      // set by a kernel whose bounded wait gave up
-    cudaEvent_t fork = nullptr, join[kResidentClasses + 1] = {};
-    cudaStream_t branch[kResidentClasses + 1] = {};  // capture branches of a segment
+    cudaEvent_t fork = nullptr, join[kAllClasses + 1] = {};
+    cudaStream_t branch[kAllClasses + 1] = {};  // capture branches of a segment: one per class, then the per-step chain
     cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
     cudaEvent_t last_segment = nullptr;
     std::vector<cudaEvent_t> pending_ready;  // admissions the next segment must wait for
-    cudaGraphExec_t graph = nullptr;
-    void* graph_worlds = nullptr;  // table pointers baked into the graph
+    // segment graphs without and with the per-step kernel's launches (the
+    // second only when some world is too large to be resident)
+    cudaGraphExec_t graph = nullptr, graph_steps = nullptr;
+    void* graph_worlds = nullptr;  // table pointers baked into the graphs
     void* graph_items = nullptr;
     void* graph_order = nullptr;
     int grid = 0;
@@ -105,6 +110,35 @@ struct fs3d_batch {
 };
 
 namespace {
+
+// Worlds younger than this (steps since admission) are still mostly moving:
+// the hybrid mode keeps them in shared memory, where dense steps are cheap.
+constexpr uint64_t kYoungSteps = 256;
+
+// Segment class of a running world (-1: the per-step kernel) under the
+// batch's mode: 1 shared-memory classes, 2 global-memory classes, 3 hybrid
+// (young worlds in shared memory when they fit, settled ones in global
+// memory), 0 none.  `promote` moves single-CTA worlds to wider classes.
+int segment_class(const fs3d_batch* b, const BWorld& w) {
+    const int mode = b->cfg.use_smem;
+    auto smem = [&]() {
+        int c = resident_class(w.X, w.Y, w.Z);
+        if (c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
+        return c;
+    };
+    auto gm = [&]() {
+        const int c = resident_class_gm(w.X, w.Y, w.Z);
+        return c < 0 ? -1 : kResidentClasses + std::min(c + b->promote, kGmClasses - 1);
+    };
+    if (mode == 1) return smem();
+    if (mode == 2) return gm();
+    if (mode == 3) {
+        const int first = (w.t - w.t0 < kYoungSteps) ? smem() : gm();
+        if (first >= 0) return first;
+        return (w.t - w.t0 < kYoungSteps) ? gm() : smem();
+    }
+    return -1;
+}
 
 fs3d_status wait_stream(cudaStream_t st, int64_t timeout_ns) {
     if (timeout_ns < 0) {
@@ -137,31 +171,36 @@ void free_world(fs3d_batch* b, BWorld& w) {
 // fit in shared memory take all their steps in one launch) and
 // steps_per_segment launches of the per-step kernel (the larger worlds).
 // With `fork` each goes to its own branch stream so they run concurrently.
-fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork) {
+fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_steps) {
     if (fork) {
         FS3D_CUDA(cudaEventRecord(b->fork, a));
         for (cudaStream_t br : b->branch) FS3D_CUDA(cudaStreamWaitEvent(br, b->fork, 0));
     }
     fs3d_status s = FS3D_OK;
-    if (b->cfg.use_smem)
+    const int mode = b->cfg.use_smem;
+    if (mode == 1 || mode == 3)
         for (int c = 0; c < kResidentClasses && s == FS3D_OK; ++c)
             s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
                                               fork ? b->branch[c] : a, b->processed_dev);
-    for (int k = 0; k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
-        s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, fork ? b->branch[kResidentClasses] : a);
+    if (mode == 2 || mode == 3)
+        for (int c = 0; c < kGmClasses && s == FS3D_OK; ++c)
+            s = launch_plane_segment_gm(c, b->tw.d, b->to.d, b->tn.d, b->counter + kResidentClasses + c, b->err,
+                                        fork ? b->branch[kResidentClasses + c] : a, b->processed_dev);
+    for (int k = 0; with_steps && k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
+        s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, fork ? b->branch[kAllClasses] : a);
     if (s != FS3D_OK) return s;
     if (fork)
-        for (int c = 0; c <= kResidentClasses; ++c) {
+        for (int c = 0; c <= kAllClasses; ++c) {
             FS3D_CUDA(cudaEventRecord(b->join[c], b->branch[c]));
             FS3D_CUDA(cudaStreamWaitEvent(a, b->join[c], 0));
         }
     return FS3D_OK;
 }
 
-fs3d_status capture_graph(fs3d_batch* b) {
-    if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
+fs3d_status capture_one(fs3d_batch* b, bool with_steps, cudaGraphExec_t* out) {
+    if (*out) {
+        cudaGraphExecDestroy(*out);
+        *out = nullptr;
     }
     cudaStream_t cs;
     FS3D_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -169,14 +208,21 @@ fs3d_status capture_graph(fs3d_batch* b) {
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        s = enqueue_segment(b, cs, true);
+        s = enqueue_segment(b, cs, true, with_steps);
         e = cudaStreamEndCapture(cs, &g);
     }
-    if (e == cudaSuccess && s == FS3D_OK) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (e == cudaSuccess && s == FS3D_OK) e = cudaGraphInstantiate(out, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
     if (s != FS3D_OK) return s;
     if (e != cudaSuccess) return cuda_fail(e, "segment graph capture");
+    return FS3D_OK;
+}
+
+fs3d_status capture_graph(fs3d_batch* b) {
+    fs3d_status s = capture_one(b, false, &b->graph);
+    if (s == FS3D_OK) s = capture_one(b, true, &b->graph_steps);
+    if (s != FS3D_OK) return s;
     b->graph_worlds = b->tw.d;
     b->graph_items = b->ti.d;
     b->graph_order = b->to.d;
@@ -205,11 +251,11 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->processed_dev, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->processed_dev, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int) * kResidentClasses);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int) * kAllClasses);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    for (int c = 0; c <= kResidentClasses && e == cudaSuccess; ++c) {
+    for (int c = 0; c <= kAllClasses && e == cudaSuccess; ++c) {
         e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->branch[c], cudaStreamNonBlocking);
     }
@@ -223,7 +269,7 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
         }
     }
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_create");
-    if (s == FS3D_OK) s = b->tn.reserve(1 + 2 * kResidentClasses);
+    if (s == FS3D_OK) s = b->tn.reserve(kMetaInts);
     // size the tables for a few thousand worlds and capture the segment graph
     // now, so the first segments of a run (or a server) pay neither a pinned
     // allocation nor a capture
@@ -273,13 +319,15 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     w.nw = plane_nw(X);
     w.seed = seed;
     w.t = start_step;
+    w.t0 = start_step;
     w.remaining = n_steps;
     w.done = n_steps == 0;
-    w.bytes = plane_bytes(X, Y, Z) + (stat ? n : 0) + sizeof(PlaneWorld);
+    w.bytes = plane_bytes(X, Y, Z) + layer_flag_bytes(Y) + (stat ? n : 0) + sizeof(PlaneWorld);
     if (b->used + w.bytes > b->budget)
         return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
     uint8_t* staging = nullptr;
-    FS3D_CUDA(cudaMallocAsync((void**)&w.rows, plane_bytes(X, Y, Z), b->side));
+    FS3D_CUDA(cudaMallocAsync((void**)&w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
+    w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(X, Y, Z);
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaSuccess;
     if (g) {
@@ -337,8 +385,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
-        int c = b->cfg.use_smem ? resident_class(w.X, w.Y, w.Z) : -1;
-        if (c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
+        const int c = segment_class(b, w);
         run.emplace_back(c, &w);
         if (c >= 0)
             ++ns;
@@ -353,7 +400,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     if (s == FS3D_OK) s = b->ti.reserve(ni > 0 ? ni : 1);
     if (s == FS3D_OK) s = b->to.reserve(ns > 0 ? ns : 1);
     if (s != FS3D_OK) return s;
-    std::vector<int> by_class[kResidentClasses];
+    std::vector<int> by_class[kAllClasses];
     size_t ii = 0;
     for (size_t wi = 0; wi < nw_; ++wi) {
         const BWorld& w = *run[wi].second;
@@ -369,6 +416,15 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         d.nw = w.nw;
         d.steps = steps;
         d.lg = plane_lg(w.nw);
+        // resident segments keep the layer flags; the per-step kernel does not
+        BWorld& wm = *run[wi].second;
+        if (run[wi].first >= 0) {
+            d.lflags = wm.lflags;
+            d.lflags_fresh = wm.flags_valid ? 0 : 1;
+            wm.flags_valid = wm.lflags != nullptr;
+        } else {
+            wm.flags_valid = false;
+        }
         const uint64_t cs = (uint64_t)w.X * w.Y * w.Z * (uint64_t)steps;
         b->dense_cell_steps += cs;
         if (run[wi].first < 0) b->stepped_cell_steps += cs;
@@ -383,7 +439,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     int* meta = b->tn.h;
     meta[0] = (int)ii;
     size_t si = 0;
-    for (int c = 0; c < kResidentClasses; ++c) {
+    for (int c = 0; c < kAllClasses; ++c) {
         std::vector<int>& v = by_class[c];
         std::sort(v.begin(), v.end(), [&](int x, int y) {
             const PlaneWorld &a = b->tw.h[x], &e2 = b->tw.h[y];
@@ -391,7 +447,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
             return ca != cc ? ca > cc : x < y;
         });
         meta[1 + c] = (int)v.size();
-        meta[1 + kResidentClasses + c] = (int)si;
+        meta[1 + kAllClasses + c] = (int)si;
         for (int x : v) b->to.h[si++] = x;
     }
     // admissions complete before the segment reads their planes
@@ -409,7 +465,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * nw_, cudaMemcpyHostToDevice, b->stream));
     if (ii) FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
     if (si) FS3D_CUDA(cudaMemcpyAsync(b->to.d, b->to.h, sizeof(int) * si, cudaMemcpyHostToDevice, b->stream));
-    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * (1 + 2 * kResidentClasses), cudaMemcpyHostToDevice,
+    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * kMetaInts, cudaMemcpyHostToDevice,
                               b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
     if (b->cfg.use_graphs) {
@@ -417,10 +473,12 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
             s = capture_graph(b);
             if (s != FS3D_OK) return s;
         }
-        FS3D_CUDA(cudaGraphLaunch(b->graph, b->stream));
-        note_launch((uint64_t)S + (b->cfg.use_smem ? kResidentClasses : 0));
+        FS3D_CUDA(cudaGraphLaunch(ii ? b->graph_steps : b->graph, b->stream));
+        note_launch((ii ? (uint64_t)S : 0u) +
+                    (b->cfg.use_smem == 1 || b->cfg.use_smem == 3 ? kResidentClasses : 0) +
+                    (b->cfg.use_smem == 2 || b->cfg.use_smem == 3 ? kGmClasses : 0));
     } else {
-        s = enqueue_segment(b, b->stream, false);
+        s = enqueue_segment(b, b->stream, false, ii > 0);
         if (s != FS3D_OK) return s;
     }
     FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
@@ -525,7 +583,7 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         if (!p.grid || p.X <= 0 || p.Y <= 0 || p.Z <= 0 || p.X > kPlaneMaxX || p.Y > 65536 || p.Z > 65536 ||
             p.n_steps < 0)
             return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: bad world spec");
-        const size_t need = plane_bytes(p.X, p.Y, p.Z) + sizeof(PlaneWorld);
+        const size_t need = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld);
         if (used + need > b->budget) break;
         used += need;
     }
@@ -557,7 +615,7 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     if (e == cudaSuccess) e = cudaMallocAsync(&table, flags_off + sizeof(int) * (size_t)k, b->side);
     for (int a = 0; a < k && e == cudaSuccess; ++a) {
         const fs3d_world_spec& p = specs[a];
-        e = cudaMallocAsync((void**)&rows[(size_t)a], plane_bytes(p.X, p.Y, p.Z), b->side);
+        e = cudaMallocAsync((void**)&rows[(size_t)a], plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y), b->side);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, p.grid, (size_t)p.X * p.Y * p.Z,
                                 cudaMemcpyHostToDevice, b->side);
@@ -610,11 +668,13 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         w.nw = plane_nw(p.X);
         w.seed = p.seed;
         w.t = p.start_step;
+        w.t0 = p.start_step;
         w.remaining = p.n_steps;
         w.done = p.n_steps == 0;
         w.rows = rows[(size_t)a];
+        w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(p.X, p.Y, p.Z);
         w.statics = statics[(size_t)a];
-        w.bytes = plane_bytes(p.X, p.Y, p.Z) + sizeof(PlaneWorld) +
+        w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld) +
                   (w.statics ? (size_t)p.X * p.Y * p.Z : 0);
         b->used += w.bytes;
         tickets[a] = b->next_ticket++;
@@ -709,7 +769,13 @@ namespace {
 // tuned choices per batch shape: the count of live worlds per resident class
 // (and of worlds too large to be resident), so a batch of the same make-up
 // starts from the measured best
-std::map<std::vector<int>, std::pair<int, int>> g_tuned;
+struct Tuning {
+    int mode, promote, ctas_per_sm;
+    bool operator==(const Tuning& o) const {
+        return mode == o.mode && promote == o.promote && ctas_per_sm == o.ctas_per_sm;
+    }
+};
+std::map<std::vector<int>, Tuning> g_tuned;
 std::mutex g_tuned_mu;
 
 std::vector<int> batch_shape(const fs3d_batch* b) {
@@ -724,10 +790,11 @@ std::vector<int> batch_shape(const fs3d_batch* b) {
 
 // applies a launch configuration; the segment graph (which bakes in the
 // per-step kernel's grid) is re-captured once the stream is idle
-fs3d_status apply_tuning(fs3d_batch* b, int promote, int ctas_per_sm) {
+fs3d_status apply_tuning(fs3d_batch* b, const Tuning& t) {
     FS3D_CUDA(cudaStreamSynchronize(b->stream));
-    b->promote = promote;
-    b->grid = sm_count_public() * ctas_per_sm;
+    b->cfg.use_smem = t.mode;
+    b->promote = t.promote;
+    b->grid = sm_count_public() * t.ctas_per_sm;
     return b->cfg.use_graphs ? capture_graph(b) : FS3D_OK;
 }
 
@@ -751,34 +818,52 @@ fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_rep
     if (!b || trial_segments <= 0) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_autotune: bad args");
     if (out) memset(out, 0, sizeof(*out));
     const std::vector<int> shape = batch_shape(b);
+    auto report = [&](const Tuning& t) {
+        if (!out) return;
+        out->mode = t.mode;
+        out->promote = t.promote;
+        out->ctas_per_sm = t.ctas_per_sm;
+    };
     {
         std::lock_guard<std::mutex> lock(g_tuned_mu);
         auto it = g_tuned.find(shape);
         if (it != g_tuned.end()) {
-            const fs3d_status s = apply_tuning(b, it->second.first, it->second.second);
+            const fs3d_status s = apply_tuning(b, it->second);
             if (s != FS3D_OK) return s;
-            if (out) {
-                out->promote = b->promote;
-                out->ctas_per_sm = it->second.second;
-                out->cached = 1;
-            }
+            report(it->second);
+            if (out) out->cached = 1;
             return FS3D_OK;
         }
     }
+    // candidates: resident kernels in global or shared memory (when resident
+    // segments are on), two class promotions, and the per-step kernel's grid
+    // only when some world is too large to be resident in both
     const int resident = plane_step_ctas_per_sm();
-    std::vector<std::pair<int, int>> cand;
-    for (int p = 0; p < kSingleCtaClasses; ++p)
-        for (int cps : {resident, resident > 1 ? resident / 2 : resident})
-            if (std::find(cand.begin(), cand.end(), std::make_pair(p, cps)) == cand.end()) cand.emplace_back(p, cps);
+    bool stepped = false;
+    for (auto& kv : b->worlds)
+        if (!kv.second.done && resident_class(kv.second.X, kv.second.Y, kv.second.Z) < 0 &&
+            resident_class_gm(kv.second.X, kv.second.Y, kv.second.Z) < 0)
+            stepped = true;
+    // the hybrid mode picks a world's memory by its age itself; an explicit
+    // mode 1 or 2 is tuned between the two
+    std::vector<Tuning> cand;
+    const int m0 = b->cfg.use_smem;
+    const std::vector<int> modes = m0 == 3 ? std::vector<int>{3} : (m0 ? std::vector<int>{2, 1} : std::vector<int>{0});
+    for (int m : modes)
+        for (int p = 0; p < (m ? 2 : 1); ++p)
+            for (int cps : {resident, resident > 1 ? resident / 2 : resident}) {
+                const Tuning t{m, p, (stepped || m == 0) ? cps : resident};
+                if (std::find(cand.begin(), cand.end(), t) == cand.end()) cand.push_back(t);
+            }
     cudaEvent_t e0, e1;
     FS3D_CUDA(cudaEventCreate(&e0));
     FS3D_CUDA(cudaEventCreate(&e1));
     double best_rate = -1.0;
-    std::pair<int, int> best = {b->promote, b->grid / sm_count_public()};
+    Tuning best{b->cfg.use_smem, b->promote, b->grid / sm_count_public()};
     fs3d_status s = FS3D_OK;
     int trials = 0, segments = 0;
     for (size_t ci = 0; ci < cand.size() && s == FS3D_OK; ++ci) {
-        s = apply_tuning(b, cand[ci].first, cand[ci].second);
+        s = apply_tuning(b, cand[ci]);
         double rate = 0.0;
         for (int r = 0; r < trial_segments + 1 && s == FS3D_OK; ++r) {
             const double work = segment_work(b);
@@ -801,16 +886,15 @@ fs3d_status fs3d_batch_autotune(fs3d_batch* b, int trial_segments, fs3d_tune_rep
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const fs3d_status sa = apply_tuning(b, best.first, best.second);
+    const fs3d_status sa = apply_tuning(b, best);
     if (s != FS3D_OK) return s;
     if (sa != FS3D_OK) return sa;
     if (best_rate > 0.0) {
         std::lock_guard<std::mutex> lock(g_tuned_mu);
         g_tuned[shape] = best;
     }
+    report(best);
     if (out) {
-        out->promote = best.first;
-        out->ctas_per_sm = best.second;
         out->trials = trials;
         out->segments = segments;
         out->best_vox_per_ms = best_rate;
@@ -856,6 +940,7 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     b->pending_ready.clear();
     if (b->side) cudaStreamSynchronize(b->side);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph_steps) cudaGraphExecDestroy(b->graph_steps);
     b->tw.release();
     b->ti.release();
     b->tn.release();
@@ -865,7 +950,7 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     cudaFree(b->err);
     cudaFree(b->processed_dev);
     if (b->fork) cudaEventDestroy(b->fork);
-    for (int c = 0; c <= kResidentClasses; ++c) {
+    for (int c = 0; c <= kAllClasses; ++c) {
         if (b->join[c]) cudaEventDestroy(b->join[c]);
         if (b->branch[c]) cudaStreamDestroy(b->branch[c]);
     }

@@ -299,11 +299,13 @@ __device__ __forceinline__ void bulk_store_wait(void* gdst, const void* smem_src
 
 // The rows of one world held in shared memory by the CTAs of a cluster: CTA
 // r holds rows y in [lo_r, hi_r) (lo_r even), stored as ((y - lo_r)*Z + z)*nw
-// + word, followed (at the next 16-byte boundary) by one flag byte per layer
-// y: the low 8 bits of the last step that changed a row of the layer, and a
-// list of up to (hi_r - lo_r)/2 + 2 16-bit layer-pair indices.  `left` is the
-// shared memory of CTA r-1 (null for r == 0): the only layer a CTA touches
-// outside its slab is y = lo_r - 1, in the odd phase.
+// + word, followed (at the next 16-byte boundary) by four change buffers of
+// one byte per layer y (buffer t & 3: 1 if step t changed a row of the
+// layer) and a list of up to (hi_r - lo_r)/2 + 2 16-bit layer-pair indices.
+// Step t writes buffer t & 3, reads buffers (t-1) & 3 and (t-2) & 3 and
+// clears buffer (t+1) & 3, so no buffer is both read and written in a step.
+// `left` is the shared memory of CTA r-1 (null for r == 0): the only layer a
+// CTA touches outside its slab is y = lo_r - 1, in the odd phase.
 template <bool CL>
 struct SlabView {
     uint4* mine;
@@ -315,15 +317,29 @@ struct SlabView {
         if (!CL || y >= lo) return mine + ((y - lo) * Z + z) * nw + g;
         return left + ((y - left_lo) * Z + z) * nw + g;
     }
-    __device__ __forceinline__ uint8_t* flag(int y) const {
-        if (!CL || y >= lo) return fmine + (y - lo);
-        return fleft + (y - left_lo);
+    __device__ __forceinline__ uint8_t* flag(int y, uint32_t b) const {
+        if (!CL || y >= lo) return fmine + b * flag_stride(hi - lo) + (y - lo);
+        return fleft + b * flag_stride(lo - left_lo) + (y - left_lo);
     }
+    __host__ __device__ static __forceinline__ uint32_t flag_stride(int layers) { return ((uint32_t)layers + 15u) & ~15u; }
 };
 
-// shared-memory bytes after a slab's planes: layer flags and the layer list
+// shared-memory bytes after a slab's planes: change buffers and the layer list
 __host__ __device__ __forceinline__ uint32_t slab_aux_bytes(uint32_t layers) {
-    return ((layers + 15u) & ~15u) + ((2u * (layers / 2u + 2u) + 15u) & ~15u);
+    return 4u * ((layers + 15u) & ~15u) + ((2u * (layers / 2u + 2u) + 15u) & ~15u);
+}
+
+// index of the n-th (from 0) set bit of m; m has more than n set bits
+__device__ __forceinline__ int select_bit(uint32_t m, int n) {
+    int pos = 0, c = __popc(m & 0xFFFFu);
+    if (n >= c) { n -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xFFu);
+    if (n >= c) { n -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xFu);
+    if (n >= c) { n -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (n >= c) { n -= c; m >>= 2; pos += 2; }
+    return pos + (n >= (int)(m & 1u) ? 1 : 0);
 }
 
 // bytes of a slab's planes, rounded up so its row flags start 16-byte aligned
@@ -336,17 +352,17 @@ __host__ __device__ __forceinline__ uint32_t slab_flag_offset(uint32_t plane_byt
 // Otherwise every pair's cells are those of its last evaluation in the same
 // phase, two steps back, which changed nothing, and whether a block can
 // change depends on its cells alone (the rule's activity mask), so it would
-// change nothing again.  The first two steps of a segment evaluate every
-// pair (the flags start at step t0 - 1).
+// change nothing again.  A world without kept flags starts with every layer
+// changed at steps t0 - 1 and t0 - 2.
 template <bool CL>
-__device__ __forceinline__ bool layer_dirty(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t tt, int j) {
-    bool dirty = false;
+__device__ __forceinline__ bool layer_dirty(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t tb, int j) {
+    uint32_t dirty = 0;
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
         const int y = 2 * j - o + a;
-        if (y >= 0 && y < w.Y) dirty |= ((tt - (uint32_t)*v.flag(y)) & 0xFFu) <= 2u;
+        if (y >= 0 && y < w.Y) dirty |= (uint32_t)*v.flag(y, (tb + 3u) & 3u) | (uint32_t)*v.flag(y, (tb + 2u) & 3u);
     }
-    return dirty;
+    return dirty != 0;
 }
 
 // Evaluates block row-pair (j, k) of a world held in shared memory when `run`
@@ -355,8 +371,8 @@ __device__ __forceinline__ bool layer_dirty(const SlabView<CL>& v, const PlaneWo
 // the cells evaluated are added to *s_processed.
 template <bool CL>
 __device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk,
-                                             uint32_t tt, int j, int k, bool run, int gl, int G,
-                                             unsigned long long* s_processed) {
+                                             uint32_t tt /* step & 3 */, int j, int k, bool run, int gl,
+                                             int G, unsigned long long* s_processed) {
     if (!__any_sync(0xFFFFFFFFu, run)) return;
     const int y0 = 2 * j - o, z0 = 2 * k - o;
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
@@ -379,7 +395,7 @@ __device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneW
     for (int a = 0; a < 4; ++a)
         if (ptr[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w)) {
             *ptr[a] = q[a];
-            *v.flag((a < 2) ? y0 + 1 : y0) = (uint8_t)tt;
+            *v.flag((a < 2) ? y0 + 1 : y0, tt) = 1u;
         }
 }
 
@@ -394,7 +410,7 @@ __device__ __forceinline__ int slab_lo(int Y, int r, int CS) { return 2 * ((r * 
 // the one row a CTA reads from its neighbour travels through distributed
 // shared memory), and each CTA writes its slab back with one TMA bulk store.
 // Worlds are independent, so groups never wait on one another.
-// meta: [0] per-step items, [1 + c] resident worlds of class c, [1 + kResidentClasses + c] their offset in order[].
+// meta: [0] per-step items, [1 + c] resident worlds of class c, [1 + kAllClasses + c] their offset in order[].
 // CTAs of each single-CTA class that share an SM (the register cap that lets
 // them: 24 warps of at most 80 registers per SM)
 template <int NT>
@@ -402,8 +418,11 @@ constexpr int resident_ctas_per_sm() {
     return NT == 128 ? 6 : (NT == 256 ? 3 : 1);
 }
 
-template <int NT, bool CL>
-__global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
+// GM: the world stays in global memory (L2) and the CTA keeps only the layer
+// flags and list in shared memory, so as many worlds are in flight as warps
+// allow; no bulk copies.  CTAs per SM of a GM kernel: 24 warps in all.
+template <int NT, bool CL, bool GM = false>
+__global__ void __launch_bounds__(NT, CL ? 1 : (GM ? 768 / NT : resident_ctas_per_sm<NT>()))
     k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
                                                              const int* __restrict__ order,
                                                              const int* __restrict__ meta, int cls, int CS,
@@ -413,7 +432,7 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
     __shared__ __align__(8) uint64_t bar;
     __shared__ int item;
     namespace cg = cooperative_groups;
-    const int n = meta[1 + cls], off = meta[1 + kResidentClasses + cls];
+    const int n = meta[1 + cls], off = meta[1 + kAllClasses + cls];
     if (!CL) CS = 1;
     const int r = CL ? (int)cg::this_cluster().block_rank() : 0;
     auto group_sync = [&]() {
@@ -446,19 +465,30 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
         v.lo = slab_lo(w.Y, r, CS);
         v.hi = r == CS - 1 ? w.Y : slab_lo(w.Y, r + 1, CS);
         v.left_lo = r > 0 ? slab_lo(w.Y, r - 1, CS) : 0;
-        v.mine = srows;
+        const uint32_t row_bytes = (uint32_t)w.Z * (uint32_t)w.nw * 16u;
+        const uint32_t bytes = GM ? 0u : (uint32_t)(v.hi - v.lo) * row_bytes;  // bulk-copied bytes
+        uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
+        v.mine = GM ? gslab : srows;
         v.left = left;
         v.Z = w.Z;
         v.nw = w.nw;
-        const uint32_t row_bytes = (uint32_t)w.Z * (uint32_t)w.nw * 16u;
-        const uint32_t bytes = (uint32_t)(v.hi - v.lo) * row_bytes;
         v.fmine = reinterpret_cast<uint8_t*>(srows) + slab_flag_offset(bytes);
         v.fleft = left ? reinterpret_cast<uint8_t*>(left) + slab_flag_offset((uint32_t)(v.lo - v.left_lo) * row_bytes)
                        : nullptr;
-        uint4* gslab = w.rows + (int64_t)v.lo * w.Z * w.nw;
         if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
-        // every layer counts as changed at step t0 - 1: the first two steps evaluate all pairs
-        for (int i = threadIdx.x; i < v.hi - v.lo; i += NT) v.fmine[i] = (uint8_t)(w.t - 1u);
+        // change buffers from the kept flags (the low 8 bits of the last step
+        // that changed the layer), or every layer changed at t0 - 1 and t0 - 2
+        {
+            const bool kept = w.lflags != nullptr && !w.lflags_fresh;
+            const uint32_t t0b = (uint32_t)w.t & 3u, fs = SlabView<CL>::flag_stride(v.hi - v.lo);
+            for (int i = threadIdx.x; i < v.hi - v.lo; i += NT) {
+                const uint32_t age = kept ? (((uint32_t)w.t - (uint32_t)w.lflags[v.lo + i]) & 0xFFu) : 0u;
+                v.fmine[((t0b + 3u) & 3u) * fs + i] = kept ? (age == 1u) : 1u;
+                v.fmine[((t0b + 2u) & 3u) * fs + i] = kept ? (age == 2u) : 1u;
+                v.fmine[t0b * fs + i] = 0u;
+                v.fmine[((t0b + 1u) & 3u) * fs + i] = 0u;
+            }
+        }
         bool ok = true;
         if (bytes) {
             ok = mbar_wait(&bar, phase);
@@ -473,8 +503,9 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
         group_sync();  // every slab is loaded before a neighbour reads it
         const int G = 1 << w.lg, per = NT >> w.lg;
         const int gl = lane & (G - 1);
-        // layer pairs to evaluate in a step (16-bit offsets from j_lo), after the flags
-        uint16_t* jlist = reinterpret_cast<uint16_t*>(v.fmine + (((v.hi - v.lo) + 15) & ~15));
+        // layer pairs to evaluate in a step (16-bit offsets from j_lo), after the buffers
+        const uint32_t fs = SlabView<CL>::flag_stride(v.hi - v.lo);
+        uint16_t* jlist = reinterpret_cast<uint16_t*>(v.fmine + 4u * fs);
         for (int s = 0; s < w.steps; ++s) {
             if (poisoned) {
                 group_sync();
@@ -486,14 +517,25 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
             const int NBZ = nblocks(w.Z, o);
             const int j_lo = v.lo / 2, j_hi = (r == CS - 1) ? nblocks(w.Y, o) : v.hi / 2;
             const int nj = j_hi - j_lo;
-            const uint32_t tt = (uint32_t)t & 0xFFu;
-            int n_layers = nj;
-            const bool listed = s >= 2;  // the first two steps evaluate every layer pair
-            if (listed) {
+            const uint32_t tb = (uint32_t)t & 3u;
+            // the buffer the next step writes: read and written by no one in this step
+            for (int i = threadIdx.x; i < v.hi - v.lo; i += NT) v.fmine[((tb + 1u) & 3u) * fs + i] = 0u;
+            // dirty layer pairs: up to 96 as bit masks every warp computes for
+            // itself (the buffers it reads are not written in this step), more
+            // through the shared list
+            uint32_t dm0 = 0, dm1 = 0, dm2 = 0;
+            int n_layers;
+            const bool masked = nj <= 96;
+            if (masked) {
+                dm0 = __ballot_sync(0xFFFFFFFFu, lane < nj && layer_dirty(v, w, o, tb, j_lo + lane));
+                if (nj > 32) dm1 = __ballot_sync(0xFFFFFFFFu, lane + 32 < nj && layer_dirty(v, w, o, tb, j_lo + 32 + lane));
+                if (nj > 64) dm2 = __ballot_sync(0xFFFFFFFFu, lane + 64 < nj && layer_dirty(v, w, o, tb, j_lo + 64 + lane));
+                n_layers = __popc(dm0) + __popc(dm1) + __popc(dm2);
+            } else {
                 int* cnt = &s_count[s & 1];
                 for (int base = 0; base < nj; base += NT) {
                     const int i = base + (int)threadIdx.x;
-                    const bool add = i < nj && layer_dirty(v, w, o, tt, j_lo + i);
+                    const bool add = i < nj && layer_dirty(v, w, o, tb, j_lo + i);
                     const uint32_t m = __ballot_sync(0xFFFFFFFFu, add);
                     if (m) {
                         int pos = 0;
@@ -511,10 +553,27 @@ __global__ void __launch_bounds__(NT, CL ? 1 : resident_ctas_per_sm<NT>())
                 const int e = base + (int)(threadIdx.x >> w.lg);
                 const bool valid = e < npairs;
                 const int jd = valid ? e / NBZ : 0, kk = valid ? e - jd * NBZ : 0;
-                const int jj = listed ? (valid ? (int)jlist[jd] : 0) : jd;
-                slab_rowpair(v, w, o, sk, tt, j_lo + jj, kk, valid, gl, G, &s_processed);
+                int jj = 0;
+                if (valid) {
+                    if (!masked)
+                        jj = (int)jlist[jd];
+                    else if (jd < __popc(dm0))
+                        jj = select_bit(dm0, jd);
+                    else if (jd < __popc(dm0) + __popc(dm1))
+                        jj = 32 + select_bit(dm1, jd - __popc(dm0));
+                    else
+                        jj = 64 + select_bit(dm2, jd - __popc(dm0) - __popc(dm1));
+                }
+                slab_rowpair(v, w, o, sk, tb, j_lo + jj, kk, valid, gl, G, &s_processed);
             }
             group_sync();
+        }
+        if (w.lflags && !poisoned) {
+            // kept for the next segment: the last of the final two steps that changed the layer
+            const uint64_t te = w.t + (uint64_t)w.steps;
+            const uint32_t b1 = (uint32_t)(te - 1u) & 3u, b2 = (uint32_t)(te - 2u) & 3u;
+            for (int i = threadIdx.x; i < v.hi - v.lo; i += NT)
+                w.lflags[v.lo + i] = (uint8_t)(v.fmine[b1 * fs + i] ? te - 1u : (v.fmine[b2 * fs + i] ? te - 2u : te - 3u));
         }
         // make the threads' shared-memory writes visible to the bulk copy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -595,6 +654,67 @@ int resident_class(int X, int Y, int Z) {
         if (need <= k.smem && (k.cs == 1 || nyp >= k.cs)) return c;
     }
     return -1;
+}
+
+// ---- global-memory segment classes: one CTA per world; the planes stay in
+// global memory (L2-resident for a batch of a few hundred MB) and shared
+// memory holds only the change buffers and the layer list.  A step's work is
+// the dirty layer pairs (a few per step: the moving surface), each of
+// ceil(Z/2) block row-pairs times the lanes per pair, so the CTA is sized by
+// that layer work, not by the world's volume: idle warps would wait at every
+// step's barrier.  Each class caps the layers it holds flags for so that its
+// CTAs per SM (24 warps in all) fit in shared memory.
+namespace {
+constexpr int kGmThreads[kGmClasses] = {32, 64, 128, 256};
+constexpr int kGmMaxY[kGmClasses] = {1024, 1024, 2048, 4096};
+bool g_gm_ready = false;
+}  // namespace
+
+int resident_class_gm(int X, int Y, int Z) {
+    const int lanes = nblocks(Z, 1) << plane_lg(plane_nw(X));  // lane tasks of one layer pair
+    int c = lanes <= 16 ? 0 : (lanes <= 48 ? 1 : (lanes <= 96 ? 2 : 3));
+    while (c < kGmClasses && Y > kGmMaxY[c]) ++c;
+    return c < kGmClasses ? c : -1;
+}
+
+template <int NT>
+static cudaError_t launch_gm(int cls, int grid, size_t smem, cudaStream_t st, const PlaneWorld* worlds,
+                             const int* order, const int* meta, int* counter, int* err,
+                             unsigned long long* processed_cells) {
+    k_plane_segment_resident<NT, false, true>
+        <<<grid, NT, smem, st>>>(worlds, order, meta, kResidentClasses + cls, 1, counter, err, processed_cells);
+    return cudaGetLastError();
+}
+
+fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
+                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells) {
+    if (cls < 0 || cls >= kGmClasses) return set_error(FS3D_ERR_INVALID_ARG, "global-memory class out of range");
+    if (!g_gm_ready) {
+        // the planes are read through L1: leave most of the unified memory to it
+        const void* fns[kGmClasses] = {reinterpret_cast<const void*>(&k_plane_segment_resident<32, false, true>),
+                                       reinterpret_cast<const void*>(&k_plane_segment_resident<64, false, true>),
+                                       reinterpret_cast<const void*>(&k_plane_segment_resident<128, false, true>),
+                                       reinterpret_cast<const void*>(&k_plane_segment_resident<256, false, true>)};
+        for (const void* fn : fns) cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
+        cudaGetLastError();
+        g_gm_ready = true;
+    }
+    FS3D_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    const int nt = kGmThreads[cls];
+    const int grid = sm_count_public() * (768 / nt);
+    const size_t smem = slab_aux_bytes((uint32_t)kGmMaxY[cls]);
+    cudaError_t e;
+    if (nt == 32)
+        e = launch_gm<32>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+    else if (nt == 64)
+        e = launch_gm<64>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+    else if (nt == 128)
+        e = launch_gm<128>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+    else
+        e = launch_gm<256>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+    if (e != cudaSuccess) return cuda_fail(e, "global-memory segment launch");
+    note_launch();
+    return FS3D_OK;
 }
 
 int smem_world_limit() {

@@ -16,7 +16,9 @@ struct PlaneWorld {
     int32_t X, Y, Z, nw;
     int32_t steps;    // steps this world takes in the current segment
     int32_t lg;       // log2 of the lane-group size (pow2ceil(nw))
-    int32_t pad[4];
+    uint8_t* lflags;       // nullable: per-layer last-changed step (low 8 bits), kept across segments
+    int32_t lflags_fresh;  // 1: lflags hold nothing yet (start from "every layer changed")
+    int32_t pad;
 };
 static_assert(sizeof(PlaneWorld) == 64, "PlaneWorld layout");
 
@@ -28,6 +30,8 @@ struct PlaneItem {
 
 inline int plane_nw(int X) { return (X + 63) / 64; }
 inline size_t plane_bytes(int X, int Y, int Z) { return (size_t)Y * Z * plane_nw(X) * sizeof(uint4); }
+// layer flags stored after a world's planes in the same allocation
+inline size_t layer_flag_bytes(int Y) { return ((size_t)Y + 15) & ~(size_t)15; }
 constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 
 // Resident segment classes: worlds whose planes fit in shared memory take
@@ -36,6 +40,16 @@ constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 // world into y-slabs over a cluster of 2 / 4 / 8 CTAs of 512 threads.
 constexpr int kResidentClasses = 6;
 constexpr int kSingleCtaClasses = 3;  // classes 0..2 hold a world in one CTA
+// Global-memory segment classes (the world stays in L2/HBM; one CTA of
+// 32/64/128/256 threads per world, by the work of one layer pair); -1 if the
+// world has too many layers.
+constexpr int kGmClasses = 4;
+int resident_class_gm(int X, int Y, int Z);
+// Class ids of a segment's tables: shared-memory classes 0..5, then the
+// global-memory classes 6..9.  meta = {per-step items, worlds per class,
+// offset of each class in the order array}.
+constexpr int kAllClasses = kResidentClasses + kGmClasses;
+constexpr int kMetaInts = 1 + 2 * kAllClasses;
 // smallest class that holds a world of these dims, -1 if none does
 int resident_class(int X, int Y, int Z);
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable
@@ -48,6 +62,9 @@ int smem_world_limit();
 fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
                                           int* counter, int* err, cudaStream_t st,
                                           unsigned long long* processed_cells = nullptr);
+
+fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
+                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells);
 
 // One world of a many-world conversion: its planes, its static bytes
 // (nullable) and the offset of its canonical bytes in a shared staging buffer.

@@ -103,7 +103,9 @@ __device__ __forceinline__ uint32_t lt_const(const uint32_t (&p)[8]) {
 }
 
 // Chooses among up to three ordered candidate masks c1..c3 for the blocks in
-// `mov`; r = draw(n) from the slot's random words.  Outputs destination masks.
+// `mov`; r = draw(n) with n = the number of candidates, from the slot's random
+// words P_w = plane(rk, g, s, w) (draw(2) = P_0; draw(3) compares u = sum_w
+// P_w << w with 85 and 170).  Outputs destination masks.
 __device__ __forceinline__ void bs_select(uint32_t mov, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t rk,
                                           uint32_t g, uint32_t s, uint32_t& d1, uint32_t& d2, uint32_t& d3) {
     const uint32_t two = (c1 & c2) | (c1 & c3) | (c2 & c3);
@@ -134,23 +136,30 @@ __host__ __device__ constexpr int other_col(int q, int n) { return n < q ? n : n
 // Runs one step of the rule on 32 blocks.  A[s], B[s] in/out per slot s.
 // Returns the mask of blocks that changed.
 __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], uint32_t rk, uint32_t g) {
-    uint32_t P[8], W[8], E[8], M[8];
+    // Only the empty and water planes change as slots are visited.  A slot
+    // acts exactly on the particles it held at the start (A[s]): a particle
+    // only ever moves into an empty cell, so a cell's own particle is still
+    // there when its slot comes, and a particle that arrives is never moved
+    // again.  The particle plane is rebuilt at the end from E and the solids.
+    uint32_t W[8], E[8];
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
-        P[s] = A[s];
         W[s] = A[s] & B[s];
         E[s] = ~(A[s] | B[s]);
-        M[s] = 0u;
     }
     const uint32_t etop = E[0] | E[1] | E[2] | E[3], ebot = E[4] | E[5] | E[6] | E[7];
-    const uint32_t active = ((P[0] | P[1] | P[2] | P[3]) & ebot) | ((W[0] | W[1] | W[2] | W[3]) & etop) |
+    const uint32_t active = ((A[0] | A[1] | A[2] | A[3]) & ebot) | ((W[0] | W[1] | W[2] | W[3]) & etop) |
                             ((W[4] | W[5] | W[6] | W[7]) & ebot);
     if (!active) return 0u;
 #pragma unroll
+    for (int s = 0; s < 8; ++s) B[s] = ~A[s] & B[s];  // from here on B holds the solids, which never change
+    uint32_t changed = 0;  // a block changes iff one of its particles moves
+#pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int q = s & 3, base = s & 4;
-        const uint32_t act = P[s] & ~M[s] & active;
+        const uint32_t act = A[s] & active;
         if (!act) continue;
+        const uint32_t wat = W[s];  // on the acting blocks: the slot's own water, untouched so far
         uint32_t fall = 0, dg1 = 0, dg2 = 0, dg3 = 0, side;
         if (s < 4) {
             const int b = 4 + q;
@@ -159,9 +168,9 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
             const uint32_t c1 = E[4 + other_col(q, 0)], c2 = E[4 + other_col(q, 1)], c3 = E[4 + other_col(q, 2)];
             const uint32_t any = c1 | c2 | c3;
             bs_select(rest & any, c1, c2, c3, rk, g, (uint32_t)s, dg1, dg2, dg3);
-            side = rest & ~any & W[s];
+            side = rest & ~any & wat;
         } else {
-            side = act & W[s];
+            side = act & wat;
         }
         const uint32_t e1 = E[base + other_col(q, 0)], e2 = E[base + other_col(q, 1)],
                        e3 = E[base + other_col(q, 2)];
@@ -170,15 +179,12 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
         if (smov) bs_select(smov, e1, e2, e3, rk, g, (uint32_t)s, sd1, sd2, sd3);
         const uint32_t moved = fall | dg1 | dg2 | dg3 | smov;
         if (!moved) continue;
-        const uint32_t wat = W[s];
-        P[s] &= ~moved;
+        changed |= moved;
         W[s] &= ~moved;
         E[s] |= moved;
         auto put = [&](int t, uint32_t m) {
             E[t] &= ~m;
-            P[t] |= m;
             W[t] |= m & wat;
-            M[t] |= m;
         };
         if (s < 4) {
             put(4 + q, fall);
@@ -190,13 +196,11 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
         put(base + other_col(q, 1), sd2);
         put(base + other_col(q, 2), sd3);
     }
-    uint32_t changed = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
-        const uint32_t nA = P[s], nB = W[s] | (~P[s] & ~E[s]);
-        changed |= (nA ^ A[s]) | (nB ^ B[s]);
-        A[s] = nA;
-        B[s] = nB;
+        const uint32_t solid = B[s];
+        A[s] = ~E[s] & ~solid;
+        B[s] = W[s] | solid;
     }
     return changed;
 }

@@ -22,7 +22,7 @@ struct RunScratch {
     PlaneItem* items = nullptr;
 };
 
-constexpr int kOrder = 1 + 2 * kResidentClasses, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
+constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
 
 }  // namespace
 

@@ -38,7 +38,7 @@ constexpr int kMaxDevices = 64;
 // scratch layout: [planes][one-world descriptor][ints][work items]
 constexpr size_t kDescOff = kNoAllocPlaneBytes;
 constexpr size_t kIntsOff = kDescOff + 256;
-constexpr int kOrder = 1 + 2 * kResidentClasses, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
+constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
 constexpr size_t kItemsOff = kIntsOff + 256;
 constexpr size_t kScratchBytes = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
 static_assert(kInts * sizeof(int) <= 256, "ints region");

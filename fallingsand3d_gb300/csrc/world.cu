@@ -39,7 +39,7 @@ namespace {
 
 // layout of fs3d_world::aux (device ints)
 constexpr int kAuxMeta = 0;                              // 1 + 2*classes ints
-constexpr int kAuxOrder = 1 + 2 * kResidentClasses;      // order[0] = 0
+constexpr int kAuxOrder = kMetaInts;      // order[0] = 0
 constexpr int kAuxCounter = kAuxOrder + 1;
 constexpr int kAuxErr = kAuxCounter + 1;
 constexpr int kAuxInts = kAuxErr + 1;

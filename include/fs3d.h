@@ -77,8 +77,12 @@ typedef struct fs3d_config {
     int steps_per_segment; /* steps per segment (graph length); default 64          */
     int ctas_per_sm;       /* persistent grid of the step kernel; 0 = all resident  */
     int use_graphs;        /* 1 (default) = run each segment as one CUDA graph       */
-    int use_smem;          /* 1 (default) = worlds that fit in shared memory take all
-                              their segment steps in one resident launch             */
+    int use_smem;          /* resident segments (all of a world's segment steps in
+                              one launch): 1 = the planes are held in shared memory
+                              (worlds that fit); 2 = the planes stay in global
+                              memory (L2), one CTA per world sized by the work of
+                              one layer; 3 (default) = 1 for a world's first 256
+                              steps, then 2; 0 = the per-step kernel only          */
     int reserved[12];
 } fs3d_config;
 
@@ -188,9 +192,11 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
 /* Autotuner: times each candidate launch configuration on trial_segments real
  * segments of the live worlds (they advance as usual), keeps the fastest per
  * voxel-update and remembers it for batches of the same make-up (live worlds
- * per size class).  Knobs: worlds that fit one CTA may run in the next wider
- * CTA class (promote), and the per-step kernel's CTAs per SM. */
+ * per size class).  Knobs: resident segments in global or shared memory
+ * (use_smem 2 or 1), worlds may run in the next wider CTA class (promote), and
+ * the per-step kernel's CTAs per SM when some world needs that kernel. */
 typedef struct fs3d_tune_report {
+    int mode;               /* chosen fs3d_config.use_smem                         */
     int promote;            /* chosen class promotion (0 = smallest fitting CTA)  */
     int ctas_per_sm;        /* chosen CTAs per SM of the per-step kernel           */
     int trials;             /* configurations timed                                */

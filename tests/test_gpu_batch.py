@@ -22,7 +22,8 @@ def oracle_final(orc, fs3d, dims, seed, n, start=0):
     return g
 
 
-@pytest.mark.parametrize("use_graphs,use_smem", [(True, True), (False, True), (True, False), (False, False)])
+@pytest.mark.parametrize("use_graphs,use_smem", [(True, True), (False, True), (True, False), (False, False),
+                                                  (True, 2), (False, 2)])
 def test_batch_matches_oracle(fs3d, orc, use_graphs, use_smem):
     worlds = small_batch(fs3d, 5, 24, max_dim=128)
     rng = np.random.default_rng(1)
@@ -87,7 +88,7 @@ def test_mix_equals_alone_with_continuous_admission(fs3d, orc):
 
 def test_budget_admission_and_release(fs3d):
     g = fs3d.gen_batch_world(1, 64, 64, 64)
-    per = 64 * 64 * 16 + 64  # planes: 64 rows x 64 rows x 16 bytes, plus descriptor
+    per = 64 * 64 * 16 + 64 + 64  # planes (64 x 64 rows of 16 bytes), layer flags (64 bytes), descriptor
     with fs3d.Batch(2 * per + 10, steps_per_segment=8) as b:
         t1 = b.admit(g, 1, 8)
         t2 = b.admit(g, 2, 8)
@@ -154,7 +155,7 @@ def test_admit_many_and_retire_many(fs3d, orc):
         ref = g.copy()
         orc.run(ref, seed, 0, n, nthreads=0)
         assert (o == ref).all()
-    with fs3d.Batch(2 * 64 * 64 * 16 + 200, steps_per_segment=8) as b:
+    with fs3d.Batch(2 * (64 * 64 * 16 + 64 + 64) + 100, steps_per_segment=8) as b:
         big = [fs3d.gen_batch_world(1, 64, 64, 64)] * 3
         assert len(b.admit_many(big, [1, 2, 3], 8)) == 2  # the third does not fit
 
@@ -165,7 +166,7 @@ CLASS_DIMS = [(16, 16, 16), (64, 64, 64), (64, 96, 128), (96, 96, 96), (128, 128
               (64, 512, 128), (40, 37, 21), (130, 66, 90)]
 
 
-@pytest.mark.parametrize("use_smem", [True, False])
+@pytest.mark.parametrize("use_smem", [True, False, 2])
 def test_every_resident_class_matches_oracle(fs3d, orc, use_smem):
     n = 67  # odd and not a multiple of the segment: phases and partial segments
     with fs3d.Batch(8 * GiB, steps_per_segment=32, use_smem=use_smem) as b:
@@ -208,7 +209,7 @@ def test_autotune_keeps_results_exact(fs3d, orc):
             rpt = b.autotune(trial_segments=1)
             assert rpt["cached"] == (rep == 1), rpt
             if rep == 0:
-                assert rpt["trials"] >= 3 and rpt["best_vox_per_ms"] > 0, rpt
+                assert rpt["trials"] >= 2 and rpt["best_vox_per_ms"] > 0, rpt
             assert 0 <= rpt["promote"] <= 2 and rpt["ctas_per_sm"] >= 1
             for _ in range(n // 32 + 1):
                 b.run_segment()
@@ -256,3 +257,25 @@ def test_counters_dense_and_processed(fs3d, orc):
         assert 0 < c["processed_cell_steps"] < c["dense_cell_steps"]
         for t, (dims, seed) in zip(tickets[:4], worlds):
             assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n))
+
+
+@pytest.mark.parametrize("use_smem", [True, 2])
+def test_kept_layer_flags_across_segments(fs3d, orc, use_smem):
+    """The layer change flags persist between segments (the first two steps of
+    a segment are not re-evaluated densely); worlds of every class, segments
+    of several lengths, joined by late admissions, must follow the oracle."""
+    worlds = [((16, 16, 16), 1), ((64, 64, 64), 2), ((96, 96, 96), 3), ((128, 128, 128), 4), ((40, 37, 21), 5),
+              ((16, 256, 16), 6), ((2048, 8, 6), 7)]
+    n = 333
+    with fs3d.Batch(8 * GiB, steps_per_segment=37, use_smem=use_smem) as b:
+        tickets = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for dims, seed in worlds[:4]]
+        for _ in range(3):
+            b.run_segment()
+        late = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n, start_step=250) for dims, seed in worlds[4:]]
+        for _ in range(n // 37 + 1):
+            b.run_segment()
+        b.sync()
+        for t, (dims, seed) in zip(tickets, worlds[:4]):
+            assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n)), dims
+        for t, (dims, seed) in zip(late, worlds[4:]):
+            assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n, start=250)), dims
