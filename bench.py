@@ -521,8 +521,12 @@ def run_only(args):
         worlds = batch_worlds(fs3d, args.master, args.worlds)
         with fs3d.Batch(150 << 30, steps_per_segment=args.segment) as b:
             for (X, Y, Z), seed in worlds:
-                b.admit_generated(X, Y, Z, seed, args.segment * (args.warmup + args.steps))
-            for _ in range(args.warmup + args.steps):
+                b.admit_generated(X, Y, Z, seed, args.segment * (args.warmup + args.steps + 8))
+            for _ in range(args.warmup):
+                b.run_segment()
+            if not args.no_autotune:
+                b.autotune(trial_segments=1)  # as the headline run does before its timed segments
+            for _ in range(args.steps):
                 b.run_segment()
             b.sync()
     else:

@@ -420,9 +420,13 @@ constexpr int resident_ctas_per_sm() {
 
 // GM: the world stays in global memory (L2) and the CTA keeps only the layer
 // flags and list in shared memory, so as many worlds are in flight as warps
-// allow; no bulk copies.  CTAs per SM of a GM kernel: 24 warps in all.
+// allow; no bulk copies.  CTAs per SM of a GM kernel: kGmThreadsPerSm threads.
+#ifndef FS3D_GM_THREADS_PER_SM
+#define FS3D_GM_THREADS_PER_SM 768
+#endif
+constexpr int kGmThreadsPerSm = FS3D_GM_THREADS_PER_SM;
 template <int NT, bool CL, bool GM = false>
-__global__ void __launch_bounds__(NT, CL ? 1 : (GM ? 768 / NT : resident_ctas_per_sm<NT>()))
+__global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resident_ctas_per_sm<NT>()))
     k_plane_segment_resident(const PlaneWorld* __restrict__ worlds,
                                                              const int* __restrict__ order,
                                                              const int* __restrict__ meta, int cls, int CS,
@@ -701,7 +705,7 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
     }
     FS3D_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
     const int nt = kGmThreads[cls];
-    const int grid = sm_count_public() * (768 / nt);
+    const int grid = sm_count_public() * (kGmThreadsPerSm / nt);
     const size_t smem = slab_aux_bytes((uint32_t)kGmMaxY[cls]);
     cudaError_t e;
     if (nt == 32)
