@@ -415,12 +415,13 @@ def run_fs3d(args):
         traffic = traffic * cells / traffic_cells
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 3), "traffic": traffic,
-                "kernel": "segment graph: k_plane_segment_resident (size classes) + k_plane_step",
+                "kernel": "segment graph: k_plane_segment_resident (shared- and global-memory classes)",
                 "launch": f"one {S}-step segment", "peak_source": src, "alg_bytes_per_launch": alg_bytes,
                 "dense_equiv_state_gbs": round(0.5 * cells * S / (ms / 1e3) / 1e9, 1),
                 "processed_fraction": round(proc_frac, 4),
-                "note": "the state stays in shared memory for the 64 steps of a segment, so DRAM sees about "
-                        "1/64 of the algorithmic bytes; the kernels are issue-bound (see profiles/)"}
+                "note": "algorithmic bytes count the evaluated cell-steps (settled layer pairs are skipped "
+                        "exactly); the worlds stay in L2, so DRAM sees a few MB per segment; the kernels are "
+                        "latency-bound: each world's steps are a serial chain (see profiles/)"}
 
     # ---- CPU baseline (rank 0, N=1)
     cpu = None
