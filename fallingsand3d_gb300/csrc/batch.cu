@@ -16,6 +16,7 @@
 
 #include <chrono>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -33,13 +34,14 @@ struct BWorld {
     uint64_t t0 = 0;  // step at admission
     int64_t remaining = 0;
     uint4* rows = nullptr;
+    std::shared_ptr<void> arena;  // set when rows live in a block shared by the worlds of one admit_many
     uint8_t* statics = nullptr;
     uint8_t* lflags = nullptr;  // layer flags after the planes (same allocation)
     bool flags_valid = false;   // kept up to date by every segment that stepped the world
     size_t bytes = 0;
     bool done = false;
     cudaEvent_t ready = nullptr;     // admission finished (side stream)
-    cudaEvent_t finished = nullptr;  // last segment that stepped it
+    std::shared_ptr<CUevent_st> finished;  // recorded after the segment that took its last step (shared)
     bool hash_valid = false;
     uint64_t hash = 0;
 };
@@ -158,13 +160,16 @@ fs3d_status wait_stream(cudaStream_t st, int64_t timeout_ns) {
 }
 
 void free_world(fs3d_batch* b, BWorld& w) {
-    if (w.rows) cudaFreeAsync(w.rows, b->side);
+    if (w.arena)
+        w.arena.reset();  // the block is freed with its last world
+    else if (w.rows)
+        cudaFreeAsync(w.rows, b->side);
     if (w.statics) cudaFreeAsync(w.statics, b->side);
     if (w.ready) cudaEventDestroy(w.ready);
-    if (w.finished) cudaEventDestroy(w.finished);
+    w.finished.reset();
     w.rows = nullptr;
     w.statics = nullptr;
-    w.ready = w.finished = nullptr;
+    w.ready = nullptr;
 }
 
 // One segment on stream `a`: the resident kernel of every class (worlds that
@@ -482,6 +487,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         if (s != FS3D_OK) return s;
     }
     FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
+    std::shared_ptr<CUevent_st> fin;  // one event for every world that finishes in this segment
     for (auto& kv : b->worlds) {
         BWorld& w = kv.second;
         if (w.done) continue;
@@ -490,8 +496,13 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         w.remaining -= steps;
         if (w.remaining == 0) {
             w.done = true;
-            if (!w.finished) FS3D_CUDA(cudaEventCreateWithFlags(&w.finished, cudaEventDisableTiming));
-            FS3D_CUDA(cudaEventRecord(w.finished, b->stream));
+            if (!fin) {
+                cudaEvent_t ev = nullptr;
+                FS3D_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                fin.reset(ev, [](CUevent_st* x) { cudaEventDestroy(x); });
+                FS3D_CUDA(cudaEventRecord(ev, b->stream));
+            }
+            w.finished = fin;
         }
     }
     ++b->segments;
@@ -516,7 +527,7 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
     *done = 0;
     if (!w.done) return FS3D_OK;
     if (w.finished) {
-        const cudaError_t q = cudaEventQuery(w.finished);
+        const cudaError_t q = cudaEventQuery(w.finished.get());
         if (q == cudaErrorNotReady) return FS3D_OK;
         if (q != cudaSuccess) return cuda_fail(q, "fs3d_batch_poll");
     }
@@ -545,7 +556,7 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
     auto it = b->worlds.find(ticket);
     if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire: unknown ticket");
     BWorld& w = it->second;
-    FS3D_CUDA(cudaStreamWaitEvent(b->side, w.finished ? w.finished : b->last_segment, 0));
+    FS3D_CUDA(cudaStreamWaitEvent(b->side, w.finished ? w.finished.get() : b->last_segment, 0));
     if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
     fs3d_status s = FS3D_OK;
     if (grid_out) {
@@ -610,25 +621,58 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     void* table = nullptr;
     const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k, off_bytes = sizeof(int64_t) * (size_t)k;
     const size_t flags_off = (jobs_bytes + off_bytes + 15) / 16 * 16;
+    const size_t copy_off = (flags_off + sizeof(int) * (size_t)k + 15) / 16 * 16;
+    const size_t copy_bytes = sizeof(CopyJob) * (size_t)k + sizeof(int64_t) * (size_t)k;
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
-    if (e == cudaSuccess) e = cudaMallocAsync(&table, flags_off + sizeof(int) * (size_t)k, b->side);
+    if (e == cudaSuccess) e = cudaMallocAsync(&table, copy_off + copy_bytes, b->side);
+    // grids the device can address (page-locked host or device memory) are
+    // gathered by one copy kernel; pageable ones take a copy call each
+    std::vector<CopyJob> copies;
+    std::vector<int64_t> chunk_off;
+    int64_t chunks = 0;
+    // one block for all the worlds' planes and layer flags (freed with the last of them)
+    std::vector<size_t> row_off((size_t)k);
+    size_t block_bytes = 0;
+    for (int a = 0; a < k; ++a) {
+        row_off[(size_t)a] = block_bytes;
+        block_bytes += (plane_bytes(specs[a].X, specs[a].Y, specs[a].Z) + layer_flag_bytes(specs[a].Y) + 255) & ~(size_t)255;
+    }
+    void* block = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync(&block, block_bytes, b->side);
     for (int a = 0; a < k && e == cudaSuccess; ++a) {
         const fs3d_world_spec& p = specs[a];
-        e = cudaMallocAsync((void**)&rows[(size_t)a], plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y), b->side);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, p.grid, (size_t)p.X * p.Y * p.Z,
-                                cudaMemcpyHostToDevice, b->side);
+        rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
+        const int64_t cells = (int64_t)p.X * p.Y * p.Z;
+        if (e == cudaSuccess) {
+            if (const uint8_t* dv = device_view(p.grid)) {
+                copies.push_back(CopyJob{dv, staging + jobs[(size_t)a].byte_off, cells});
+                chunk_off.push_back(chunks);
+                chunks += (cells + 15) / 16;
+            } else {
+                e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, p.grid, (size_t)cells, cudaMemcpyHostToDevice,
+                                    b->side);
+            }
+        }
         jobs[(size_t)a].rows = rows[(size_t)a];
     }
     ConvJob* jobs_dev = static_cast<ConvJob*>(table);
     int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
     int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(table) + flags_off);
-    // pageable sources: staged before the calls return
+    CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);
+    int64_t* chunk_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
+    // the tables are pageable: staged before the calls return
     if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
     if (e == cudaSuccess) e = cudaMemcpyAsync(off_dev, unit_off.data(), off_bytes, cudaMemcpyHostToDevice, b->side);
     if (e == cudaSuccess) e = cudaMemsetAsync(flags_dev, 0, sizeof(int) * (size_t)k, b->side);
+    if (e == cudaSuccess && !copies.empty())
+        e = cudaMemcpyAsync(copies_dev, copies.data(), sizeof(CopyJob) * copies.size(), cudaMemcpyHostToDevice,
+                            b->side);
+    if (e == cudaSuccess && !copies.empty())
+        e = cudaMemcpyAsync(chunk_dev, chunk_off.data(), sizeof(int64_t) * chunk_off.size(), cudaMemcpyHostToDevice,
+                            b->side);
     if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many upload");
+    if (s == FS3D_OK) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side);
     if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, k, units, staging, flags_dev, b->side);
     std::vector<int> flags((size_t)k, 0);
     if (s == FS3D_OK) {
@@ -651,14 +695,15 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     if (staging) cudaFreeAsync(staging, b->side);
     if (table) cudaFreeAsync(table, b->side);
     if (s != FS3D_OK) {
-        for (int a = 0; a < k; ++a) {
-            if (rows[(size_t)a]) cudaFreeAsync(rows[(size_t)a], b->side);
+        if (block) cudaFreeAsync(block, b->side);
+        for (int a = 0; a < k; ++a)
             if (statics[(size_t)a]) cudaFreeAsync(statics[(size_t)a], b->side);
-        }
         return s;
     }
     cudaEvent_t ready = nullptr;
     if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) == cudaSuccess) cudaEventRecord(ready, b->side);
+    cudaStream_t side = b->side;
+    std::shared_ptr<void> arena(block, [side](void* p) { cudaFreeAsync(p, side); });
     for (int a = 0; a < k; ++a) {
         const fs3d_world_spec& p = specs[a];
         BWorld w;
@@ -672,6 +717,7 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         w.remaining = p.n_steps;
         w.done = p.n_steps == 0;
         w.rows = rows[(size_t)a];
+        w.arena = arena;
         w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(p.X, p.Y, p.Z);
         w.statics = statics[(size_t)a];
         w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld) +
@@ -728,8 +774,10 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
             uint8_t* staging = nullptr;
             void* table = nullptr;
             const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k;
+            const size_t copy_off = (jobs_bytes + sizeof(int64_t) * (size_t)k + 15) / 16 * 16;
             cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
-            if (e == cudaSuccess) e = cudaMallocAsync(&table, jobs_bytes + sizeof(int64_t) * (size_t)k, b->side);
+            if (e == cudaSuccess)
+                e = cudaMallocAsync(&table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, b->side);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
             if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
@@ -738,11 +786,35 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
                                     b->side);
             if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
             if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, b->side);
+            // outputs the device can address are written by one copy kernel,
+            // pageable ones take a copy call each
+            std::vector<CopyJob> copies;
+            std::vector<int64_t> chunk_off;
+            int64_t chunks = 0;
             for (int q = 0; q < k && s == FS3D_OK; ++q) {
                 const BWorld& w = its[(size_t)who[(size_t)q]]->second;
-                e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off,
-                                    (size_t)w.X * w.Y * w.Z, cudaMemcpyDeviceToHost, b->side);
+                const int64_t cells = (int64_t)w.X * w.Y * w.Z;
+                if (uint8_t* dv = device_view(grids_out[who[(size_t)q]])) {
+                    copies.push_back(CopyJob{staging + jobs[(size_t)q].byte_off, dv, cells});
+                    chunk_off.push_back(chunks);
+                    chunks += (cells + 15) / 16;
+                    continue;
+                }
+                e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off, (size_t)cells,
+                                    cudaMemcpyDeviceToHost, b->side);
                 if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+            }
+            if (s == FS3D_OK && !copies.empty()) {
+                CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);
+                int64_t* chunk_dev =
+                    reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
+                e = cudaMemcpyAsync(copies_dev, copies.data(), sizeof(CopyJob) * copies.size(), cudaMemcpyHostToDevice,
+                                    b->side);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(chunk_dev, chunk_off.data(), sizeof(int64_t) * chunk_off.size(),
+                                        cudaMemcpyHostToDevice, b->side);
+                s = e == cudaSuccess ? copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side)
+                                     : cuda_fail(e, "fs3d_batch_retire_many readback table");
             }
             if (staging) cudaFreeAsync(staging, b->side);
             if (table) cudaFreeAsync(table, b->side);

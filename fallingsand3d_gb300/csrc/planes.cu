@@ -24,6 +24,7 @@
 #include "fs3d_common.h"
 #include "pcg.h"
 #include "planes.h"
+#include "conv_device.cuh"
 #include "rule_device.cuh"
 
 namespace fs3d {
@@ -31,9 +32,20 @@ namespace fs3d {
 // ---------------------------------------------------------------------------
 // conversions
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void classify(uint32_t v, uint32_t& a, uint32_t& b) {
-    a = (v == 2u || v == 3u) ? 1u : 0u;
-    b = (v == 0u || v == 2u) ? 0u : 1u;
+// One (row, word) unit: the 64-cell chunk at x = 64w of row r.
+__device__ __forceinline__ uint4 chunk_to_planes(const uint8_t* row, int X, int w, bool& big) {
+    uint32_t v[16];
+    load_chunk64(row + 64 * w, min(64, X - 64 * w), v, big);
+    return bytes_to_planes64(v);
+}
+
+__device__ __forceinline__ void planes_to_chunk(const uint4& q, const uint8_t* statics_row, uint8_t* row, int X,
+                                                int w) {
+    uint32_t v[16];
+    planes_to_words64(q, v);
+    const int n = min(64, X - 64 * w);
+    if (statics_row) patch_statics64(q, statics_row + 64 * w, n, v);
+    store_chunk64(row + 64 * w, n, v);
 }
 
 __global__ void k_bytes_to_planes(const uint8_t* __restrict__ g, int X, int Y, int Z, int nw,
@@ -42,22 +54,12 @@ __global__ void k_bytes_to_planes(const uint8_t* __restrict__ g, int X, int Y, i
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
         const int w = (int)(u % nw);
         const int64_t r = u / nw;
-        const uint8_t* row = g + r * X;
-        uint32_t ae = 0, ao = 0, be = 0, bo = 0;
-        for (int m = 0; m < 32; ++m) {
-            const int xe = 64 * w + 2 * m, xo = xe + 1;
-            uint32_t a, b;
-            classify(xe < X ? row[xe] : 1u, a, b);
-            ae |= a << m;
-            be |= b << m;
-            classify(xo < X ? row[xo] : 1u, a, b);
-            ao |= a << m;
-            bo |= b << m;
-        }
-        rows[u] = make_uint4(ae, ao, be, bo);
+        bool big;
+        rows[u] = chunk_to_planes(g + r * X, X, w, big);
     }
 }
 
+// the byte value of one cell of a plane word (static cells from `statics`, or stone)
 __device__ __forceinline__ uint32_t cell_value(const uint4& q, int m, int odd, const uint8_t* statics, int64_t idx) {
     const uint32_t a = ((odd ? q.y : q.x) >> m) & 1u, b = ((odd ? q.w : q.z) >> m) & 1u;
     if (a) return b ? 3u : 2u;
@@ -71,11 +73,7 @@ __global__ void k_planes_to_bytes(const uint4* __restrict__ rows, const uint8_t*
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
         const int w = (int)(u % nw);
         const int64_t r = u / nw;
-        const uint4 q = rows[u];
-        for (int x = 64 * w; x < 64 * w + 64 && x < X; ++x) {
-            const int64_t idx = r * X + x;
-            g[idx] = (uint8_t)cell_value(q, (x >> 1) & 31, x & 1, statics, idx);
-        }
+        planes_to_chunk(rows[u], statics ? statics + r * X : nullptr, g + r * X, X, w);
     }
 }
 
@@ -120,21 +118,8 @@ __global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const 
         const int64_t lu = u - unit_off[j];
         const int w = (int)(lu % jb.nw);
         const int64_t r = lu / jb.nw;
-        const uint8_t* row = staging + jb.byte_off + r * jb.X;
-        uint32_t ae = 0, ao = 0, be = 0, bo = 0, big = 0;
-        for (int m = 0; m < 32; ++m) {
-            const int xe = 64 * w + 2 * m, xo = xe + 1;
-            const uint32_t ve = xe < jb.X ? row[xe] : 1u, vo = xo < jb.X ? row[xo] : 1u;
-            big |= (ve | vo) & 0xFCu;
-            uint32_t a, b;
-            classify(ve, a, b);
-            ae |= a << m;
-            be |= b << m;
-            classify(vo, a, b);
-            ao |= a << m;
-            bo |= b << m;
-        }
-        jb.rows[lu] = make_uint4(ae, ao, be, bo);
+        bool big;
+        jb.rows[lu] = chunk_to_planes(staging + jb.byte_off + r * jb.X, jb.X, w, big);
         if (big) atomicOr(flags + j, 1);  // holds a static material >= 4: keep its bytes
     }
 }
@@ -147,12 +132,8 @@ __global__ void k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs, const 
         const int64_t lu = u - unit_off[j];
         const int w = (int)(lu % jb.nw);
         const int64_t r = lu / jb.nw;
-        const uint4 q = jb.rows[lu];
-        uint8_t* dst = staging + jb.byte_off;
-        for (int x = 64 * w; x < 64 * w + 64 && x < jb.X; ++x) {
-            const int64_t idx = r * jb.X + x;
-            dst[idx] = (uint8_t)cell_value(q, (x >> 1) & 31, x & 1, jb.statics, idx);
-        }
+        planes_to_chunk(jb.rows[lu], jb.statics ? jb.statics + r * jb.X : nullptr, staging + jb.byte_off + r * jb.X,
+                        jb.X, w);
     }
 }
 
@@ -181,8 +162,7 @@ __global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p,
                 st = st * kPcgMult + p.inc;
                 v = d < p.sand_thr ? 2u : (d < p.water_thr ? 3u : 0u);
             }
-            uint32_t a, b;
-            classify(v, a, b);
+            const uint32_t a = v >> 1, b = v & 1u;  // codes 0..3 are their own (A, B)
             if (m & 1) {
                 ao |= a << (m >> 1);
                 bo |= b << (m >> 1);
@@ -798,6 +778,43 @@ fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off
                                                                      flags);
     FS3D_CHECK_LAUNCH("bytes->planes (many worlds) launch");
     return FS3D_OK;
+}
+
+__global__ void k_copy_many(const CopyJob* __restrict__ jobs, const int64_t* __restrict__ chunk_off, int njobs,
+                            int64_t total) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int j = find_job(chunk_off, njobs, u);
+        const CopyJob jb = jobs[j];
+        const int64_t off = (u - chunk_off[j]) * 16;
+        const int64_t n = jb.bytes - off < 16 ? jb.bytes - off : 16;
+        const uint8_t* s = jb.src + off;
+        uint8_t* d = jb.dst + off;
+        if (n == 16 && ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d)) & 15u) == 0) {
+            *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(s);
+        } else {
+            for (int64_t i = 0; i < n; ++i) d[i] = s[i];
+        }
+    }
+}
+
+fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, int64_t total_chunks,
+                      cudaStream_t st) {
+    if (njobs <= 0 || total_chunks <= 0) return FS3D_OK;
+    k_copy_many<<<conv_grid(total_chunks), 256, 0, st>>>(jobs, chunk_off, njobs, total_chunks);
+    FS3D_CHECK_LAUNCH("many-copy launch");
+    return FS3D_OK;
+}
+
+uint8_t* device_view(const void* p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return static_cast<uint8_t*>(const_cast<void*>(p));
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return static_cast<uint8_t*>(a.devicePointer);
+    return nullptr;
 }
 
 fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,

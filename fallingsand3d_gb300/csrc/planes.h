@@ -81,6 +81,20 @@ fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off
 fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
                                   uint8_t* staging, cudaStream_t st);
 
+// Many byte copies in one launch (each thread moves a 16-byte chunk): used
+// instead of one cudaMemcpyAsync per world when both sides are addressable
+// by the device (device memory, or page-locked host memory, which the GPU
+// reads and writes directly).  chunk_off[j] = sum of ceil(bytes/16) before j.
+struct CopyJob {
+    const uint8_t* src;
+    uint8_t* dst;
+    int64_t bytes;
+};
+fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, int64_t total_chunks, cudaStream_t st);
+// A device-addressable alias of p (itself for device or managed memory, the
+// mapped address for page-locked host memory), or nullptr for pageable memory.
+uint8_t* device_view(const void* p);
+
 int plane_lg(int nw);
 int plane_items_for(int Y, int Z, int nw);
 int plane_step_grid(int64_t n_items);

@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "fs3d_common.h"
+#include "conv_device.cuh"
 #include "rule_device.cuh"
 
 namespace fs3d {
@@ -202,41 +203,6 @@ __global__ void __launch_bounds__(256) k_step_rows16(uint8_t* __restrict__ grid,
 // bit-sliced row-pair step (32 blocks per 32-bit operation) and writes back
 // only the 16-byte pieces whose cells changed class.
 // ---------------------------------------------------------------------------
-
-// bits 0, 8, 16, 24 -> bits 0..3
-__device__ __forceinline__ uint32_t gather_lo4(uint32_t m) { return (m * 0x10204080u) >> 28; }
-// bits 0..3 -> bit 0 of bytes 0..3
-__device__ __forceinline__ uint32_t spread4(uint32_t n) { return (n * 0x00204081u) & 0x01010101u; }
-
-// Four cells (one byte each) -> nibbles of A (sand or water) and B (water or
-// solid).  A value 0..3 is its own 2-bit code (A = bit 1, B = bit 0); any
-// value >= 4 is static and solid, code (0,1).
-__device__ __forceinline__ void classify4(uint32_t v, uint32_t& a4, uint32_t& b4) {
-    const uint32_t big = v & 0xFCFCFCFCu;
-    if (big) {
-        const uint32_t nz = ((big & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | big;  // bit 7 set iff byte >= 4
-        const uint32_t m = ((nz & 0x80808080u) >> 7) * 0xFFu;
-        v = (v & ~m) | (0x01010101u & m);
-    }
-    a4 = gather_lo4((v >> 1) & 0x01010101u);
-    b4 = gather_lo4(v & 0x01010101u);
-}
-
-// 64 cells (16 words, x = 4k + byte) -> {A even, A odd, B even, B odd}
-__device__ __forceinline__ uint4 bytes_to_planes64(const uint32_t (&w)[16]) {
-    uint32_t ae = 0, ao = 0, be = 0, bo = 0;
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-        uint32_t a, b;
-        classify4(__byte_perm(w[2 * p], w[2 * p + 1], 0x6420), a, b);  // x = 8p, 8p+2, 8p+4, 8p+6
-        ae |= a << (4 * p);
-        be |= b << (4 * p);
-        classify4(__byte_perm(w[2 * p], w[2 * p + 1], 0x7531), a, b);  // x = 8p+1, +3, +5, +7
-        ao |= a << (4 * p);
-        bo |= b << (4 * p);
-    }
-    return make_uint4(ae, ao, be, bo);
-}
 
 // Merges the new class of every changed cell of one 16-byte piece u (word
 // pairs 2u, 2u+1 of a 64-cell chunk) into its bytes.  Only empty, sand and

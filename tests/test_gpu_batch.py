@@ -279,3 +279,49 @@ def test_kept_layer_flags_across_segments(fs3d, orc, use_smem):
             assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n)), dims
         for t, (dims, seed) in zip(late, worlds[4:]):
             assert b.poll(t)[1] == orc.hash(oracle_final(orc, fs3d, dims, seed, n, start=250)), dims
+
+
+def test_admit_and_retire_many_pinned_and_device(fs3d, orc, cuda):
+    """Grids in page-locked host memory and in device memory are gathered and
+    scattered by one copy kernel (no copy call per world); pageable ones take
+    a copy each.  A mix of all three, odd sizes included, must round-trip and
+    step exactly."""
+    worlds = small_batch(fs3d, 23, 18, max_dim=96) + [((37, 21, 13), 901), ((5, 7, 3), 902)]
+    grids = [fs3d.gen_batch_world(seed, *dims) if dims[1] >= 4 else orc.gen_c1(seed, *dims)
+             for dims, seed in worlds]
+    kinds = ["pinned", "device", "pageable"]
+    srcs, ptrs = [], []
+    for i, g in enumerate(grids):
+        k = kinds[i % 3]
+        if k == "pinned":
+            t = cuda.from_numpy(g.copy()).pin_memory()
+        elif k == "device":
+            t = cuda.from_numpy(g.copy()).cuda()
+        else:
+            t = g.copy()
+        srcs.append(t)
+        ptrs.append(t.data_ptr() if k != "pageable" else t.ctypes.data)
+    outs, out_ptrs = [], []
+    for i, g in enumerate(grids):
+        k = kinds[(i + 1) % 3]
+        if k == "pinned":
+            t = cuda.zeros(g.shape, dtype=cuda.uint8).pin_memory()
+        elif k == "device":
+            t = cuda.zeros(g.shape, dtype=cuda.uint8, device="cuda")
+        else:
+            t = np.zeros_like(g)
+        outs.append(t)
+        out_ptrs.append(t.data_ptr() if k != "pageable" else t.ctypes.data)
+    cuda.cuda.synchronize()
+    n = 90
+    with fs3d.Batch(GiB, steps_per_segment=64) as b:
+        ts = b.admit_many(grids, [s for _, s in worlds], n, ptrs=ptrs)
+        assert len(ts) == len(worlds)
+        for _ in range(2):
+            b.run_segment()
+        b.retire_many(ts, out_ptrs)
+    for (dims, seed), g, o in zip(worlds, grids, outs):
+        ref = g.copy()
+        orc.run(ref, seed, 0, n, nthreads=0)
+        got = o.cpu().numpy() if hasattr(o, "cpu") else o
+        assert (got == ref).all(), dims
