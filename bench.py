@@ -115,19 +115,30 @@ def batch_worlds(fs3d, master: int, count: int):
     return [(tuple(int(v) for v in dims[w]), int(seeds[w])) for w in range(count)]
 
 
+def pinned_views(torch, shapes):
+    """One page-locked arena with a (Y, Z, X) view per world, back to back (the
+    way a server keeps request payloads): the library moves such runs over the
+    host link in one copy-engine transfer."""
+    sizes = [int(np.prod(sh)) for sh in shapes]
+    arena = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
+    views, off = [], 0
+    for sh, n in zip(shapes, sizes):
+        views.append(arena[off:off + n].view(*sh))
+        off += n
+    return views
+
+
 def gen_grids(fs3d, worlds, pinned_torch=None):
-    """Host grids (pinned when torch is given), generated in parallel."""
+    """Host grids (in one pinned arena when torch is given), generated in parallel."""
     def one(w):
         (X, Y, Z), seed = w
         return fs3d.gen_batch_world(seed, X, Y, Z)
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         grids = list(ex.map(one, worlds))
     if pinned_torch is not None:
-        out = []
-        for g in grids:
-            t = pinned_torch.empty(g.shape, dtype=pinned_torch.uint8, pin_memory=True)
+        out = pinned_views(pinned_torch, [g.shape for g in grids])
+        for t, g in zip(out, grids):
             t.numpy()[...] = g
-            out.append(t)
         return out
     return grids
 
@@ -295,24 +306,36 @@ def run_fs3d(args):
 
     # ---- e2e through the C ABI from pinned host buffers
     # one step = admit every world from pinned host memory (H2D + conversion),
-    # one segment, retire every world into pinned host memory (conversion + D2H)
-    e2e_ms, h2d, d2h = [], cells, cells
-    outs = [torch.empty(g.shape, dtype=torch.uint8, pin_memory=True) for g in host]
-    seeds = [seed for _, seed in worlds]
-    in_ptrs = [g.data_ptr() for g in host]
-    out_ptrs = [o.data_ptr() for o in outs]
+    # one segment, retire every world into pinned host memory (conversion + D2H).
+    # The host grids sit back to back in one page-locked arena (and so do the
+    # outputs), so each direction is one copy-engine transfer over the host link.
+    h2d, d2h = cells, cells
+    outs = pinned_views(torch, [tuple(g.shape) for g in host])
+    seeds = np.array([seed for _, seed in worlds], dtype=np.uint64)
+    dims_xyz = np.array([d for d, _ in worlds], dtype=np.int64)
+    in_ptrs = np.array([g.data_ptr() for g in host], dtype=np.uint64)
+    out_ptrs = np.array([o.data_ptr() for o in outs], dtype=np.uint64)
+    e2e_ms = []
     with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
-        for it in range(4):
+        for it in range(2 + args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ts = eb.admit_many(host, seeds, S, ptrs=in_ptrs)
-            if it == 0 and not args.no_autotune:
-                eb.autotune(trial_segments=1)  # same make-up: applies the choice made above
+            ts = eb.admit_many(None, seeds, S, ptrs=in_ptrs, dims=dims_xyz)
             eb.run_segment()
             eb.retire_many(ts, out_ptrs)
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_ms = e2e_ms[1:]  # the first call also captures the segment graph
+    e2e_ms = e2e_ms[2:]  # the first calls also capture the segment graph and grow the pool
     e2e_val = cells * S / (float(np.mean(e2e_ms)) / 1e3)
+    if parity is not None:
+        # the round trip: each output is its input stepped S steps
+        for i in (0, len(worlds) - 1):
+            (X, Y, Z), seed = worlds[i]
+            g = host[i].numpy().copy()
+            orc.run(g, seed, 0, S, nthreads=0)
+            if not (outs[i].numpy() == g).all():
+                parity = "MISMATCH (e2e)"
+        if not parity.startswith("MISMATCH"):
+            parity += "; 2 worlds of the e2e round trip bit-exact"
 
     # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
     offs, off = [], 0
@@ -446,7 +469,8 @@ def run_fs3d(args):
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(float(np.mean(e2e_ms)), 2),
-                        "path": "fs3d_batch_admit_many (pinned) + fs3d_batch_run_segment + fs3d_batch_retire_many"},
+                        "path": "fs3d_batch_admit_many (pinned arena) + fs3d_batch_run_segment + "
+                                "fs3d_batch_retire_many (pinned arena)"},
                 "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
                                     "launches_per_segment": S * len(worlds),
                                     "speedup_batched_vs_plain": round(value / world / plain_val, 2)},
@@ -546,6 +570,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--e2e-steps", type=int, default=6, help="timed steps of the e2e leg")
     ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
     ap.add_argument("--worlds", type=int, default=2048)
     ap.add_argument("--master", type=int, default=1)

@@ -89,6 +89,12 @@ class WorldSpec(C.Structure):
                 ("seed", C.c_uint64), ("start_step", C.c_uint64), ("n_steps", C.c_int64)]
 
 
+# numpy view of fs3d_world_spec (same field offsets), for building many at once
+_SPEC_DTYPE = np.dtype([("grid", np.uint64), ("X", np.int32), ("Y", np.int32), ("Z", np.int32), ("pad", np.int32),
+                        ("seed", np.uint64), ("start_step", np.uint64), ("n_steps", np.int64)])
+assert _SPEC_DTYPE.itemsize == C.sizeof(WorldSpec)
+
+
 class TuneReport(C.Structure):
     _fields_ = [("mode", C.c_int), ("promote", C.c_int), ("ctas_per_sm", C.c_int), ("trials", C.c_int), ("cached", C.c_int),
                 ("segments", C.c_int), ("best_vox_per_ms", C.c_double), ("trial_vox_per_ms", C.c_double * 8)]
@@ -446,38 +452,50 @@ class Batch:
         check(lib().fs3d_batch_admit_generated(self.handle, X, Y, Z, seed, start_step, n_steps, C.byref(t)))
         return int(t.value)
 
-    def admit_many(self, grids, seeds, n_steps, start_steps=None, ptrs=None):
-        """Admits many host grids with one host wait.  `ptrs` may give raw
-        host pointers (e.g. pinned buffers) instead of the numpy arrays'.
-        Returns the tickets of the admitted worlds (in order)."""
-        n = len(grids)
-        specs = (WorldSpec * max(n, 1))()
-        keep = []
-        for a, g in enumerate(grids):
-            Y, Z, X = g.shape
-            if ptrs is None:
-                g = np.ascontiguousarray(g, dtype=np.uint8)
-                keep.append(g)
-                p = _ptr(g)
+    def admit_many(self, grids, seeds, n_steps, start_steps=None, ptrs=None, dims=None):
+        """Admits many grids with one host wait.  `ptrs` may give raw pointers
+        (page-locked host or device buffers are gathered on the device in one
+        pass) instead of the numpy arrays'; with `ptrs`, `dims` (an n x 3 array
+        of X, Y, Z) may replace `grids`.  Returns the tickets of the admitted
+        worlds (in order)."""
+        n = len(ptrs) if grids is None else len(grids)
+        spec = np.zeros(max(n, 1), dtype=_SPEC_DTYPE)
+        keep = None
+        if n:
+            if dims is not None:
+                xyz = np.asarray(dims, dtype=np.int64).reshape(n, 3)
             else:
-                p = ptrs[a]
-            specs[a] = WorldSpec(p, X, Y, Z, 0, int(seeds[a]), int(start_steps[a]) if start_steps is not None else 0,
-                                 int(n_steps[a]) if hasattr(n_steps, "__len__") else int(n_steps))
-        tickets = (u64 * max(n, 1))()
+                shp = np.array([tuple(g.shape) for g in grids], dtype=np.int64).reshape(n, 3)  # (Y, Z, X)
+                xyz = shp[:, [2, 0, 1]]
+            if ptrs is None:
+                keep = [np.ascontiguousarray(g, dtype=np.uint8) for g in grids]
+                ptrs = [k.ctypes.data for k in keep]
+            spec["grid"][:n] = np.asarray(ptrs, dtype=np.uint64)
+            spec["X"][:n], spec["Y"][:n], spec["Z"][:n] = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+            spec["seed"][:n] = np.asarray(seeds, dtype=np.uint64)
+            spec["start_step"][:n] = np.asarray(start_steps if start_steps is not None else 0, dtype=np.uint64)
+            spec["n_steps"][:n] = np.asarray(n_steps, dtype=np.int64)
+        tickets = np.zeros(max(n, 1), dtype=np.uint64)
         done = i32()
-        st = lib().fs3d_batch_admit_many(self.handle, n, specs, tickets, C.byref(done))
+        st = lib().fs3d_batch_admit_many(self.handle, n, spec.ctypes.data_as(C.POINTER(WorldSpec)),
+                                         tickets.ctypes.data_as(C.POINTER(u64)), C.byref(done))
         if st not in (OK, ERR_BUDGET):
             check(st)
-        return [int(tickets[a]) for a in range(done.value)]
+        del keep
+        return tickets[:done.value].tolist()
 
     def retire_many(self, tickets, out_ptrs=None) -> None:
-        """Retires worlds with one host wait; out_ptrs: host buffers (or None)."""
+        """Retires worlds with one host wait; out_ptrs: host (or device) buffers, or None."""
         n = len(tickets)
-        ts = (u64 * max(n, 1))(*tickets)
+        ts = np.asarray(tickets if n else [0], dtype=np.uint64)
         outs = None
         if out_ptrs is not None:
-            outs = (vp * max(n, 1))(*[p for p in out_ptrs])
-        check(lib().fs3d_batch_retire_many(self.handle, n, ts, outs))
+            try:
+                outs_arr = np.asarray(out_ptrs if n else [0], dtype=np.uint64)
+            except TypeError:  # None entries: those worlds are not read back
+                outs_arr = np.asarray([p or 0 for p in out_ptrs], dtype=np.uint64)
+            outs = outs_arr.ctypes.data_as(C.POINTER(vp))
+        check(lib().fs3d_batch_retire_many(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)), outs))
 
     def try_admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> Optional[int]:
         try:

@@ -120,12 +120,14 @@ constexpr uint64_t kYoungSteps = 256;
 // Segment class of a running world (-1: the per-step kernel) under the
 // batch's mode: 1 shared-memory classes, 2 global-memory classes, 3 hybrid
 // (young worlds in shared memory when they fit, settled ones in global
-// memory), 0 none.  `promote` moves single-CTA worlds to wider classes.
+// memory), 0 none.  `promote` moves worlds to wider classes: the shared-memory
+// single-CTA classes in mode 1, the global-memory classes in modes 2 and 3
+// (the hybrid mode tunes on settled worlds, which run in global memory).
 int segment_class(const fs3d_batch* b, const BWorld& w) {
     const int mode = b->cfg.use_smem;
     auto smem = [&]() {
         int c = resident_class(w.X, w.Y, w.Z);
-        if (c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
+        if (mode == 1 && c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
         return c;
     };
     auto gm = [&]() {
@@ -626,8 +628,10 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
     if (e == cudaSuccess) e = cudaMallocAsync(&table, copy_off + copy_bytes, b->side);
-    // grids the device can address (page-locked host or device memory) are
-    // gathered by one copy kernel; pageable ones take a copy call each
+    // grids the device can address (page-locked host or device memory) that lie
+    // back to back go over in one copy-engine transfer per run (the SMs stay
+    // free for segments in flight); other device-addressable grids are gathered
+    // by one copy kernel; pageable ones take a copy call each
     std::vector<CopyJob> copies;
     std::vector<int64_t> chunk_off;
     int64_t chunks = 0;
@@ -640,22 +644,32 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     }
     void* block = nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync(&block, block_bytes, b->side);
-    for (int a = 0; a < k && e == cudaSuccess; ++a) {
-        const fs3d_world_spec& p = specs[a];
+    for (int a = 0; a < k; ++a)
         rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
-        const int64_t cells = (int64_t)p.X * p.Y * p.Z;
-        if (e == cudaSuccess) {
-            if (const uint8_t* dv = device_view(p.grid)) {
-                copies.push_back(CopyJob{dv, staging + jobs[(size_t)a].byte_off, cells});
-                chunk_off.push_back(chunks);
-                chunks += (cells + 15) / 16;
-            } else {
-                e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, p.grid, (size_t)cells, cudaMemcpyHostToDevice,
-                                    b->side);
-            }
+    for (int a = 0; a < k && e == cudaSuccess;) {
+        const int64_t cells = (int64_t)specs[a].X * specs[a].Y * specs[a].Z;
+        const uint8_t* dv = device_view(specs[a].grid);
+        int e_run = a + 1;  // [a, e_run): sources and staging both contiguous
+        int64_t run_bytes = cells;
+        while (dv && e_run < k) {
+            const int64_t c = (int64_t)specs[e_run].X * specs[e_run].Y * specs[e_run].Z;
+            if (specs[e_run].grid != specs[e_run - 1].grid + (jobs[(size_t)e_run].byte_off - jobs[(size_t)e_run - 1].byte_off) ||
+                run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)a].byte_off || !device_view(specs[e_run].grid))
+                break;
+            run_bytes += c;
+            ++e_run;
         }
-        jobs[(size_t)a].rows = rows[(size_t)a];
+        if (!dv || e_run - a > 1) {
+            e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, specs[a].grid, (size_t)run_bytes, cudaMemcpyDefault,
+                                b->side);
+        } else {
+            copies.push_back(CopyJob{dv, staging + jobs[(size_t)a].byte_off, cells});
+            chunk_off.push_back(chunks);
+            chunks += (cells + 15) / 16;
+        }
+        a = e_run;
     }
+    for (int a = 0; a < k; ++a) jobs[(size_t)a].rows = rows[(size_t)a];
     ConvJob* jobs_dev = static_cast<ConvJob*>(table);
     int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
     int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(table) + flags_off);
@@ -791,18 +805,34 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
             std::vector<CopyJob> copies;
             std::vector<int64_t> chunk_off;
             int64_t chunks = 0;
-            for (int q = 0; q < k && s == FS3D_OK; ++q) {
+            // outputs lying back to back go back in one copy-engine transfer per run
+            for (int q = 0; q < k && s == FS3D_OK;) {
+                uint8_t* out = grids_out[who[(size_t)q]];
                 const BWorld& w = its[(size_t)who[(size_t)q]]->second;
                 const int64_t cells = (int64_t)w.X * w.Y * w.Z;
-                if (uint8_t* dv = device_view(grids_out[who[(size_t)q]])) {
+                uint8_t* dv = device_view(out);
+                int e_run = q + 1;
+                int64_t run_bytes = cells;
+                while (dv && e_run < k) {
+                    const BWorld& w2 = its[(size_t)who[(size_t)e_run]]->second;
+                    const int64_t d = jobs[(size_t)e_run].byte_off - jobs[(size_t)e_run - 1].byte_off;
+                    if (grids_out[who[(size_t)e_run]] != grids_out[who[(size_t)e_run - 1]] + d ||
+                        run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)q].byte_off ||
+                        !device_view(grids_out[who[(size_t)e_run]]))
+                        break;
+                    run_bytes += (int64_t)w2.X * w2.Y * w2.Z;
+                    ++e_run;
+                }
+                if (!dv || e_run - q > 1) {
+                    e = cudaMemcpyAsync(out, staging + jobs[(size_t)q].byte_off, (size_t)run_bytes, cudaMemcpyDefault,
+                                        b->side);
+                    if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+                } else {
                     copies.push_back(CopyJob{staging + jobs[(size_t)q].byte_off, dv, cells});
                     chunk_off.push_back(chunks);
                     chunks += (cells + 15) / 16;
-                    continue;
                 }
-                e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off, (size_t)cells,
-                                    cudaMemcpyDeviceToHost, b->side);
-                if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+                q = e_run;
             }
             if (s == FS3D_OK && !copies.empty()) {
                 CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);

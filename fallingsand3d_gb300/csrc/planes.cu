@@ -780,19 +780,40 @@ fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off
     return FS3D_OK;
 }
 
+// Each warp moves 2 KB blocks: lane l takes the 16-byte chunks 32i + l of its
+// block (contiguous 512 bytes per instruction), all four loads before the
+// stores; one job search per block (a block spans at most a few jobs).
 __global__ void k_copy_many(const CopyJob* __restrict__ jobs, const int64_t* __restrict__ chunk_off, int njobs,
                             int64_t total) {
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
-        const int j = find_job(chunk_off, njobs, u);
-        const CopyJob jb = jobs[j];
-        const int64_t off = (u - chunk_off[j]) * 16;
-        const int64_t n = jb.bytes - off < 16 ? jb.bytes - off : 16;
-        const uint8_t* s = jb.src + off;
-        uint8_t* d = jb.dst + off;
-        if (n == 16 && ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d)) & 15u) == 0) {
-            *reinterpret_cast<uint4*>(d) = *reinterpret_cast<const uint4*>(s);
-        } else {
-            for (int64_t i = 0; i < n; ++i) d[i] = s[i];
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t blk = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; blk * 128 < total; blk += nwarps) {
+        int j = find_job(chunk_off, njobs, blk * 128);
+        const uint8_t* src[4];
+        uint8_t* dst[4];
+        int n[4];
+        uint4 v[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int64_t u = blk * 128 + 32 * i + lane;
+            n[i] = 0;
+            if (u >= total) continue;
+            while (j + 1 < njobs && __ldg(chunk_off + j + 1) <= u) ++j;
+            const CopyJob& jb = jobs[j];
+            const int64_t off = (u - __ldg(chunk_off + j)) * 16;
+            n[i] = (int)(jb.bytes - off < 16 ? jb.bytes - off : 16);
+            src[i] = jb.src + off;
+            dst[i] = jb.dst + off;
+            if (n[i] == 16 && ((reinterpret_cast<uintptr_t>(src[i]) | reinterpret_cast<uintptr_t>(dst[i])) & 15u) == 0)
+                v[i] = *reinterpret_cast<const uint4*>(src[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (!n[i]) continue;
+            if (n[i] == 16 && ((reinterpret_cast<uintptr_t>(src[i]) | reinterpret_cast<uintptr_t>(dst[i])) & 15u) == 0)
+                *reinterpret_cast<uint4*>(dst[i]) = v[i];
+            else
+                for (int k = 0; k < n[i]; ++k) dst[i][k] = src[i][k];
         }
     }
 }
@@ -800,7 +821,9 @@ __global__ void k_copy_many(const CopyJob* __restrict__ jobs, const int64_t* __r
 fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, int64_t total_chunks,
                       cudaStream_t st) {
     if (njobs <= 0 || total_chunks <= 0) return FS3D_OK;
-    k_copy_many<<<conv_grid(total_chunks), 256, 0, st>>>(jobs, chunk_off, njobs, total_chunks);
+    const int64_t blocks_needed = (total_chunks + 128 * 8 - 1) / (128 * 8), cap = (int64_t)sm_count_public() * 8;
+    const int grid = (int)(blocks_needed < cap ? blocks_needed : cap);
+    k_copy_many<<<grid < 1 ? 1 : grid, 256, 0, st>>>(jobs, chunk_off, njobs, total_chunks);
     FS3D_CHECK_LAUNCH("many-copy launch");
     return FS3D_OK;
 }

@@ -325,3 +325,43 @@ def test_admit_and_retire_many_pinned_and_device(fs3d, orc, cuda):
         orc.run(ref, seed, 0, n, nthreads=0)
         got = o.cpu().numpy() if hasattr(o, "cpu") else o
         assert (got == ref).all(), dims
+
+
+@pytest.mark.parametrize("where", ["pinned", "device"])
+def test_admit_and_retire_many_contiguous_runs(fs3d, orc, cuda, where):
+    """Worlds stored back to back in one arena go over in one copy per run;
+    a gap (and a world whose size is not a multiple of 16) ends a run."""
+    worlds = small_batch(fs3d, 29, 14, max_dim=64) + [((37, 21, 13), 903)] + small_batch(fs3d, 31, 6, max_dim=48)
+    grids = [fs3d.gen_batch_world(seed, *dims) for dims, seed in worlds]
+    sizes = [g.size for g in grids]
+    gap = 48
+    total = sum(sizes) + gap
+
+    def arena():
+        t = cuda.zeros(total, dtype=cuda.uint8)
+        return t.pin_memory() if where == "pinned" else t.cuda()
+
+    src, dst = arena(), arena()
+    offs, off = [], 0
+    for i, n in enumerate(sizes):
+        if i == 7:
+            off += gap  # a hole in the middle of a run
+        offs.append(off)
+        off += n
+    flat = cuda.from_numpy(np.concatenate([g.reshape(-1) for g in grids]))
+    for o, n, g in zip(offs, sizes, grids):
+        src[o:o + n].copy_(cuda.from_numpy(g.reshape(-1)))
+    cuda.cuda.synchronize()
+    del flat
+    n_steps = 70
+    with fs3d.Batch(GiB, steps_per_segment=64) as b:
+        ts = b.admit_many(None, [s for _, s in worlds], n_steps, ptrs=[src.data_ptr() + o for o in offs],
+                          dims=[d for d, _ in worlds])
+        for _ in range(2):
+            b.run_segment()
+        b.retire_many(ts, [dst.data_ptr() + o for o in offs])
+    out = dst.cpu().numpy()
+    for (dims, seed), g, o, n in zip(worlds, grids, offs, sizes):
+        ref = g.copy()
+        orc.run(ref, seed, 0, n_steps, nthreads=0)
+        assert (out[o:o + n].reshape(g.shape) == ref).all(), dims
