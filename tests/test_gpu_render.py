@@ -110,3 +110,23 @@ def test_object_material_custom_mesh(fs3d, orc, cuda):
     fs3d.render_object_device(view, tri, W, H, out.data_ptr(), cuda.cuda.current_stream().cuda_stream)
     exp = orc.render_object(oracle_lib.scene_view(rot_y=10.0), tri, W, H)
     assert np.array_equal(out.cpu().numpy(), exp)
+
+
+def test_dda_after_steps_of_a_large_world(fs3d, orc):
+    """A plane world too large for the resident kernels (per-step kernel),
+    rendered between runs of steps that rain water into empty bricks: every
+    frame (brick map rebuilt from the current planes) equals the CPU DDA of
+    the read-back grid exactly, from outside and from inside the world."""
+    X, Y, Z = 256, 160, 192
+    g = orc.gen_c5(11, X, Y, Z)
+    W, H = 192, 108
+    cam = fs3d.camera_world_view(X, Y, Z, W, H)
+    low = fs3d.camera_world_view(X, Y, Z, W, H)
+    low.origin[0], low.origin[1], low.origin[2] = 20.5, 30.25, 10.0
+    with fs3d.World(g, 11, 0, fs3d.LAYOUT_PLANES) as w:
+        check_img(w.render(cam, W, H), orc.render_dda(g, oracle_lib.camera_from(cam), W, H))
+        for n in (40, 1, 75):
+            w.step(n)
+            cur = w.read()
+            for c in (cam, low):
+                check_img(w.render(c, W, H), orc.render_dda(cur, oracle_lib.camera_from(c), W, H))
