@@ -47,7 +47,7 @@ EXPORTS = (
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
-    "fs3d_render_object", "fs3d_gen_parity", "fs3d_gen_pillars",
+    "fs3d_render_object", "fs3d_render_meshes", "fs3d_gen_parity", "fs3d_gen_pillars",
     "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
 )
 
@@ -104,6 +104,14 @@ class ObjectView(C.Structure):
     _fields_ = [("cam_pos", C.c_float * 3), ("cam_rot_y_deg", C.c_float), ("fovy_deg", C.c_float),
                 ("aspect", C.c_float), ("znear", C.c_float), ("zfar", C.c_float), ("model", C.c_float * 16),
                 ("clear", C.c_float * 4)]
+
+
+MAT_BASIC, MAT_TEXTURED, MAT_TEXTURE = 0, 1, 2
+
+
+class MeshDraw(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("n_vertices", C.c_int), ("material", C.c_int), ("model", C.c_float * 16),
+                ("color", C.c_float * 4), ("texture", C.c_void_p), ("tex_width", C.c_int), ("tex_height", C.c_int)]
 
 
 class Config(C.Structure):
@@ -169,6 +177,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_object_view_scene": (None, [C.POINTER(ObjectView)]),
         "fs3d_mesh_cube": (C.c_int, [vp]),
         "fs3d_render_object": (S, [C.POINTER(ObjectView), vp, i32, i32, i32, vp, vp]),
+        "fs3d_render_meshes": (S, [C.POINTER(ObjectView), C.POINTER(MeshDraw), i32, i32, i32, vp, vp]),
         "fs3d_gen_parity": (S, [u64, i32, i32, i32, vp]),
         "fs3d_gen_pillars": (S, [u64, i32, i32, i32, vp]),
         "fs3d_gen_batch_dims": (S, [u64, i32, vp, vp]),
@@ -279,6 +288,24 @@ def render_object_device(view: ObjectView, tri: np.ndarray, W: int, H: int, rgba
     """The raymarch_sphere material over a triangle mesh into W*H RGBA float32 at rgba_ptr."""
     tri = np.ascontiguousarray(tri, np.float32).reshape(-1, 9)
     check(lib().fs3d_render_object(C.byref(view), _ptr(tri), tri.shape[0], W, H, rgba_ptr, stream))
+
+
+def mesh_draw(vertices_ptr: int, n_vertices: int, material: int = MAT_BASIC, model=None, color=(1.0, 1.0, 1.0, 1.0),
+              texture_ptr: int = 0, tex_width: int = 0, tex_height: int = 0) -> MeshDraw:
+    """One draw of fs3d_render_meshes: vertices as {x,y,z,u,v} float32 (device or
+    page-locked), model a row-major 4x4 (stored column-major), RGBA8 sRGB texture."""
+    d = MeshDraw()
+    d.vertices, d.n_vertices, d.material = vertices_ptr, n_vertices, material
+    d.model[:] = [float(x) for x in np.asarray(model if model is not None else np.eye(4), np.float32).T.reshape(-1)]
+    d.color[:] = [float(c) for c in color]
+    d.texture, d.tex_width, d.tex_height = texture_ptr, tex_width, tex_height
+    return d
+
+
+def render_meshes_device(view: ObjectView, draws, W: int, H: int, rgba_ptr: int, stream: int = 0) -> None:
+    """The basic_mat / textured_mat / tri materials over the given draws into W*H RGBA float32."""
+    arr = (MeshDraw * max(len(draws), 1))(*draws)
+    check(lib().fs3d_render_meshes(C.byref(view), arr, len(draws), W, H, rgba_ptr, stream))
 
 
 # ---------------------------------------------------------------- device entry points

@@ -23,6 +23,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <vector>
+
 #include "fs3d_common.h"
 #include "planes.h"
 
@@ -241,6 +243,242 @@ __global__ void k_render_object(const __grid_constant__ ObjScene sc, int W, int 
     out[(size_t)py * W + px] = make_float4(col, 0.0f, 0.0f, 1.0f);
 }
 
+// ---- mesh materials: basic_mat / textured_mat / tri ------------------------
+// Restated pipelines: basic_mat.{vert,frag} (flat colour), textured_mat (the
+// colour plus the texel, alpha + 1), tri (the texel, alpha 1), with the
+// fixed-function state they are drawn with (no culling, depth LESS_OR_EQUAL
+// against 1, one sample per pixel, NEAREST filtering with REPEAT addressing
+// of R8G8B8A8_SRGB textures).  Three passes: per primitive, transform by
+// P*V*model and clip against 0 <= z <= w (Vulkan's depth range) into up to
+// three screen triangles; per screen triangle, test the pixel centres of its
+// box with edge functions and keep per pixel the smallest 64-bit key
+// (depth bits, then the later primitive first: LESS_OR_EQUAL lets a later
+// fragment at equal depth win); per pixel, shade the winner with
+// perspective-correct texture coordinates.  The order in which fragments
+// arrive does not matter, so the frame is deterministic and equals the CPU
+// restatement bit for bit (every float operation single-rounded, in the same
+// order).
+
+struct MeshDrawDev {
+    float mvp[16];
+    float color[4];
+    const float* verts;
+    const uint8_t* tex;
+    int tex_w, tex_h, material, n_tri;
+    long long prim0;
+};
+
+struct ScrTri {
+    float sx[3], sy[3], sz[3], iw[3], uw[3], vw[3];
+    float area;
+    int tl;
+    int valid;
+};
+
+struct ClipVtx {
+    float x, y, z, w, u, v;
+};
+
+__device__ __forceinline__ int floor_to_int_dev(float x) {
+    if (x != x) return 0;
+    x = floorf(x);
+    if (x >= 2147483647.0f) return 2147483647;
+    if (x <= -2147483648.0f) return -2147483647 - 1;
+    return (int)x;
+}
+
+__device__ __forceinline__ ClipVtx clip_lerp_dev(const ClipVtx& a, const ClipVtx& b, float t) {
+    ClipVtx r;
+    r.x = __fadd_rn(a.x, __fmul_rn(t, __fsub_rn(b.x, a.x)));
+    r.y = __fadd_rn(a.y, __fmul_rn(t, __fsub_rn(b.y, a.y)));
+    r.z = __fadd_rn(a.z, __fmul_rn(t, __fsub_rn(b.z, a.z)));
+    r.w = __fadd_rn(a.w, __fmul_rn(t, __fsub_rn(b.w, a.w)));
+    r.u = __fadd_rn(a.u, __fmul_rn(t, __fsub_rn(b.u, a.u)));
+    r.v = __fadd_rn(a.v, __fmul_rn(t, __fsub_rn(b.v, a.v)));
+    return r;
+}
+
+// keeps the part with d >= 0, d = z (plane 0) or w - z (plane 1)
+__device__ __forceinline__ int clip_plane_dev(const ClipVtx* in, int n, ClipVtx* out, int plane) {
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        const ClipVtx& a = in[i];
+        const ClipVtx& b = in[(i + 1) % n];
+        const float da = plane ? __fsub_rn(a.w, a.z) : a.z, db = plane ? __fsub_rn(b.w, b.z) : b.z;
+        if (da >= 0.0f) out[m++] = a;
+        if ((da >= 0.0f) != (db >= 0.0f)) out[m++] = clip_lerp_dev(a, b, __fdiv_rn(da, __fsub_rn(da, db)));
+    }
+    return m;
+}
+
+__device__ __forceinline__ float dot4_dev(float m0, float m1, float m2, float m3, const float* p) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m0, p[0]), __fmul_rn(m1, p[1])), __fmul_rn(m2, p[2])), m3);
+}
+
+__device__ __forceinline__ int top_left_dev(float ax, float ay, float bx, float by) {
+    return by < ay || (by == ay && bx > ax);
+}
+
+// the draw holding primitive p: the last one whose first primitive is <= p
+__device__ __forceinline__ int find_draw(const MeshDrawDev* __restrict__ draws, int n_draws, long long p) {
+    int lo = 0, hi = n_draws - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (draws[mid].prim0 <= p)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_mesh_setup(const MeshDrawDev* __restrict__ draws, int n_draws, long long n_prims, int W, int H,
+                             ScrTri* __restrict__ tris) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_prims) return;
+    const int d = find_draw(draws, n_draws, p);
+    const MeshDrawDev& dr = draws[d];
+    const float* v = dr.verts + 15 * (p - dr.prim0);
+    const float* m = dr.mvp;
+    ClipVtx a[8], b[8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float* q = v + 5 * k;
+        a[k].x = dot4_dev(m[0], m[4], m[8], m[12], q);
+        a[k].y = dot4_dev(m[1], m[5], m[9], m[13], q);
+        a[k].z = dot4_dev(m[2], m[6], m[10], m[14], q);
+        a[k].w = dot4_dev(m[3], m[7], m[11], m[15], q);
+        a[k].u = q[3];
+        a[k].v = q[4];
+    }
+    int n = clip_plane_dev(a, 3, b, 0);
+    n = clip_plane_dev(b, n, a, 1);
+    const float hw = __fmul_rn((float)W, 0.5f), hh = __fmul_rn((float)H, 0.5f);
+    for (int t = 0; t < 3; ++t) {
+        ScrTri s;
+        s.valid = 0;
+        bool ok = t + 2 < n;
+        const int idx[3] = {0, t + 1, t + 2};
+        for (int k = 0; k < 3 && ok; ++k) {
+            const ClipVtx& c = a[idx[k]];
+            if (!(c.w > 0.0f)) {
+                ok = false;
+                break;
+            }
+            s.sx[k] = __fadd_rn(__fmul_rn(__fdiv_rn(c.x, c.w), hw), hw);
+            s.sy[k] = __fadd_rn(__fmul_rn(__fdiv_rn(c.y, c.w), hh), hh);
+            s.sz[k] = __fdiv_rn(c.z, c.w);
+            s.iw[k] = __fdiv_rn(1.0f, c.w);
+            s.uw[k] = __fmul_rn(c.u, s.iw[k]);
+            s.vw[k] = __fmul_rn(c.v, s.iw[k]);
+        }
+        if (ok) {
+            s.area = edge_dev(s.sx[0], s.sy[0], s.sx[1], s.sy[1], s.sx[2], s.sy[2]);
+            ok = !(s.area == 0.0f || s.area != s.area);
+        }
+        if (ok) {
+            if (s.area < 0.0f) {
+                float* f[6] = {s.sx, s.sy, s.sz, s.iw, s.uw, s.vw};
+                for (int q = 0; q < 6; ++q) {
+                    const float x = f[q][1];
+                    f[q][1] = f[q][2];
+                    f[q][2] = x;
+                }
+                s.area = -s.area;
+            }
+            s.tl = top_left_dev(s.sx[1], s.sy[1], s.sx[2], s.sy[2]) | top_left_dev(s.sx[2], s.sy[2], s.sx[0], s.sy[0]) << 1 |
+                   top_left_dev(s.sx[0], s.sy[0], s.sx[1], s.sy[1]) << 2;
+            s.valid = 1;
+        }
+        tris[3 * p + t] = s;
+    }
+}
+
+__device__ __forceinline__ bool tri_cover_dev(const ScrTri& s, float fx, float fy, float (&l)[3]) {
+    const float w0 = edge_dev(s.sx[1], s.sy[1], s.sx[2], s.sy[2], fx, fy);
+    const float w1 = edge_dev(s.sx[2], s.sy[2], s.sx[0], s.sy[0], fx, fy);
+    const float w2 = edge_dev(s.sx[0], s.sy[0], s.sx[1], s.sy[1], fx, fy);
+    if (!inside_edge(w0, s.tl, 0) || !inside_edge(w1, s.tl, 1) || !inside_edge(w2, s.tl, 2)) return false;
+    l[0] = __fdiv_rn(w0, s.area);
+    l[1] = __fdiv_rn(w1, s.area);
+    l[2] = __fdiv_rn(w2, s.area);
+    return true;
+}
+
+// one warp per screen triangle: the lanes walk the pixels of its box
+__global__ void k_mesh_cover(const ScrTri* __restrict__ tris, long long n_slots, int W, int H,
+                             unsigned long long* __restrict__ key) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long sl = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < n_slots; sl += nwarps) {
+        const ScrTri& s = tris[sl];
+        if (!s.valid) continue;
+        const float xmin = fminf(fminf(s.sx[0], s.sx[1]), s.sx[2]), xmax = fmaxf(fmaxf(s.sx[0], s.sx[1]), s.sx[2]);
+        const float ymin = fminf(fminf(s.sy[0], s.sy[1]), s.sy[2]), ymax = fmaxf(fmaxf(s.sy[0], s.sy[1]), s.sy[2]);
+        const int x0 = max(0, floor_to_int_dev(xmin)), x1 = min(W - 1, floor_to_int_dev(ceilf(xmax)));
+        const int y0 = max(0, floor_to_int_dev(ymin)), y1 = min(H - 1, floor_to_int_dev(ceilf(ymax)));
+        if (x0 > x1 || y0 > y1) continue;
+        const long long bw = x1 - x0 + 1, npx = bw * (long long)(y1 - y0 + 1);
+        const uint32_t code = 0xFFFFFFFFu - (uint32_t)sl / 3u * 4u - (uint32_t)(sl % 3);
+        for (long long i = lane; i < npx; i += 32) {
+            const int px = x0 + (int)(i % bw), py = y0 + (int)(i / bw);
+            float l[3];
+            if (!tri_cover_dev(s, __fadd_rn((float)px, 0.5f), __fadd_rn((float)py, 0.5f), l)) continue;
+            const float z = lerp3(l[0], l[1], l[2], s.sz);
+            if (!(z >= 0.0f && z <= 1.0f)) continue;
+            const unsigned long long k = ((unsigned long long)__float_as_uint(z) << 32) | code;
+            atomicMin(key + (size_t)py * W + px, k);
+        }
+    }
+}
+
+__device__ __forceinline__ float clamp01_dev(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+__global__ void k_mesh_resolve(const MeshDrawDev* __restrict__ draws, int n_draws, const ScrTri* __restrict__ tris,
+                               const unsigned long long* __restrict__ key, const float* __restrict__ lut, int W, int H,
+                               float c0, float c1, float c2, float c3, float4* __restrict__ out) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= W || py >= H) return;
+    const unsigned long long k = key[(size_t)py * W + px];
+    if (k == ~0ull) {
+        out[(size_t)py * W + px] = make_float4(c0, c1, c2, c3);
+        return;
+    }
+    const uint32_t code = 0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFull);
+    const long long prim = code >> 2;
+    const int q = (int)(code & 3u);
+    const int d = find_draw(draws, n_draws, prim);
+    const MeshDrawDev& dr = draws[d];
+    const ScrTri& s = tris[3 * prim + q];
+    float l[3];
+    tri_cover_dev(s, __fadd_rn((float)px, 0.5f), __fadd_rn((float)py, 0.5f), l);
+    float r = dr.color[0], g = dr.color[1], b = dr.color[2], a = dr.color[3];
+    if (dr.material != FS3D_MAT_BASIC) {
+        const float den = lerp3(l[0], l[1], l[2], s.iw);
+        const float u = __fdiv_rn(lerp3(l[0], l[1], l[2], s.uw), den);
+        const float v = __fdiv_rn(lerp3(l[0], l[1], l[2], s.vw), den);
+        int ti = floor_to_int_dev(__fmul_rn(u, (float)dr.tex_w)) % dr.tex_w;
+        int tj = floor_to_int_dev(__fmul_rn(v, (float)dr.tex_h)) % dr.tex_h;
+        if (ti < 0) ti += dr.tex_w;
+        if (tj < 0) tj += dr.tex_h;
+        const uchar4 t = reinterpret_cast<const uchar4*>(dr.tex)[(size_t)tj * dr.tex_w + ti];
+        const float tr = lut[t.x], tg = lut[t.y], tb = lut[t.z];
+        if (dr.material == FS3D_MAT_TEXTURED) {
+            r = __fadd_rn(r, tr);
+            g = __fadd_rn(g, tg);
+            b = __fadd_rn(b, tb);
+            a = __fadd_rn(a, 1.0f);
+        } else {
+            r = tr;
+            g = tg;
+            b = tb;
+            a = 1.0f;
+        }
+    }
+    out[(size_t)py * W + px] = make_float4(clamp01_dev(r), clamp01_dev(g), clamp01_dev(b), clamp01_dev(a));
+}
+
 }  // namespace fs3d
 
 extern "C" {
@@ -285,3 +523,87 @@ fs3d_status fs3d_render_object(const fs3d_object_view* v, const float* tri_xyz, 
 }
 
 }  // extern "C"
+
+extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_mesh_draw* draws, int n_draws, int W,
+                                          int H, float* rgba_dev, void* stream) {
+    using namespace fs3d;
+    if (!v || (n_draws > 0 && !draws) || n_draws < 0 || n_draws > 4096 || !rgba_dev || W <= 0 || H <= 0)
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: bad args");
+    cudaStream_t st = (cudaStream_t)stream;
+    fs3d_object_view cam = *v;
+    for (int i = 0; i < 16; ++i) cam.model[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    float vp[16];
+    object_mvp(&cam, vp);
+    std::vector<MeshDrawDev> dd((size_t)(n_draws > 0 ? n_draws : 1));
+    long long prims = 0;
+    for (int d = 0; d < n_draws; ++d) {
+        const fs3d_mesh_draw& m = draws[d];
+        if (m.n_vertices < 0 || m.n_vertices % 3 || (m.n_vertices && !m.vertices) || m.material < FS3D_MAT_BASIC ||
+            m.material > FS3D_MAT_TEXTURE ||
+            (m.material != FS3D_MAT_BASIC && (!m.texture || m.tex_width <= 0 || m.tex_height <= 0)))
+            return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: bad draw");
+        // the kernels read the vertices and texels: they must be device or
+        // page-locked memory (used through its device alias), 4-byte aligned
+        const uint8_t* vdev = m.n_vertices ? device_view(m.vertices) : nullptr;
+        const uint8_t* tdev = m.material != FS3D_MAT_BASIC ? device_view(m.texture) : nullptr;
+        if ((m.n_vertices && (!vdev || (reinterpret_cast<uintptr_t>(vdev) & 3))) ||
+            (m.material != FS3D_MAT_BASIC && (!tdev || (reinterpret_cast<uintptr_t>(tdev) & 3))))
+            return set_error(FS3D_ERR_INVALID_ARG,
+                             "fs3d_render_meshes: vertices and textures must be 4-byte aligned device or page-locked memory");
+        MeshDrawDev& x = dd[(size_t)d];
+        mat4_mul(vp, m.model, x.mvp);
+        memcpy(x.color, m.color, sizeof(x.color));
+        x.verts = reinterpret_cast<const float*>(vdev);
+        x.tex = tdev;
+        x.tex_w = m.tex_width;
+        x.tex_h = m.tex_height;
+        x.material = m.material;
+        x.n_tri = m.n_vertices / 3;
+        x.prim0 = prims;
+        prims += x.n_tri;
+    }
+    if (prims >= (1ll << 30)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: too many triangles");
+    // sRGB texels to linear, as the sampler of an _SRGB format does
+    float lut[256];
+    for (int i = 0; i < 256; ++i) {
+        const double c = i / 255.0;
+        lut[i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+    }
+    const size_t draws_b = sizeof(MeshDrawDev) * dd.size(), lut_b = sizeof(lut);
+    const size_t tris_b = sizeof(ScrTri) * 3 * (size_t)(prims > 0 ? prims : 1), key_b = sizeof(unsigned long long) * W * H;
+    const size_t o_lut = (draws_b + 255) & ~(size_t)255, o_tris = (o_lut + lut_b + 255) & ~(size_t)255,
+                 o_key = (o_tris + tris_b + 255) & ~(size_t)255;
+    char* scratch = nullptr;
+    FS3D_CUDA(cudaMallocAsync((void**)&scratch, o_key + key_b, st));
+    MeshDrawDev* ddev = reinterpret_cast<MeshDrawDev*>(scratch);
+    float* lut_dev = reinterpret_cast<float*>(scratch + o_lut);
+    ScrTri* tris = reinterpret_cast<ScrTri*>(scratch + o_tris);
+    unsigned long long* key = reinterpret_cast<unsigned long long*>(scratch + o_key);
+    cudaError_t e = cudaMemcpyAsync(ddev, dd.data(), draws_b, cudaMemcpyHostToDevice, st);  // pageable: staged
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lut_dev, lut, lut_b, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(key, 0xFF, key_b, st);
+    fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_render_meshes upload");
+    if (s == FS3D_OK && prims > 0) {
+        k_mesh_setup<<<(unsigned)((prims + 127) / 128), 128, 0, st>>>(ddev, n_draws, prims, W, H, tris);
+        s = FS3D_OK;
+        if (cudaGetLastError() != cudaSuccess) s = set_error(FS3D_ERR_CUDA, "mesh setup launch");
+        if (s == FS3D_OK) {
+            const long long slots = 3 * prims, warps_per_block = 8;
+            long long blocks = (slots + warps_per_block - 1) / warps_per_block;
+            const long long cap = (long long)sm_count_public() * 16;
+            if (blocks > cap) blocks = cap;
+            k_mesh_cover<<<(unsigned)blocks, 256, 0, st>>>(tris, slots, W, H, key);
+            if (cudaGetLastError() != cudaSuccess) s = set_error(FS3D_ERR_CUDA, "mesh cover launch");
+        }
+        note_launch(2);
+    }
+    if (s == FS3D_OK) {
+        const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
+        k_mesh_resolve<<<grd, blk, 0, st>>>(ddev, n_draws, tris, key, lut_dev, W, H, v->clear[0], v->clear[1],
+                                            v->clear[2], v->clear[3], reinterpret_cast<float4*>(rgba_dev));
+        if (cudaGetLastError() != cudaSuccess) s = set_error(FS3D_ERR_CUDA, "mesh resolve launch");
+        note_launch(1);
+    }
+    cudaFreeAsync(scratch, st);
+    return s;
+}

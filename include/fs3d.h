@@ -304,6 +304,33 @@ int fs3d_mesh_cube(float* tri_xyz);
 fs3d_status fs3d_render_object(const fs3d_object_view* v, const float* tri_xyz, int ntri, int W, int H,
                                float* rgba_dev, void* stream);
 
+/* ---- mesh materials: basic_mat, textured_mat, tri ----
+ * Restates the scene's mesh pipelines (basic_mat.{vert,frag}: flat colour;
+ * textured_mat: colour + texel, alpha colour.a + 1; tri: texel, alpha 1) with
+ * the state they are drawn with: no culling, depth LESS_OR_EQUAL against 1
+ * (later draws win ties), one sample per pixel, NEAREST filtering with REPEAT
+ * addressing of sRGB texels (decoded to linear), triangles clipped against
+ * the depth range 0 <= z <= w, texture coordinates interpolated
+ * perspective-correctly, the result clamped to [0,1] as the attachment stores
+ * it.  Camera and projection from `view` (its model is ignored; each draw has
+ * its own).  W*H RGBA float32 into device memory, async on `stream`; the same
+ * frame as the CPU restatement bit for bit. */
+#define FS3D_MAT_BASIC 0
+#define FS3D_MAT_TEXTURED 1
+#define FS3D_MAT_TEXTURE 2
+typedef struct fs3d_mesh_draw {
+    const float* vertices;  /* n_vertices x {x, y, z, u, v} (three per triangle), device or page-locked */
+    int n_vertices;         /* a multiple of 3                                           */
+    int material;           /* FS3D_MAT_*                                                */
+    float model[16];        /* column-major                                              */
+    float color[4];         /* the material's colour (BASIC, TEXTURED)                   */
+    const uint8_t* texture; /* RGBA8 texels, row-major, sRGB; device or page-locked      */
+    int tex_width, tex_height;
+} fs3d_mesh_draw;
+/* n_draws <= 4096, fewer than 2^30 triangles in all */
+fs3d_status fs3d_render_meshes(const fs3d_object_view* view, const fs3d_mesh_draw* draws, int n_draws, int W, int H,
+                               float* rgba_dev, void* stream);
+
 /* ---- synthetic worlds (seeded, bit-reproducible) ---- */
 fs3d_status fs3d_gen_parity(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);
 fs3d_status fs3d_gen_pillars(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);

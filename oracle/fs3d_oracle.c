@@ -814,3 +814,244 @@ int orc_mesh_cube(float* tri) {
         for (int k = 0; k < 3; ++k) memcpy(tri + 9 * t + 3 * k, vtx[face[t][k] - 1], 3 * sizeof(float));
     return 12;
 }
+
+/* ---- mesh materials basic_mat / textured_mat / tri --------------------------
+ * Restates basic_mat.{vert,frag}, textured_mat.{vert,frag} and tri.{vert,frag}
+ * with the fixed-function state the pipelines set (no culling, depth
+ * LESS_OR_EQUAL against 1, one sample per pixel, NEAREST filtering with
+ * REPEAT addressing, R8G8B8A8_SRGB textures: materials.cpp:438,
+ * initializers.cpp:49-58, pipelines.cpp:114,131, renderer.cpp:1233).
+ * Stages: clip = P*V*model*(x,y,z,1); Sutherland-Hodgman clipping of each
+ * triangle against 0 <= z <= w (Vulkan's depth range), fan triangulation;
+ * screen position (x/w, y/w) to pixels, depth z/w; coverage by edge functions
+ * at pixel centres with the top-left rule; per pixel the nearest fragment,
+ * ties going to the later primitive; texture coordinates interpolated
+ * perspective-correctly; texel i = floor(u*width) wrapped (likewise v);
+ * sRGB-decoded through a 256-entry table; the result clamped to [0,1] as the
+ * 8-bit attachment stores it. */
+void orc_srgb_table(float* lut) {
+    for (int i = 0; i < 256; ++i) {
+        const double c = i / 255.0;
+        lut[i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+    }
+}
+
+/* floor to int, saturating, NaN -> 0 (the same on every platform) */
+static int floor_to_int(float x) {
+    if (x != x) return 0;
+    x = floorf(x);
+    if (x >= 2147483647.0f) return 2147483647;
+    if (x <= -2147483648.0f) return -2147483647 - 1;
+    return (int)x;
+}
+
+typedef struct {
+    float x, y, z, w, u, v;
+} clip_vtx;
+
+static clip_vtx clip_lerp(const clip_vtx* a, const clip_vtx* b, float t) {
+    clip_vtx r;
+    r.x = a->x + t * (b->x - a->x);
+    r.y = a->y + t * (b->y - a->y);
+    r.z = a->z + t * (b->z - a->z);
+    r.w = a->w + t * (b->w - a->w);
+    r.u = a->u + t * (b->u - a->u);
+    r.v = a->v + t * (b->v - a->v);
+    return r;
+}
+
+/* keeps the part with d >= 0, d = z (plane 0) or w - z (plane 1) */
+static int clip_plane(const clip_vtx* in, int n, clip_vtx* out, int plane) {
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        const clip_vtx* a = &in[i];
+        const clip_vtx* b = &in[(i + 1) % n];
+        const float da = plane ? a->w - a->z : a->z, db = plane ? b->w - b->z : b->z;
+        if (da >= 0.0f) out[m++] = *a;
+        if ((da >= 0.0f) != (db >= 0.0f)) out[m++] = clip_lerp(a, b, da / (da - db));
+    }
+    return m;
+}
+
+/* screen triangle: positions, depth, 1/w and u/w, v/w per vertex */
+typedef struct {
+    float sx[3], sy[3], sz[3], iw[3], uw[3], vw[3];
+    float area;
+    int tl;
+    int valid;
+} scr_tri;
+
+/* up to three screen triangles of primitive p (vertices v: 3 x {x,y,z,u,v}) */
+static void setup_prim(const float* mvp, const float* v, int W, int H, scr_tri* out) {
+    clip_vtx a[8], b[8];
+    for (int k = 0; k < 3; ++k) {
+        const float* p = v + 5 * k;
+        a[k].x = mvp[0] * p[0] + mvp[4] * p[1] + mvp[8] * p[2] + mvp[12];
+        a[k].y = mvp[1] * p[0] + mvp[5] * p[1] + mvp[9] * p[2] + mvp[13];
+        a[k].z = mvp[2] * p[0] + mvp[6] * p[1] + mvp[10] * p[2] + mvp[14];
+        a[k].w = mvp[3] * p[0] + mvp[7] * p[1] + mvp[11] * p[2] + mvp[15];
+        a[k].u = p[3];
+        a[k].v = p[4];
+    }
+    int n = clip_plane(a, 3, b, 0);
+    n = clip_plane(b, n, a, 1);
+    const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+    for (int t = 0; t < 3; ++t) {
+        scr_tri* s = &out[t];
+        s->valid = 0;
+        if (t + 2 >= n) continue;
+        const int idx[3] = {0, t + 1, t + 2};
+        for (int k = 0; k < 3; ++k) {
+            const clip_vtx* c = &a[idx[k]];
+            if (!(c->w > 0.0f)) goto next;
+            s->sx[k] = (c->x / c->w) * hw + hw;
+            s->sy[k] = (c->y / c->w) * hh + hh;
+            s->sz[k] = c->z / c->w;
+            s->iw[k] = 1.0f / c->w;
+            s->uw[k] = c->u * s->iw[k];
+            s->vw[k] = c->v * s->iw[k];
+        }
+        s->area = edge_fn((float[]){s->sx[0], s->sy[0]}, (float[]){s->sx[1], s->sy[1]}, s->sx[2], s->sy[2]);
+        if (s->area == 0.0f || s->area != s->area) continue;
+        if (s->area < 0.0f) {
+            float* f[6] = {s->sx, s->sy, s->sz, s->iw, s->uw, s->vw};
+            for (int q = 0; q < 6; ++q) {
+                const float x = f[q][1];
+                f[q][1] = f[q][2];
+                f[q][2] = x;
+            }
+            s->area = -s->area;
+        }
+        s->tl = top_left((float[]){s->sx[1], s->sy[1]}, (float[]){s->sx[2], s->sy[2]}) |
+                top_left((float[]){s->sx[2], s->sy[2]}, (float[]){s->sx[0], s->sy[0]}) << 1 |
+                top_left((float[]){s->sx[0], s->sy[0]}, (float[]){s->sx[1], s->sy[1]}) << 2;
+        s->valid = 1;
+    next:;
+    }
+}
+
+/* barycentric weights of pixel centre (fx, fy); 0 if not covered */
+static int tri_cover(const scr_tri* s, float fx, float fy, float* l) {
+    const float w0 = edge_fn((float[]){s->sx[1], s->sy[1]}, (float[]){s->sx[2], s->sy[2]}, fx, fy);
+    const float w1 = edge_fn((float[]){s->sx[2], s->sy[2]}, (float[]){s->sx[0], s->sy[0]}, fx, fy);
+    const float w2 = edge_fn((float[]){s->sx[0], s->sy[0]}, (float[]){s->sx[1], s->sy[1]}, fx, fy);
+    if (!(w0 > 0.0f || (w0 == 0.0f && (s->tl & 1)))) return 0;
+    if (!(w1 > 0.0f || (w1 == 0.0f && (s->tl & 2)))) return 0;
+    if (!(w2 > 0.0f || (w2 == 0.0f && (s->tl & 4)))) return 0;
+    l[0] = w0 / s->area;
+    l[1] = w1 / s->area;
+    l[2] = w2 / s->area;
+    return 1;
+}
+
+static float clamp01(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+int orc_render_meshes(const orc_object_view* view, const orc_mesh_draw* draws, int n_draws, int W, int H,
+                      float* rgba) {
+    float lut[256];
+    orc_srgb_table(lut);
+    orc_object_view cam = *view;
+    for (int i = 0; i < 16; ++i) cam.model[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    float vp[16];
+    orc_object_mvp(&cam, vp);
+    const size_t npx = (size_t)W * H;
+    uint64_t* key = (uint64_t*)malloc(npx * sizeof(uint64_t));
+    if (!key) return -1;
+    for (size_t i = 0; i < npx; ++i) key[i] = ~0ull;
+    /* pass 1: nearest fragment per pixel, keyed (depth, primitive) */
+    int64_t prim0 = 0;
+    for (int d = 0; d < n_draws; ++d) {
+        float mvp[16];
+        mat4_mul(vp, draws[d].model, mvp);
+        const int nt = draws[d].n_vertices / 3;
+        for (int t = 0; t < nt; ++t) {
+            scr_tri st[3];
+            setup_prim(mvp, draws[d].vertices + 15 * t, W, H, st);
+            const uint32_t prim = (uint32_t)(prim0 + t);
+            for (int q = 0; q < 3; ++q) {
+                if (!st[q].valid) continue;
+                float xmin = st[q].sx[0], xmax = xmin, ymin = st[q].sy[0], ymax = ymin;
+                for (int k = 1; k < 3; ++k) {
+                    xmin = fminf(xmin, st[q].sx[k]);
+                    xmax = fmaxf(xmax, st[q].sx[k]);
+                    ymin = fminf(ymin, st[q].sy[k]);
+                    ymax = fmaxf(ymax, st[q].sy[k]);
+                }
+                int x0 = floor_to_int(xmin), x1 = floor_to_int(ceilf(xmax));
+                int y0 = floor_to_int(ymin), y1 = floor_to_int(ceilf(ymax));
+                x0 = x0 < 0 ? 0 : x0;
+                y0 = y0 < 0 ? 0 : y0;
+                x1 = x1 > W - 1 ? W - 1 : x1;
+                y1 = y1 > H - 1 ? H - 1 : y1;
+                for (int py = y0; py <= y1; ++py)
+                    for (int px = x0; px <= x1; ++px) {
+                        float l[3];
+                        if (!tri_cover(&st[q], (float)px + 0.5f, (float)py + 0.5f, l)) continue;
+                        const float z = l[0] * st[q].sz[0] + l[1] * st[q].sz[1] + l[2] * st[q].sz[2];
+                        if (!(z >= 0.0f && z <= 1.0f)) continue;
+                        uint32_t zb;
+                        memcpy(&zb, &z, 4);
+                        const uint64_t k = ((uint64_t)zb << 32) | (uint64_t)(0xFFFFFFFFu - (prim * 4u + (uint32_t)q));
+                        size_t i = (size_t)py * W + px;
+                        if (k < key[i]) key[i] = k;
+                    }
+            }
+        }
+        prim0 += nt;
+    }
+    /* pass 2: shade the winners */
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            float* out = rgba + 4 * ((size_t)py * W + px);
+            const uint64_t k = key[(size_t)py * W + px];
+            if (k == ~0ull) {
+                memcpy(out, view->clear, 4 * sizeof(float));
+                continue;
+            }
+            const uint32_t code = 0xFFFFFFFFu - (uint32_t)(k & 0xFFFFFFFFu);
+            const uint32_t prim = code >> 2, q = code & 3u;
+            int d = 0;
+            int64_t base = 0;
+            while (prim >= base + draws[d].n_vertices / 3) {
+                base += draws[d].n_vertices / 3;
+                ++d;
+            }
+            float mvp[16];
+            mat4_mul(vp, draws[d].model, mvp);
+            scr_tri st[3];
+            setup_prim(mvp, draws[d].vertices + 15 * (prim - base), W, H, st);
+            float l[3];
+            tri_cover(&st[q], (float)px + 0.5f, (float)py + 0.5f, l);
+            const orc_mesh_draw* dr = &draws[d];
+            float r = dr->color[0], g = dr->color[1], b = dr->color[2], a = dr->color[3];
+            if (dr->material != ORC_MAT_BASIC) {
+                const float den = l[0] * st[q].iw[0] + l[1] * st[q].iw[1] + l[2] * st[q].iw[2];
+                const float u = (l[0] * st[q].uw[0] + l[1] * st[q].uw[1] + l[2] * st[q].uw[2]) / den;
+                const float v = (l[0] * st[q].vw[0] + l[1] * st[q].vw[1] + l[2] * st[q].vw[2]) / den;
+                int ti = floor_to_int(u * (float)dr->tex_width), tj = floor_to_int(v * (float)dr->tex_height);
+                ti %= dr->tex_width;
+                if (ti < 0) ti += dr->tex_width;
+                tj %= dr->tex_height;
+                if (tj < 0) tj += dr->tex_height;
+                const uint8_t* tx = dr->texture + 4 * ((size_t)tj * dr->tex_width + ti);
+                const float tr = lut[tx[0]], tg = lut[tx[1]], tb = lut[tx[2]];
+                if (dr->material == ORC_MAT_TEXTURED) {
+                    r += tr;
+                    g += tg;
+                    b += tb;
+                    a += 1.0f;
+                } else {
+                    r = tr;
+                    g = tg;
+                    b = tb;
+                    a = 1.0f;
+                }
+            }
+            out[0] = clamp01(r);
+            out[1] = clamp01(g);
+            out[2] = clamp01(b);
+            out[3] = clamp01(a);
+        }
+    free(key);
+    return 0;
+}

@@ -95,6 +95,26 @@ void orc_object_mvp(const orc_object_view* v, float* mvp);
 int orc_render_object(const orc_object_view* v, const float* tri, int ntri, int W, int H, float* rgba);
 int orc_mesh_cube(float* tri /* 108 floats */);
 
+/* mesh materials basic_mat / textured_mat / tri: triangle meshes rasterised
+ * with depth test, perspective-correct texture coordinates, nearest sRGB
+ * texels with repeat addressing */
+#define ORC_MAT_BASIC 0
+#define ORC_MAT_TEXTURED 1
+#define ORC_MAT_TEXTURE 2
+typedef struct {
+    const float* vertices; /* n_vertices x {x, y, z, u, v}, three per triangle */
+    int n_vertices;
+    int material;
+    float model[16];
+    float color[4];
+    const uint8_t* texture; /* RGBA8, row-major, sRGB */
+    int tex_width, tex_height;
+} orc_mesh_draw;
+void orc_srgb_table(float* lut /* 256 */);
+/* the camera of `view` (its model is ignored); 0, or -1 on allocation failure */
+int orc_render_meshes(const orc_object_view* view, const orc_mesh_draw* draws, int n_draws, int W, int H,
+                      float* rgba);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,11 @@ def scene_view(**kw) -> ObjectView:
     return v
 
 
+class MeshDraw(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("n_vertices", C.c_int), ("material", C.c_int), ("model", C.c_float * 16),
+                ("color", C.c_float * 4), ("texture", C.c_void_p), ("tex_width", C.c_int), ("tex_height", C.c_int)]
+
+
 class Camera(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
                 ("up", C.c_float * 3), ("tan_half_fov", C.c_float), ("aspect", C.c_float),
@@ -69,6 +74,8 @@ class Oracle:
             "orc_render_object": (i32, [C.POINTER(ObjectView), vp, i32, i32, i32, vp]),
             "orc_object_mvp": (None, [C.POINTER(ObjectView), vp]),
             "orc_mesh_cube": (i32, [vp]),
+            "orc_render_meshes": (i32, [C.POINTER(ObjectView), C.POINTER(MeshDraw), i32, i32, i32, vp]),
+            "orc_srgb_table": (None, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -151,6 +158,31 @@ class Oracle:
         img = np.empty((H, W, 4), np.float32)
         rc = self.L.orc_render_object(C.byref(view), tri.ctypes.data, tri.shape[0], W, H, img.ctypes.data)
         return img if rc == 0 else None
+
+    def render_meshes(self, view: ObjectView, draws, W: int, H: int) -> np.ndarray:
+        """draws: dicts with vertices (n x 5 float32), material, model (4x4 row-major), color, texture
+        (h x w x 4 uint8)."""
+        keep, arr = [], (MeshDraw * max(len(draws), 1))()
+        for i, d in enumerate(draws):
+            v = np.ascontiguousarray(d["vertices"], np.float32)
+            keep.append(v)
+            m = arr[i]
+            m.vertices, m.n_vertices, m.material = v.ctypes.data, v.shape[0], d.get("material", 0)
+            m.model[:] = [float(x) for x in np.asarray(d.get("model", np.eye(4)), np.float32).T.reshape(-1)]
+            m.color[:] = [float(c) for c in d.get("color", (1, 1, 1, 1))]
+            tex = d.get("texture")
+            if tex is not None:
+                tex = np.ascontiguousarray(tex, np.uint8)
+                keep.append(tex)
+                m.texture, m.tex_width, m.tex_height = tex.ctypes.data, tex.shape[1], tex.shape[0]
+        img = np.empty((H, W, 4), np.float32)
+        assert self.L.orc_render_meshes(C.byref(view), arr, len(draws), W, H, img.ctypes.data) == 0
+        return img
+
+    def srgb_table(self) -> np.ndarray:
+        t = np.empty(256, np.float32)
+        self.L.orc_srgb_table(t.ctypes.data)
+        return t
 
     def render_dda(self, g: np.ndarray, cam: Camera, W: int, H: int) -> np.ndarray:
         Y, Z, X = g.shape

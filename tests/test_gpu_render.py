@@ -130,3 +130,67 @@ def test_dda_after_steps_of_a_large_world(fs3d, orc):
             cur = w.read()
             for c in (cam, low):
                 check_img(w.render(c, W, H), orc.render_dda(cur, oracle_lib.camera_from(c), W, H))
+
+
+def _mesh_scene(fs3d, orc, cuda, n_cubes=10, seed=3):
+    """A few cubes with every material, as (gpu draws, oracle draws, tensors to keep)."""
+    rng = np.random.default_rng(seed)
+    v = orc.mesh_cube().reshape(-1, 3)
+    cube = np.c_[v, (v[:, :2] + 1) * rng.uniform(0.5, 3.0)].astype(np.float32)
+    tex = rng.integers(0, 256, (32, 24, 4), dtype=np.uint8)
+    dv, dt = cuda.from_numpy(cube).cuda(), cuda.from_numpy(tex).cuda()
+    gpu, cpu = [], []
+    for i in range(n_cubes):
+        m = np.eye(4)
+        a = rng.uniform(0, 2 * np.pi)
+        m[:3, :3] = [[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]]
+        m[:3, :3] *= rng.uniform(0.2, 0.7)
+        m[:3, 3] = rng.uniform(-2.5, 2.5, 3)
+        mat = i % 3
+        col = tuple(rng.uniform(0, 1, 4))
+        gpu.append(fs3d.mesh_draw(dv.data_ptr(), cube.shape[0], mat, m, col,
+                                  dt.data_ptr() if mat else 0, tex.shape[1], tex.shape[0]))
+        cpu.append(dict(vertices=cube, material=mat, model=m, color=col, texture=tex if mat else None))
+    return gpu, cpu, (dv, dt)
+
+
+@pytest.mark.parametrize("case", [("scene", {}, (850, 450)), ("turned", {"rot_y": 35.0}, (1920, 1080)),
+                                  ("odd", {"cam_pos": (0.3, -0.2, -3.0)}, (333, 217)),
+                                  ("inside", {"cam_pos": (0.0, 0.0, 0.0), "rot_y": 20.0}, (320, 180))],
+                         ids=lambda c: c[0])
+def test_mesh_materials_match_cpu_bit_exact(fs3d, orc, cuda, case):
+    _, kw, (W, H) = case
+    gpu, cpu, keep = _mesh_scene(fs3d, orc, cuda)
+    if case[0] == "inside":  # one big cube around the camera, textured, plus the small ones
+        big = np.eye(4) * 3.0
+        big[3, 3] = 1.0
+        gpu.append(fs3d.mesh_draw(gpu[1].vertices, 36, fs3d.MAT_TEXTURE, big, (1, 1, 1, 1), gpu[1].texture,
+                                  gpu[1].tex_width, gpu[1].tex_height))
+        cpu.append(dict(cpu[1], model=big, material=2))
+    out = cuda.full((H, W, 4), -1.0, dtype=cuda.float32, device="cuda")
+    fs3d.render_meshes_device(fs3d.object_view_scene(**kw), gpu, W, H, out.data_ptr(),
+                              cuda.cuda.current_stream().cuda_stream)
+    got = out.cpu().numpy()
+    exp = orc.render_meshes(oracle_lib.scene_view(**kw), cpu, W, H)
+    if not np.array_equal(got, exp):
+        d = np.argwhere((got != exp).any(-1))
+        y, x = d[0]
+        pytest.fail(f"{len(d)} pixels differ; first (x={x}, y={y}): got {got[y, x]} expected {exp[y, x]}")
+    assert ((got != [0, 0, 1, 1]).any(-1)).mean() > 0.01
+    del keep
+
+
+def test_mesh_pinned_vertices_and_pageable_rejected(fs3d, orc, cuda):
+    v = orc.mesh_cube().reshape(-1, 3)
+    cube = np.c_[v, np.zeros((36, 2))].astype(np.float32)
+    pinned = cuda.from_numpy(cube).pin_memory()
+    W, H = 128, 72
+    out = cuda.empty((H, W, 4), dtype=cuda.float32, device="cuda")
+    view = fs3d.object_view_scene(rot_y=10.0)
+    fs3d.render_meshes_device(view, [fs3d.mesh_draw(pinned.data_ptr(), 36, fs3d.MAT_BASIC, None, (0, 1, 0, 1))],
+                              W, H, out.data_ptr(), cuda.cuda.current_stream().cuda_stream)
+    exp = orc.render_meshes(oracle_lib.scene_view(rot_y=10.0), [dict(vertices=cube, color=(0, 1, 0, 1))], W, H)
+    assert np.array_equal(out.cpu().numpy(), exp)
+    with pytest.raises(fs3d.Fs3dError) as e:
+        fs3d.render_meshes_device(view, [fs3d.mesh_draw(cube.ctypes.data, 36)], W, H, out.data_ptr())
+    assert e.value.status == fs3d.ERR_INVALID_ARG

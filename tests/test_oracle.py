@@ -324,3 +324,93 @@ def test_object_render_translation_equivalence_and_rejections(orc):
     assert np.array_equal(a, b)
     assert orc.render_object(oracle_lib.scene_view(cam_pos=(0.0, 0.0, -1.0)), tri, 64, 32) is None  # eye in the cube
     assert orc.render_object(oracle_lib.scene_view(model=np.zeros((4, 4))), tri, 64, 32) is None
+
+
+# ---- mesh materials (rasterised triangles, depth test, textures)
+
+def _cube_uv(orc):
+    v = orc.mesh_cube().reshape(-1, 3)
+    return np.c_[v, (v[:, :2] + 1) * 0.5].astype(np.float32)
+
+
+def _rays(orc, view, W, H):
+    inv = np.linalg.inv(orc.object_mvp(view).astype(np.float64))
+    px, py = np.meshgrid(np.arange(W) + 0.5, np.arange(H) + 0.5)
+    p = [np.stack([px / (W / 2) - 1, py / (H / 2) - 1, np.full_like(px, z), np.ones_like(px)], -1) @ inv.T
+         for z in (0.3, 0.9)]
+    a, b = (q[..., :3] / q[..., 3:] for q in p)
+    return a, b - a
+
+
+@pytest.mark.parametrize("rot", [0.0, 25.0, -60.0])
+def test_mesh_basic_coverage_matches_analytic(orc, rot):
+    view = oracle_lib.scene_view(rot_y=rot)
+    W, H = 320, 180
+    img = orc.render_meshes(view, [dict(vertices=_cube_uv(orc), material=0, color=(1, 0, 0, 1))], W, H)
+    o, d = _rays(orc, view, W, H)
+    cov = _ray_box(o, d, 1.0)
+    got = img[..., 2] != 1
+    assert (got != cov).sum() <= 2e-3 * cov.sum() + 2
+    assert (img[got][:, 0] == 1).all() and (img[~got] == [0, 0, 1, 1]).all()
+
+
+def test_mesh_camera_inside_cube_is_clipped(orc):
+    """Triangles crossing the near plane are clipped, not dropped: from the
+    cube's centre every pixel sees a face."""
+    img = orc.render_meshes(oracle_lib.scene_view(cam_pos=(0.0, 0.0, 0.0), rot_y=33.0),
+                            [dict(vertices=_cube_uv(orc), material=0, color=(0, 1, 0, 1))], 160, 90)
+    assert (img[..., 1] == 1).all()
+
+
+@pytest.mark.parametrize("rot", [0.0, 40.0])
+def test_mesh_texture_perspective_correct(orc, rot):
+    """A textured quad, head-on and turned: the texel of each pixel equals the
+    one a float64 ray-plane intersection gives (nearest, repeat), except for
+    pixels within 1e-3 texel of a texel boundary."""
+    rng = np.random.default_rng(5)
+    tex = rng.integers(0, 256, (16, 16, 4), dtype=np.uint8)
+    quad = np.array([[-1, -1, 0, 0, 0], [1, -1, 0, 2, 0], [1, 1, 0, 2, 2],
+                     [-1, -1, 0, 0, 0], [1, 1, 0, 2, 2], [-1, 1, 0, 0, 2]], np.float32)  # uv 0..2: repeats
+    c, s = np.cos(np.radians(rot)), np.sin(np.radians(rot))
+    model = np.array([[c, 0, s, 0], [0, 1, 0, 0], [-s, 0, c, 0], [0, 0, 0, 1]], np.float64)
+    view = oracle_lib.scene_view(cam_pos=(0.0, 0.0, -2.5))
+    W, H = 256, 144
+    img = orc.render_meshes(view, [dict(vertices=quad, material=2, texture=tex, model=model)], W, H)
+    o, d = _rays(orc, view, W, H)
+    n = model[:3, :3] @ [0, 0, 1.0]
+    t = -(o @ n) / (d @ n)
+    hit = o + t[..., None] * d
+    local = hit @ model[:3, :3]  # back to object space (orthonormal)
+    inside = (np.abs(local[..., 0]) <= 1) & (np.abs(local[..., 1]) <= 1) & (t > 0)
+    u, v = (local[..., 0] + 1), (local[..., 1] + 1)  # 0..2
+    fu, fv = u * 16, v * 16
+    sure = inside & (np.abs(fu - np.round(fu)) > 1e-3) & (np.abs(fv - np.round(fv)) > 1e-3)
+    sure &= (np.abs(local[..., 0]) < 0.999) & (np.abs(local[..., 1]) < 0.999)
+    ti, tj = np.floor(fu).astype(int) % 16, np.floor(fv).astype(int) % 16
+    lut = orc.srgb_table()
+    exp = lut[tex[tj, ti, 0]]
+    assert sure.sum() > 1000
+    assert (img[..., 0][sure] == exp[sure]).mean() > 0.995
+    assert (img[..., 3][inside] == 1).all()
+
+
+def test_mesh_depth_ties_and_materials(orc):
+    """Coplanar quads: the later draw wins (LESS_OR_EQUAL); a farther one is
+    hidden; textured_mat adds the colour to the texel and 1 to alpha (the
+    attachment clamps to [0,1])."""
+    quad = np.array([[-1, -1, 0, 0, 0], [1, -1, 0, 1, 0], [1, 1, 0, 1, 1],
+                     [-1, -1, 0, 0, 0], [1, 1, 0, 1, 1], [-1, 1, 0, 0, 1]], np.float32)
+    back = quad.copy()
+    back[:, 2] = -0.5
+    tex = np.full((2, 2, 4), 128, np.uint8)
+    view = oracle_lib.scene_view()
+    W, H = 160, 90
+    img = orc.render_meshes(view, [dict(vertices=quad, material=0, color=(1, 0, 0, 1)),
+                                   dict(vertices=quad, material=1, color=(0.1, 0.2, 0.3, 0.5), texture=tex),
+                                   dict(vertices=back, material=0, color=(0, 0, 0, 1))], W, H)
+    cov = img[..., 2] != 1
+    cov &= ~((img[..., 0] == 0) & (img[..., 1] == 0) & (img[..., 2] == 1))
+    lut = orc.srgb_table()
+    exp = np.float32([0.1, 0.2, 0.3]) + lut[128]
+    assert cov.sum() > 500
+    assert np.allclose(img[cov][:, :3], exp, atol=0) and (img[cov][:, 3] == 1).all()
