@@ -423,6 +423,9 @@ def run_fs3d(args):
     if not args.skip_large:
         large = run_large(fs3d, torch, dev, args)
 
+    # ---- mesh materials: the upstream cube-grid scene
+    mesh = None if args.skip_large else run_mesh(fs3d, torch, args)
+
     # ---- roofline of the dominant work: the segment graph, whose time is the
     # resident kernels (one launch per size class steps its worlds 64 times in
     # shared memory).  Algorithmic bytes = the 2-bit state read and written by
@@ -477,7 +480,7 @@ def run_fs3d(args):
                 "processed": {"voxel_updates_per_s": value * proc_frac, "fraction_of_dense": round(proc_frac, 4),
                               "note": "value counts every cell of every world each step (dense-equivalent); "
                                       "this counts the cell-steps the kernels evaluated"},
-                "plain_512": p512, "served": served, "large_render": large, "parity": parity,
+                "plain_512": p512, "served": served, "large_render": large, "mesh_render": mesh, "parity": parity,
                 "segment_ms": [round(x, 4) for x in seg_ms]}
         print(json.dumps(line))
     if world > 1:
@@ -530,6 +533,49 @@ def run_large(fs3d, torch, dev, args, X=1024, Y=1024, Z=1024, W=1920, H=1080):
             "mass_conserved": bool((counts == counts0).all())}
 
 
+def run_mesh(fs3d, torch, args, W=1920, H=1080, frames=20):
+    """The cube-grid scene of the upstream renderer (renderer.cpp:1328-1352):
+    51 x 51 green cubes (basic_mat) at y = 0 and 51 x 51 red textured cubes
+    (textured_mat) at y = 5, each 0.2 in scale, one draw per cube; a seeded
+    512 x 512 texture stands in for the texture file.  Frame time with CUDA
+    events; the last frame checked against the CPU restatement."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    f = fs3d.mesh_cube().reshape(-1, 3)
+    cube = np.c_[f, (f[:, [0, 2]] + 1) * 0.5].astype(np.float32)
+    rng = np.random.default_rng(2024)
+    tex = rng.integers(0, 256, (512, 512, 4), dtype=np.uint8)
+    dv, dt = torch.from_numpy(cube).cuda(), torch.from_numpy(tex).cuda()
+    gpu, cpu = [], []
+    for y, mat, col in ((0.0, fs3d.MAT_BASIC, (0.0, 1.0, 0.0, 1.0)), (5.0, fs3d.MAT_TEXTURED, (1.0, 0.0, 0.0, 1.0))):
+        for x in range(-25, 26):
+            for z in range(-25, 26):
+                m = np.diag([0.2, 0.2, 0.2, 1.0])
+                m[:3, 3] = (x, y, z)
+                gpu.append(fs3d.mesh_draw(dv.data_ptr(), 36, mat, m, col, dt.data_ptr() if mat else 0, 512, 512))
+                cpu.append(dict(vertices=cube, material=mat, model=m, color=col, texture=tex if mat else None))
+    kw = dict(cam_pos=(0.0, -4.0, -32.0), rot_y=0.0)
+    view = fs3d.object_view_scene(**kw)
+    gpu = fs3d.mesh_draws(gpu)
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    for _ in range(3):
+        fs3d.render_meshes_device(view, gpu, W, H, out.data_ptr(), st.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(frames):
+        fs3d.render_meshes_device(view, gpu, W, H, out.data_ptr(), st.cuda_stream)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / frames
+    exp = oracle_lib.load().render_meshes(oracle_lib.scene_view(**kw), cpu, W, H)
+    got = out.cpu().numpy()
+    return {"workload": f"{len(gpu)} cube draws ({12 * len(gpu)} triangles, basic_mat and textured_mat) at {W}x{H}",
+            "frame_us": round(ms * 1e3, 1), "triangles_per_s": 12 * len(gpu) / (ms / 1e3),
+            "pixels_covered": int((got != np.float32([0, 0, 1, 1])).any(-1).sum()),
+            "bit_exact_vs_cpu": bool(np.array_equal(got, exp))}
+
+
 def run_only(args):
     """One workload without the side measurements, for ncu captures:
     `batched` runs warmup + steps segments of the 2048-world pool, `plain512`
@@ -541,6 +587,9 @@ def run_only(args):
     if args.only == "large":
         out = run_large(fs3d, torch, torch.device("cuda", 0), args)
         print(json.dumps({"only": args.only, "ok": True, "large_render": out}))
+        return 0
+    if args.only == "mesh":
+        print(json.dumps({"only": args.only, "ok": True, "mesh_render": run_mesh(fs3d, torch, args)}))
         return 0
     if args.only == "batched":
         worlds = batch_worlds(fs3d, args.master, args.worlds)
@@ -583,7 +632,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -302,9 +302,15 @@ def mesh_draw(vertices_ptr: int, n_vertices: int, material: int = MAT_BASIC, mod
     return d
 
 
+def mesh_draws(draws) -> C.Array:
+    """A ctypes array of MeshDraw, to pass to render_meshes_device frame after frame."""
+    return (MeshDraw * max(len(draws), 1))(*draws)
+
+
 def render_meshes_device(view: ObjectView, draws, W: int, H: int, rgba_ptr: int, stream: int = 0) -> None:
-    """The basic_mat / textured_mat / tri materials over the given draws into W*H RGBA float32."""
-    arr = (MeshDraw * max(len(draws), 1))(*draws)
+    """The basic_mat / textured_mat / tri materials over the given draws (a list of
+    MeshDraw, or the array mesh_draws built) into W*H RGBA float32."""
+    arr = draws if isinstance(draws, C.Array) else mesh_draws(draws)
     check(lib().fs3d_render_meshes(C.byref(view), arr, len(draws), W, H, rgba_ptr, stream))
 
 

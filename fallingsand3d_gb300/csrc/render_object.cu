@@ -527,7 +527,7 @@ fs3d_status fs3d_render_object(const fs3d_object_view* v, const float* tri_xyz, 
 extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_mesh_draw* draws, int n_draws, int W,
                                           int H, float* rgba_dev, void* stream) {
     using namespace fs3d;
-    if (!v || (n_draws > 0 && !draws) || n_draws < 0 || n_draws > 4096 || !rgba_dev || W <= 0 || H <= 0)
+    if (!v || (n_draws > 0 && !draws) || n_draws < 0 || n_draws > 65536 || !rgba_dev || W <= 0 || H <= 0)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: bad args");
     cudaStream_t st = (cudaStream_t)stream;
     fs3d_object_view cam = *v;
@@ -536,6 +536,11 @@ extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_
     object_mvp(&cam, vp);
     std::vector<MeshDrawDev> dd((size_t)(n_draws > 0 ? n_draws : 1));
     long long prims = 0;
+    // draws usually share their buffers: look each distinct pointer up once
+    const void* last_v = nullptr;
+    const void* last_t = nullptr;
+    const uint8_t* last_vdev = nullptr;
+    const uint8_t* last_tdev = nullptr;
     for (int d = 0; d < n_draws; ++d) {
         const fs3d_mesh_draw& m = draws[d];
         if (m.n_vertices < 0 || m.n_vertices % 3 || (m.n_vertices && !m.vertices) || m.material < FS3D_MAT_BASIC ||
@@ -544,8 +549,22 @@ extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_
             return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: bad draw");
         // the kernels read the vertices and texels: they must be device or
         // page-locked memory (used through its device alias), 4-byte aligned
-        const uint8_t* vdev = m.n_vertices ? device_view(m.vertices) : nullptr;
-        const uint8_t* tdev = m.material != FS3D_MAT_BASIC ? device_view(m.texture) : nullptr;
+        const uint8_t* vdev = nullptr;
+        const uint8_t* tdev = nullptr;
+        if (m.n_vertices) {
+            if (m.vertices != last_v) {
+                last_v = m.vertices;
+                last_vdev = device_view(m.vertices);
+            }
+            vdev = last_vdev;
+        }
+        if (m.material != FS3D_MAT_BASIC) {
+            if (m.texture != last_t) {
+                last_t = m.texture;
+                last_tdev = device_view(m.texture);
+            }
+            tdev = last_tdev;
+        }
         if ((m.n_vertices && (!vdev || (reinterpret_cast<uintptr_t>(vdev) & 3))) ||
             (m.material != FS3D_MAT_BASIC && (!tdev || (reinterpret_cast<uintptr_t>(tdev) & 3))))
             return set_error(FS3D_ERR_INVALID_ARG,
@@ -563,13 +582,16 @@ extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_
         prims += x.n_tri;
     }
     if (prims >= (1ll << 30)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render_meshes: too many triangles");
-    // sRGB texels to linear, as the sampler of an _SRGB format does
-    float lut[256];
-    for (int i = 0; i < 256; ++i) {
-        const double c = i / 255.0;
-        lut[i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
-    }
-    const size_t draws_b = sizeof(MeshDrawDev) * dd.size(), lut_b = sizeof(lut);
+    // sRGB texels to linear, as the sampler of an _SRGB format does (built once)
+    static const std::vector<float> lut = [] {
+        std::vector<float> t(256);
+        for (int i = 0; i < 256; ++i) {
+            const double c = i / 255.0;
+            t[(size_t)i] = (float)(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+        }
+        return t;
+    }();
+    const size_t draws_b = sizeof(MeshDrawDev) * dd.size(), lut_b = sizeof(float) * 256;
     const size_t tris_b = sizeof(ScrTri) * 3 * (size_t)(prims > 0 ? prims : 1), key_b = sizeof(unsigned long long) * W * H;
     const size_t o_lut = (draws_b + 255) & ~(size_t)255, o_tris = (o_lut + lut_b + 255) & ~(size_t)255,
                  o_key = (o_tris + tris_b + 255) & ~(size_t)255;
@@ -580,7 +602,7 @@ extern "C" fs3d_status fs3d_render_meshes(const fs3d_object_view* v, const fs3d_
     ScrTri* tris = reinterpret_cast<ScrTri*>(scratch + o_tris);
     unsigned long long* key = reinterpret_cast<unsigned long long*>(scratch + o_key);
     cudaError_t e = cudaMemcpyAsync(ddev, dd.data(), draws_b, cudaMemcpyHostToDevice, st);  // pageable: staged
-    if (e == cudaSuccess) e = cudaMemcpyAsync(lut_dev, lut, lut_b, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(lut_dev, lut.data(), lut_b, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(key, 0xFF, key_b, st);
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_render_meshes upload");
     if (s == FS3D_OK && prims > 0) {

@@ -327,7 +327,7 @@ typedef struct fs3d_mesh_draw {
     const uint8_t* texture; /* RGBA8 texels, row-major, sRGB; device or page-locked      */
     int tex_width, tex_height;
 } fs3d_mesh_draw;
-/* n_draws <= 4096, fewer than 2^30 triangles in all */
+/* n_draws <= 65536, fewer than 2^30 triangles in all */
 fs3d_status fs3d_render_meshes(const fs3d_object_view* view, const fs3d_mesh_draw* draws, int n_draws, int W, int H,
                                float* rgba_dev, void* stream);
 
