@@ -322,7 +322,7 @@ __device__ __forceinline__ int select_bit(uint32_t m, int n) {
     return pos + (n >= (int)(m & 1u) ? 1 : 0);
 }
 
-// bytes of a slab's planes, rounded up so its row flags start 16-byte aligned
+// bytes of a slab's planes, rounded up so its change buffers start 16-byte aligned
 __host__ __device__ __forceinline__ uint32_t slab_flag_offset(uint32_t plane_bytes) {
     return (plane_bytes + 15u) & ~15u;
 }
