@@ -180,8 +180,66 @@ __global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p,
 // ---------------------------------------------------------------------------
 // One block row-pair of one world; lane gl of a group of G lanes.  Every lane
 // of the warp calls this (valid = false for groups past the last row-pair).
+// Non-empty cells of each 8-cell group of a plane word, as bytes: lo byte k
+// counts group 2k, hi byte k group 2k + 1 (at most 8 each).
+__device__ __forceinline__ void group_counts(const uint4& q, uint32_t& lo, uint32_t& hi) {
+    uint32_t e = q.x | q.z, o = q.y | q.w;  // bit m of nibble i: a non-empty cell of group i
+    e = e - ((e >> 1) & 0x55555555u);
+    e = (e & 0x33333333u) + ((e >> 2) & 0x33333333u);
+    o = o - ((o >> 1) & 0x55555555u);
+    o = (o & 0x33333333u) + ((o >> 2) & 0x33333333u);
+    lo = (e & 0x0F0F0F0Fu) + (o & 0x0F0F0F0Fu);
+    hi = ((e >> 4) & 0x0F0F0F0Fu) + ((o >> 4) & 0x0F0F0F0Fu);
+}
+
+// Adds one row pair's net change of non-empty cells to the per-brick counts
+// (bricks of 8x8x8 cells, index bx + BX*(bz + BZ*by)).  The four rows are
+// split by the brick they lie in (they share one unless the pair straddles a
+// brick face in y or z); per part the group counts are summed bytewise,
+// before and after, and only the groups whose sum moved reach an atomic, so
+// cells moving within a brick cost none.  The counts stay exact: a brick is
+// empty exactly when its count is 0.
+__device__ __forceinline__ void count_bricks(int* __restrict__ counts, const PlaneWorld& w, int y0, int z0, int gl,
+                                             const uint4 (&q)[4], const uint4 (&q0)[4], const bool (&in)[4]) {
+    const int BX = (w.X + 7) >> 3, BZ = (w.Z + 7) >> 3;
+    const bool ysplit = ((y0 + 1) & 7) == 0, zsplit = ((z0 + 1) & 7) == 0;
+#pragma unroll
+    for (int part = 0; part < 4; ++part) {
+        if ((part & 1) && !ysplit) continue;
+        if ((part & 2) && !zsplit) continue;
+        uint32_t nlo = 0, nhi = 0, olo = 0, ohi = 0;
+        bool any = false;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            // rows a = 0, 1 are layer y0 + 1 (part bit 0 when the pair straddles y),
+            // rows a = 1, 3 are z0 + 1 (part bit 1 when it straddles z)
+            const int pa = (ysplit && a < 2 ? 1 : 0) | (zsplit && (a & 1) ? 2 : 0);
+            if (pa != part || !in[a]) continue;
+            uint32_t l, h;
+            group_counts(q[a], l, h);
+            nlo += l;
+            nhi += h;
+            group_counts(q0[a], l, h);
+            olo += l;
+            ohi += h;
+            any = true;
+        }
+        if (!any || (nlo == olo && nhi == ohi)) continue;
+        const int y = (part & 1) ? y0 + 1 : (ysplit ? y0 : y0 + 1);
+        const int z = (part & 2) ? z0 + 1 : z0;
+        const int64_t row = (int64_t)BX * ((z >> 3) + (int64_t)BZ * (y >> 3));
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const uint32_t nb = (((i & 1) ? nhi : nlo) >> (8 * (i >> 1))) & 0xFFu;
+            const uint32_t ob = (((i & 1) ? ohi : olo) >> (8 * (i >> 1))) & 0xFFu;
+            const int bx = 8 * gl + i;
+            if (nb != ob && bx < BX) atomicAdd(counts + row + bx, (int)nb - (int)ob);
+        }
+    }
+}
+
 __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, bool valid, int gl,
-                                              int G) {
+                                              int G, int* counts) {
     const int NBZ = nblocks(w.Z, o);
     const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
@@ -199,10 +257,14 @@ __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32
         q0[a] = q[a];
     }
     rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
+    bool any = false;
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        if (in[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w))
+        if (in[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w)) {
             *ptr[a] = q[a];
+            any = true;
+        }
+    if (counts && any) count_bricks(counts, w, y0, z0, gl, q, q0, in);
 }
 
 // One launch = one step (segment step s_seg) of every live world.  Work items
@@ -211,7 +273,7 @@ __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32
 // device memory so a captured graph keeps working as worlds come and go.
 __global__ void __launch_bounds__(256) k_plane_step(const PlaneWorld* __restrict__ worlds,
                                                    const PlaneItem* __restrict__ items,
-                                                   const int* __restrict__ n_items_p, int s_seg) {
+                                                   const int* __restrict__ n_items_p, int s_seg, int* counts) {
     const int n_items = *n_items_p;
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -225,7 +287,7 @@ __global__ void __launch_bounds__(256) k_plane_step(const PlaneWorld* __restrict
         const int gl = lane & (G - 1);
         const int rp = item.rp0 + (lane >> w.lg);
         const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
-        plane_rowpair(w, o, stepkey(w.seed, t), rp, rp < nrp, gl, G);
+        plane_rowpair(w, o, stepkey(w.seed, t), rp, rp < nrp, gl, G, item.world == 0 ? counts : nullptr);
     }
 }
 
@@ -874,8 +936,8 @@ fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, 
 }
 
 fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev,
-                              int grid, int s_seg, cudaStream_t st) {
-    k_plane_step<<<grid, 256, 0, st>>>(worlds, items, n_items_dev, s_seg);
+                              int grid, int s_seg, cudaStream_t st, int* brick_counts) {
+    k_plane_step<<<grid, 256, 0, st>>>(worlds, items, n_items_dev, s_seg, brick_counts);
     FS3D_CHECK_LAUNCH("plane step launch");
     return FS3D_OK;
 }

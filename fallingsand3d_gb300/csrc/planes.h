@@ -106,8 +106,10 @@ fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, in
                             cudaStream_t st);
 fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,
                               unsigned long long* out_dev, cudaStream_t st);
+// brick_counts: nullable per-brick counts of non-empty cells of world 0, kept
+// exact as it steps (one-world launches of a world that renders)
 fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev, int grid,
-                              int s_seg, cudaStream_t st);
+                              int s_seg, cudaStream_t st, int* brick_counts = nullptr);
 
 // byte-grid kernels (step_bytes.cu)
 bool rows16_ok(const void* grid, int X);
@@ -122,8 +124,12 @@ fs3d_status launch_render_sdf(const fs3d_camera* cam, int W, int H, float* rgba_
 size_t brickmap_bytes(int X, int Y, int Z);
 fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, uint32_t* bm_bits, const fs3d_camera* cam,
                                     int W, int H, float* rgba_dev, cudaStream_t st);
+// brick_counts (nullable): exact per-brick counts of non-empty cells; the
+// frame then derives its brick map from them (rebuild: recount from the
+// planes first) instead of a pass over the planes
 fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
                                      uint32_t* bm_bits, const fs3d_camera* cam, int W, int H, float* rgba_dev,
-                                     cudaStream_t st);
+                                     cudaStream_t st, int* brick_counts = nullptr, bool recount = true);
+size_t brick_count_bytes(int X, int Y, int Z);
 
 }  // namespace fs3d

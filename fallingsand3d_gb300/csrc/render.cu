@@ -151,6 +151,43 @@ __global__ void k_brickmap_planes(const uint4* __restrict__ rows, int X, int Y, 
     }
 }
 
+// Counts of non-empty cells per brick, from the planes (one thread per row word)
+__global__ void k_brickcount_planes(const uint4* __restrict__ rows, int X, int Y, int Z, int nw, int* counts, int BX,
+                                    int BZ) {
+    const int64_t n = (int64_t)Y * Z * nw;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(u % nw);
+        const int64_t r = u / nw;
+        const int y = (int)(r / Z), z = (int)(r % Z);
+        const uint4 q = rows[u];
+        const uint32_t e = q.x | q.z, o = q.y | q.w;
+        if (!(e | o)) continue;
+        const int64_t base = (int64_t)BX * ((z >> 3) + (int64_t)BZ * (y >> 3));
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int cnt = __popc((e >> (4 * c)) & 0xFu) + __popc((o >> (4 * c)) & 0xFu);
+            if (cnt && 8 * g + c < BX) atomicAdd(counts + base + 8 * g + c, cnt);
+        }
+    }
+}
+
+// bit b of the brick map = (counts[b] > 0): a warp builds 32 map words,
+// one ballot over 32 consecutive counts each
+__global__ void k_counts_to_bits(const int* __restrict__ counts, int64_t n, uint32_t* bits) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwords = (n + 31) / 32;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w < nwords; w += nwarps * 32) {
+        uint32_t mine = 0;
+        for (int k = 0; k < 32; ++k) {
+            const int64_t b = (w + k) * 32 + lane;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, b < n && counts[b] > 0);
+            if (lane == k) mine = m;
+        }
+        if (w + lane < nwords) bits[w + lane] = mine;
+    }
+}
+
 // bytes: a thread per 8-cell chunk of a row
 __global__ void k_brickmap_bytes(const uint8_t* __restrict__ g, int X, int Y, int Z, uint32_t* bits, int BX, int BZ) {
     const int64_t n = (int64_t)Y * Z * BX;
@@ -326,17 +363,32 @@ fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, uint3
 
 fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, int nw,
                                      uint32_t* bm_bits, const fs3d_camera* cam, int W, int H, float* rgba_dev,
-                                     cudaStream_t st) {
+                                     cudaStream_t st, int* brick_counts, bool recount) {
     const int BX = (X + 7) / 8, BY = (Y + 7) / 8, BZ = (Z + 7) / 8;
-    FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
-    k_brickmap_planes<<<map_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, X, Y, Z, nw, bm_bits, BX, BZ);
-    FS3D_CHECK_LAUNCH("brick map (planes) launch");
+    const int64_t nb = (int64_t)BX * BY * BZ;
+    if (brick_counts) {
+        if (recount) {
+            FS3D_CUDA(cudaMemsetAsync(brick_counts, 0, brick_count_bytes(X, Y, Z), st));
+            k_brickcount_planes<<<map_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, X, Y, Z, nw, brick_counts, BX, BZ);
+            FS3D_CHECK_LAUNCH("brick counts (planes) launch");
+        }
+        k_counts_to_bits<<<map_grid((nb + 31) / 32 + 32), 256, 0, st>>>(brick_counts, nb, bm_bits);
+        FS3D_CHECK_LAUNCH("brick map from counts launch");
+    } else {
+        FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
+        k_brickmap_planes<<<map_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, X, Y, Z, nw, bm_bits, BX, BZ);
+        FS3D_CHECK_LAUNCH("brick map (planes) launch");
+    }
     const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
     k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(
         PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw}, BrickMap{bm_bits, BX, BY, BZ},
         to_dev(cam), W, H, reinterpret_cast<float4*>(rgba_dev));
     FS3D_CHECK_LAUNCH("render dda (planes) launch");
     return FS3D_OK;
+}
+
+size_t brick_count_bytes(int X, int Y, int Z) {
+    return (size_t)((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8) * sizeof(int);
 }
 
 size_t brickmap_bytes(int X, int Y, int Z) {

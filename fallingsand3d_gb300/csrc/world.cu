@@ -32,6 +32,8 @@ struct fs3d_world {
     int cls = -1;        // resident class (-1: stepped by the per-step kernel)
     unsigned long long* hash_dev = nullptr;
     uint32_t* brickmap = nullptr;  // render: per-frame occupancy of 8x8x8 bricks
+    int* brick_counts = nullptr;   // PLANES render: non-empty cells per brick, kept by the per-step kernel
+    bool counts_valid = false;     // brick_counts match the planes
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
 
@@ -82,6 +84,7 @@ void destroy(fs3d_world* w) {
     cudaFree(w->aux);
     cudaFree(w->hash_dev);
     cudaFree(w->brickmap);
+    cudaFree(w->brick_counts);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
 }
@@ -200,10 +203,14 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
             // the world fits in shared memory (one CTA or a cluster): all n steps in one launch
             s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
                                               w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
+            w->counts_valid = false;  // the next frame recounts
         } else {
+            // once a frame has counted the bricks, the per-step kernel keeps
+            // the counts exact, so later frames read no pass over the planes
             const int grid = plane_step_grid(w->n_items);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
-                s = launch_plane_step(w->desc, w->items, w->n_items_dev, grid, a, w->stream);
+                s = launch_plane_step(w->desc, w->items, w->n_items_dev, grid, a, w->stream,
+                                      w->counts_valid ? w->brick_counts : nullptr);
         }
     }
     if (s == FS3D_OK) w->step += (uint64_t)n_steps;
@@ -241,6 +248,7 @@ fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* out) {
 
 fs3d_status fs3d_world_write(fs3d_world* w, const uint8_t* g) {
     if (!w || !g) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_write: bad args");
+    w->counts_valid = false;
     return upload(w, g);
 }
 
@@ -344,15 +352,20 @@ fs3d_status fs3d_render(fs3d_world* w, const fs3d_camera* cam, int W, int H, int
     const size_t bytes = (size_t)W * H * 4 * sizeof(float);
     if (mode == FS3D_RENDER_DDA && !w->brickmap)
         FS3D_CUDA(cudaMalloc((void**)&w->brickmap, brickmap_bytes(w->X, w->Y, w->Z)));
+    // planes worlds stepped by the per-step kernel keep exact brick counts
+    if (mode == FS3D_RENDER_DDA && w->layout == FS3D_LAYOUT_PLANES && w->cls < 0 && !w->brick_counts)
+        FS3D_CUDA(cudaMalloc((void**)&w->brick_counts, brick_count_bytes(w->X, w->Y, w->Z)));
     if (!out_on_device) FS3D_CUDA(cudaMallocAsync((void**)&dst, bytes, w->stream));
     fs3d_status s;
     if (mode == FS3D_RENDER_SDF_SPHERE)
         s = launch_render_sdf(cam, W, H, dst, w->stream);
     else if (w->layout == FS3D_LAYOUT_BYTES)
         s = launch_render_dda_bytes(w->bytes, w->X, w->Y, w->Z, w->brickmap, cam, W, H, dst, w->stream);
-    else
+    else {
         s = launch_render_dda_planes(w->rows, w->statics, w->X, w->Y, w->Z, plane_nw(w->X), w->brickmap, cam, W, H, dst,
-                                     w->stream);
+                                     w->stream, w->brick_counts, !w->counts_valid);
+        if (s == FS3D_OK && w->brick_counts) w->counts_valid = true;
+    }
     if (!out_on_device) {
         cudaError_t e = cudaSuccess;
         if (s == FS3D_OK) e = cudaMemcpyAsync(rgba, dst, bytes, cudaMemcpyDeviceToHost, w->stream);
