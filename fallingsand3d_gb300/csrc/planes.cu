@@ -21,6 +21,8 @@
 #include <cooperative_groups.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "fs3d_common.h"
 #include "pcg.h"
 #include "planes.h"
@@ -642,16 +644,16 @@ struct ResidentCfg {
     const void* fn;
 };
 
+// filled once per process (the first device the library is used on), from any thread
 ResidentCfg g_classes[kResidentClasses];
-bool g_classes_ready = false;
+std::once_flag g_classes_once;
 
 template <int NT, bool CL>
 const void* resident_fn() {
     return reinterpret_cast<const void*>(&k_plane_segment_resident<NT, CL>);
 }
 
-void init_classes() {
-    if (g_classes_ready) return;
+void fill_classes() {
     int dev = 0, per_sm = 0, optin = 0, reserved = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -680,8 +682,9 @@ void init_classes() {
         g_classes[c] = k;
     }
     cudaGetLastError();  // a refused attribute leaves the class unused, not an error
-    g_classes_ready = true;
 }
+
+void init_classes() { std::call_once(g_classes_once, fill_classes); }
 
 }  // namespace
 
@@ -713,7 +716,7 @@ int resident_class(int X, int Y, int Z) {
 namespace {
 constexpr int kGmThreads[kGmClasses] = {32, 64, 128, 256};
 constexpr int kGmMaxY[kGmClasses] = {1024, 1024, 2048, 4096};
-bool g_gm_ready = false;
+std::once_flag g_gm_once;
 }  // namespace
 
 int resident_class_gm(int X, int Y, int Z) {
@@ -735,7 +738,7 @@ static cudaError_t launch_gm(int cls, int grid, size_t smem, cudaStream_t st, co
 fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
                                     int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells) {
     if (cls < 0 || cls >= kGmClasses) return set_error(FS3D_ERR_INVALID_ARG, "global-memory class out of range");
-    if (!g_gm_ready) {
+    std::call_once(g_gm_once, [] {
         // the planes are read through L1: leave most of the unified memory to it
         const void* fns[kGmClasses] = {reinterpret_cast<const void*>(&k_plane_segment_resident<32, false, true>),
                                        reinterpret_cast<const void*>(&k_plane_segment_resident<64, false, true>),
@@ -743,8 +746,7 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
                                        reinterpret_cast<const void*>(&k_plane_segment_resident<256, false, true>)};
         for (const void* fn : fns) cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
         cudaGetLastError();
-        g_gm_ready = true;
-    }
+    });
     FS3D_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
     const int nt = kGmThreads[cls];
     const int grid = sm_count_public() * (kGmThreadsPerSm / nt);
@@ -944,10 +946,11 @@ fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, 
 
 // CTAs of the step kernel that fit on one SM at once
 int plane_step_ctas_per_sm() {
-    static int n = 0;
-    if (!n) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_plane_step, 256, 0) != cudaSuccess || n < 1) n = 1;
-    }
+    static const int n = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_plane_step, 256, 0) != cudaSuccess || v < 1) v = 1;
+        return v;
+    }();
     return n;
 }
 

@@ -333,14 +333,14 @@ __global__ void k_first_diff(const uint8_t* __restrict__ a, const uint8_t* __res
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// device properties, looked up once per process (thread-safe static initialisation)
 static int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
+    static const int n = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 148;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 148;
+    }();
     return n;
 }
 
@@ -365,9 +365,11 @@ static int rows64_lg(int X) {
 }
 
 static int rows64_ctas_per_sm() {
-    static int n = 0;
-    if (!n && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_rows64, 128, 0) != cudaSuccess || n < 1))
-        n = 1;
+    static const int n = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_step_rows64, 128, 0) != cudaSuccess || v < 1) v = 1;
+        return v;
+    }();
     return n;
 }
 
