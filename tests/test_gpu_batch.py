@@ -365,3 +365,41 @@ def test_admit_and_retire_many_contiguous_runs(fs3d, orc, cuda, where):
         ref = g.copy()
         orc.run(ref, seed, 0, n_steps, nthreads=0)
         assert (out[o:o + n].reshape(g.shape) == ref).all(), dims
+
+
+def test_handles_used_from_several_threads(fs3d, orc):
+    """Different handles may be used concurrently: four threads, each with its
+    own batch (and one with a plane world), step and read back at once."""
+    import threading
+    results, errors = {}, []
+
+    def run(tid):
+        try:
+            worlds = small_batch(fs3d, 40 + tid, 6, max_dim=64)
+            n = 80
+            with fs3d.Batch(GiB, steps_per_segment=32) as b:
+                ts = [b.admit(fs3d.gen_batch_world(s, *d), s, n) for d, s in worlds]
+                for _ in range(3):
+                    b.run_segment()
+                b.sync()
+                results[tid] = [(d, s, b.poll(t)[1]) for t, (d, s) in zip(ts, worlds)]
+            if tid == 0:
+                g = fs3d.gen_batch_world(99, 96, 40, 72)
+                with fs3d.World(g, 99, 0, fs3d.LAYOUT_PLANES) as w:
+                    w.step(50)
+                    results["world"] = w.hash()
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for tid in range(4):
+        for dims, seed, h in results[tid]:
+            assert h == orc.hash(oracle_final(orc, fs3d, dims, seed, 80)), (tid, dims)
+    ref = fs3d.gen_batch_world(99, 96, 40, 72)
+    orc.run(ref, 99, 0, 50, nthreads=0)
+    assert results["world"] == orc.hash(ref)
