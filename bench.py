@@ -9,6 +9,8 @@ segment.  The same line carries:
   * plain_512: the drop-in byte kernel on one 512^3 pillar world (HBM-bound);
   * roofline of the dominant kernel (CUDA-event time per launch);
   * cpu_baseline: the CPU oracle timed on this host (bounded sample);
+  * parity: results of the timed GPU runs, read back and checked against the
+    oracle in the CPU leg once every GPU measurement has ended;
   * e2e: the same metric through the C ABI from pinned host buffers
     (admit = H2D + conversion, one segment, retire = conversion + D2H).
 `--impl reference` times the CPU oracle (the upstream project has no step of
@@ -166,7 +168,7 @@ def profile_traffic(kernel: str):
     return float(m.group(1)), (float(c.group(1)) if c else None)
 
 
-# ------------------------------------------------------------------ CPU oracle timing
+# ------------------------------------------------------------------ CPU leg: oracle timing and checks
 def cpu_sample(worlds, budget_s: float, threads: int):
     """Times the oracle step on a bounded sample of the batch workload: worlds
     are stepped concurrently (one thread each) until ~budget_s has passed."""
@@ -196,6 +198,44 @@ def cpu_sample(worlds, budget_s: float, threads: int):
     dt = time.perf_counter() - t0
     return done / dt, {"worlds": len(sample), "steps_per_round": steps_each, "rounds": rounds,
                        "voxel_updates": done, "seconds": round(dt, 3)}
+
+
+class OracleChecks:
+    """GPU results recorded by the GPU legs (copies on the host), checked
+    against the oracle in the CPU leg, after every GPU measurement has ended."""
+
+    def __init__(self):
+        self.runs = {}    # label -> [(grid before, seed, first step, steps, GPU grid after)]
+        self.dda = None   # (grid, camera, W, H, GPU frame, tolerance)
+        self.mesh = None  # (scene view kwargs, draws, W, H, GPU frame)
+
+    def add_run(self, label, grid, seed, t0, n, got):
+        self.runs.setdefault(label, []).append((grid, seed, t0, n, got))
+
+    def check(self):
+        """Returns {"parity": str, "large": {...}, "mesh": {...}}."""
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        orc = oracle_lib.load()
+        out, notes = {}, []
+        for label, items in self.runs.items():
+            ok = True
+            for grid, seed, t0, n, got in items:
+                g = grid.copy()
+                orc.run(g, seed, t0, n, nthreads=0)
+                ok &= bool((got == g).all())
+            notes.append(f"{len(items)} worlds of the {label} bit-exact" if ok else f"MISMATCH ({label})")
+        out["parity"] = "; ".join(notes) if notes else None
+        if self.dda is not None:
+            grid, cam, W, H, got, tol = self.dda
+            exp = orc.render_dda(grid, oracle_lib.camera_from(cam), W, H)
+            d = float(np.abs(got - exp).max())
+            out["large"] = {"last_frame_max_abs_diff_vs_cpu": d, "tolerance": tol, "within_tolerance": d <= tol}
+        if self.mesh is not None:
+            kw, draws, W, H, got = self.mesh
+            exp = orc.render_meshes(oracle_lib.scene_view(**kw), draws, W, H)
+            out["mesh"] = {"bit_exact_vs_cpu": bool(np.array_equal(got, exp))}
+        return out
 
 
 def run_reference(args):
@@ -287,21 +327,15 @@ def run_fs3d(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = cells * S * world / (ms / 1e3)
-    # parity spot check of the timed run: a few worlds against the oracle
-    parity = None
-    if rank == 0 and not args.no_check:
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        import oracle_lib
-        orc = oracle_lib.load()
+    # parity spot check of the timed run: three worlds read back now, checked
+    # against the oracle in the CPU leg
+    checks = OracleChecks() if rank == 0 and not args.no_check else None
+    if checks is not None:
         b.sync()
-        ok = True
         for i in range(3):
             (X, Y, Z), seed = worlds[i]
-            g = host[i].numpy().copy()
-            orc.run(g, seed, 0, S * (untimed + args.steps), nthreads=0)
-            got = b.retire(tickets[i], (Y, Z, X))
-            ok &= bool((got == g).all())
-        parity = "3 worlds bit-exact after the timed segments" if ok else "MISMATCH"
+            checks.add_run("timed batch", host[i].numpy().copy(), seed, 0, S * (untimed + args.steps),
+                           b.retire(tickets[i], (Y, Z, X)))
     b.close()
 
     # ---- e2e through the C ABI from pinned host buffers
@@ -326,16 +360,10 @@ def run_fs3d(args):
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = e2e_ms[2:]  # the first calls also capture the segment graph and grow the pool
     e2e_val = cells * S / (float(np.mean(e2e_ms)) / 1e3)
-    if parity is not None:
+    if checks is not None:
         # the round trip: each output is its input stepped S steps
         for i in (0, len(worlds) - 1):
-            (X, Y, Z), seed = worlds[i]
-            g = host[i].numpy().copy()
-            orc.run(g, seed, 0, S, nthreads=0)
-            if not (outs[i].numpy() == g).all():
-                parity = "MISMATCH (e2e)"
-        if not parity.startswith("MISMATCH"):
-            parity += "; 2 worlds of the e2e round trip bit-exact"
+            checks.add_run("e2e round trip", host[i].numpy().copy(), worlds[i][1], 0, S, outs[i].numpy().copy())
 
     # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
     offs, off = [], 0
@@ -421,10 +449,10 @@ def run_fs3d(args):
     # ---- large world + render: 1024^3 dunes, every step followed by a 1920x1080 DDA frame
     large = None
     if not args.skip_large:
-        large = run_large(fs3d, torch, dev, args)
+        large = run_large(fs3d, torch, dev, args, checks)
 
     # ---- mesh materials: the upstream cube-grid scene
-    mesh = None if args.skip_large else run_mesh(fs3d, torch, args)
+    mesh = None if args.skip_large else run_mesh(fs3d, torch, args, checks)
 
     # ---- roofline of the dominant work: the segment graph, whose time is the
     # resident kernels (one launch per size class steps its worlds 64 times in
@@ -449,7 +477,7 @@ def run_fs3d(args):
                         "exactly); the worlds stay in L2, so DRAM sees a few MB per segment; the kernels are "
                         "latency-bound: each world's steps are a serial chain (see profiles/)"}
 
-    # ---- CPU baseline (rank 0, N=1)
+    # ---- CPU leg (rank 0): the oracle timed (N=1), then the recorded GPU results checked against it
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -457,6 +485,14 @@ def run_fs3d(args):
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{info['worlds']} of the {args.worlds} worlds x {info['steps_per_round']} steps x "
                          f"{info['rounds']} rounds, one world per thread ({info['seconds']} s)"}
+    parity = None
+    if checks is not None:
+        res = checks.check()
+        parity = res["parity"]
+        if large is not None and "large" in res:
+            large.update(res["large"])
+        if mesh is not None and "mesh" in res:
+            mesh.update(res["mesh"])
 
     if rank == 0:
         line = {"metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -488,12 +524,11 @@ def run_fs3d(args):
     return 0
 
 
-def run_large(fs3d, torch, dev, args, X=1024, Y=1024, Z=1024, W=1920, H=1080):
+def run_large(fs3d, torch, dev, args, checks=None, X=1024, Y=1024, Z=1024, W=1920, H=1080):
     """1024^3 dune world (plane layout, per-step kernel), each step followed by
-    a 1920x1080 DDA frame into a device buffer; the last frame is checked
-    against the CPU DDA and per-material mass against the initial grid."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
+    a 1920x1080 DDA frame into a device buffer; per-material mass is checked
+    against the initial grid, and the last frame is recorded in `checks` for
+    the CPU DDA."""
     g = fs3d.gen_dunes(1, X, Y, Z)
     counts0 = np.bincount(g.reshape(-1), minlength=4)
     cam = fs3d.camera_world_view(X, Y, Z, W, H)
@@ -522,25 +557,23 @@ def run_large(fs3d, torch, dev, args, X=1024, Y=1024, Z=1024, W=1920, H=1080):
         sampled = max(1, n // 50)
         last = frame.cpu().numpy()
         final = w.read()
-    exp = oracle_lib.load().render_dda(final, oracle_lib.camera_from(cam), W, H)
+    if checks is not None:
+        checks.dda = (final, cam, W, H, last, 1e-5)
     counts = np.bincount(final.reshape(-1), minlength=4)
     cells = X * Y * Z
     return {"workload": f"{X}x{Y}x{Z} dunes (plane layout), {n} steps, each followed by a {W}x{H} fp32 DDA frame",
             "wall_s": round(wall, 3), "step_us": round(step_ms / sampled * 1e3, 2),
             "frame_us": round(frame_ms / sampled * 1e3, 2),
             "voxel_updates_per_s": cells * n / wall, "rays_per_s": W * H * n / wall,
-            "last_frame_max_abs_diff_vs_cpu": float(np.abs(last - exp).max()), "tolerance": 1e-5,
             "mass_conserved": bool((counts == counts0).all())}
 
 
-def run_mesh(fs3d, torch, args, W=1920, H=1080, frames=20):
+def run_mesh(fs3d, torch, args, checks=None, W=1920, H=1080, frames=20):
     """The cube-grid scene of the upstream renderer (renderer.cpp:1328-1352):
     51 x 51 green cubes (basic_mat) at y = 0 and 51 x 51 red textured cubes
     (textured_mat) at y = 5, each 0.2 in scale, one draw per cube; a seeded
     512 x 512 texture stands in for the texture file.  Frame time with CUDA
-    events; the last frame checked against the CPU restatement."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
+    events; the last frame is recorded in `checks` for the CPU restatement."""
     f = fs3d.mesh_cube().reshape(-1, 3)
     cube = np.c_[f, (f[:, [0, 2]] + 1) * 0.5].astype(np.float32)
     rng = np.random.default_rng(2024)
@@ -568,12 +601,12 @@ def run_mesh(fs3d, torch, args, W=1920, H=1080, frames=20):
     e1.record(st)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / frames
-    exp = oracle_lib.load().render_meshes(oracle_lib.scene_view(**kw), cpu, W, H)
     got = out.cpu().numpy()
+    if checks is not None:
+        checks.mesh = (kw, cpu, W, H, got)
     return {"workload": f"{len(gpu)} cube draws ({12 * len(gpu)} triangles, basic_mat and textured_mat) at {W}x{H}",
             "frame_us": round(ms * 1e3, 1), "triangles_per_s": 12 * len(gpu) / (ms / 1e3),
-            "pixels_covered": int((got != np.float32([0, 0, 1, 1])).any(-1).sum()),
-            "bit_exact_vs_cpu": bool(np.array_equal(got, exp))}
+            "pixels_covered": int((got != np.float32([0, 0, 1, 1])).any(-1).sum())}
 
 
 def run_only(args):
