@@ -87,7 +87,7 @@ struct fs3d_batch {
     uint64_t next_ticket = 1;
     PinnedArray<PlaneWorld> tw;
     PinnedArray<PlaneItem> ti;
-    PinnedArray<int> tn;  // meta: {per-step items, resident count per class, offset per class}
+    PinnedArray<int> tn;  // meta: {per-step items, resident count per class, offset per class, worlds}
     PinnedArray<int> to;  // resident worlds (indices into tw) by class, largest first
     int* counter = nullptr;  // work counters of the resident kernels, one per class
     int* err = nullptr;      // set by a kernel whose bounded wait gave up
@@ -109,6 +109,15 @@ struct fs3d_batch {
     uint64_t segments = 0;
     uint64_t dense_cell_steps = 0;   // every cell of every stepped world, per step
     uint64_t stepped_cell_steps = 0; // of those, taken by the per-step kernel (always evaluated)
+    // The device tables as the last segment left them (each world advanced by
+    // its steps) are the next segment's tables while no world is admitted or
+    // retired, changes class, or takes fewer steps than a full segment:
+    // `reuse_left` more segments may launch without rebuilding them.
+    bool tables_stale = true;
+    uint64_t reuse_left = 0;
+    std::vector<BWorld*> running;  // the worlds of the tables, in table order
+    size_t table_items = 0;        // per-step kernel items in the tables
+    uint64_t table_dense = 0, table_stepped = 0;  // cell-steps per segment of the tables
 };
 
 namespace {
@@ -201,7 +210,7 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
             FS3D_CUDA(cudaEventRecord(b->join[c], b->branch[c]));
             FS3D_CUDA(cudaStreamWaitEvent(a, b->join[c], 0));
         }
-    return FS3D_OK;
+    return launch_advance_worlds(b->tw.d, b->tn.d, a);
 }
 
 fs3d_status capture_one(fs3d_batch* b, bool with_steps, cudaGraphExec_t* out) {
@@ -363,6 +372,7 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     b->used += w.bytes;
     *ticket = b->next_ticket++;
     b->worlds.emplace(*ticket, w);
+    b->tables_stale = true;
     return FS3D_OK;
 }
 
@@ -381,9 +391,19 @@ fs3d_status fs3d_batch_admit_generated(fs3d_batch* b, int X, int Y, int Z, uint6
     return admit(b, nullptr, X, Y, Z, seed, start_step, n_steps, ticket);
 }
 
-fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
-    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_run_segment: NULL batch");
+}  // extern "C"
+
+namespace {
+
+// Rebuilds the segment tables from the running worlds (their segment class,
+// steps and kept layer flags), uploads them and works out how many following
+// segments may reuse them as the device advances them.
+fs3d_status build_tables(fs3d_batch* b) {
     const int S = b->cfg.steps_per_segment;
+    b->running.clear();
+    b->table_items = 0;
+    b->table_dense = b->table_stepped = 0;
+    b->reuse_left = 0;
     // the pinned tables may be rewritten once the previous upload has run
     FS3D_CUDA(cudaEventSynchronize(b->tables_free));
     // resident class of every running world (-1: stepped by the per-step kernel)
@@ -409,8 +429,9 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     if (s != FS3D_OK) return s;
     std::vector<int> by_class[kAllClasses];
     size_t ii = 0;
+    uint64_t reuse = UINT64_MAX;  // segments these tables hold for, this one included
     for (size_t wi = 0; wi < nw_; ++wi) {
-        const BWorld& w = *run[wi].second;
+        BWorld& w = *run[wi].second;
         const int steps = (int)(w.remaining < S ? w.remaining : S);
         PlaneWorld& d = b->tw.h[wi];
         memset(&d, 0, sizeof(d));
@@ -424,27 +445,34 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
         d.steps = steps;
         d.lg = plane_lg(w.nw);
         // resident segments keep the layer flags; the per-step kernel does not
-        BWorld& wm = *run[wi].second;
         if (run[wi].first >= 0) {
-            d.lflags = wm.lflags;
-            d.lflags_fresh = wm.flags_valid ? 0 : 1;
-            wm.flags_valid = wm.lflags != nullptr;
+            d.lflags = w.lflags;
+            d.lflags_fresh = w.flags_valid ? 0 : 1;
+            w.flags_valid = w.lflags != nullptr;
         } else {
-            wm.flags_valid = false;
+            w.flags_valid = false;
         }
         const uint64_t cs = (uint64_t)w.X * w.Y * w.Z * (uint64_t)steps;
-        b->dense_cell_steps += cs;
-        if (run[wi].first < 0) b->stepped_cell_steps += cs;
+        b->table_dense += cs;
+        if (run[wi].first < 0) b->table_stepped += cs;
         if (run[wi].first >= 0) {
             by_class[run[wi].first].push_back((int)wi);
         } else {
             const int per = 32 >> d.lg, items = plane_items_for(w.Y, w.Z, w.nw);
             for (int a = 0; a < items; ++a) b->ti.h[ii++] = PlaneItem{(int32_t)wi, a * per};
         }
+        // full segments while `remaining` lasts; in the hybrid mode a young
+        // world changes class once it is kYoungSteps old
+        uint64_t hold = (uint64_t)std::max<int64_t>(1, w.remaining / S);
+        const uint64_t age = w.t - w.t0;
+        if (b->cfg.use_smem == 3 && age < kYoungSteps) hold = std::min(hold, (kYoungSteps - age + S - 1) / S);
+        reuse = std::min(reuse, hold);
+        b->running.push_back(&w);
     }
     // per class, largest worlds first, so each launch ends with short work
     int* meta = b->tn.h;
     meta[0] = (int)ii;
+    meta[kMetaWorlds] = (int)nw_;
     size_t si = 0;
     for (int c = 0; c < kAllClasses; ++c) {
         std::vector<int>& v = by_class[c];
@@ -475,24 +503,50 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * kMetaInts, cudaMemcpyHostToDevice,
                               b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
-    if (b->cfg.use_graphs) {
-        if (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d) {
-            s = capture_graph(b);
-            if (s != FS3D_OK) return s;
+    if (b->cfg.use_graphs &&
+        (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d)) {
+        s = capture_graph(b);
+        if (s != FS3D_OK) {
+            b->running.clear();
+            return s;
         }
+    }
+    b->table_items = ii;
+    b->reuse_left = reuse - 1;
+    b->tables_stale = false;
+    return FS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_run_segment: NULL batch");
+    const int S = b->cfg.steps_per_segment;
+    if (!b->tables_stale && b->reuse_left > 0 && !b->running.empty()) {
+        --b->reuse_left;  // the tables on the device are this segment's
+    } else {
+        const fs3d_status s = build_tables(b);
+        if (s != FS3D_OK) return s;
+        if (b->running.empty()) return FS3D_OK;
+    }
+    b->dense_cell_steps += b->table_dense;
+    b->stepped_cell_steps += b->table_stepped;
+    const size_t ii = b->table_items;
+    if (b->cfg.use_graphs) {
         FS3D_CUDA(cudaGraphLaunch(ii ? b->graph_steps : b->graph, b->stream));
         note_launch((ii ? (uint64_t)S : 0u) +
                     (b->cfg.use_smem == 1 || b->cfg.use_smem == 3 ? kResidentClasses : 0) +
-                    (b->cfg.use_smem == 2 || b->cfg.use_smem == 3 ? kGmClasses : 0));
+                    (b->cfg.use_smem == 2 || b->cfg.use_smem == 3 ? kGmClasses : 0) + 1u);
     } else {
-        s = enqueue_segment(b, b->stream, false, ii > 0);
+        const fs3d_status s = enqueue_segment(b, b->stream, false, ii > 0);
         if (s != FS3D_OK) return s;
     }
     FS3D_CUDA(cudaEventRecord(b->last_segment, b->stream));
     std::shared_ptr<CUevent_st> fin;  // one event for every world that finishes in this segment
-    for (auto& kv : b->worlds) {
-        BWorld& w = kv.second;
-        if (w.done) continue;
+    for (BWorld* pw : b->running) {
+        BWorld& w = *pw;
         const int steps = (int)(w.remaining < S ? w.remaining : S);
         w.t += (uint64_t)steps;
         w.remaining -= steps;
@@ -575,6 +629,7 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
     b->used -= w.bytes;
     free_world(b, w);
     b->worlds.erase(it);
+    b->tables_stale = true;
     return s;
 }
 
@@ -740,6 +795,7 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         tickets[a] = b->next_ticket++;
         b->worlds.emplace(tickets[a], w);
     }
+    b->tables_stale = true;
     // the next segment runs after the static copies (side stream) are done
     if (ready) {
         b->pending_ready.push_back(ready);
@@ -855,6 +911,7 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
         free_world(b, it->second);
         b->worlds.erase(it);
     }
+    if (!its.empty()) b->tables_stale = true;
     FS3D_CUDA(cudaStreamSynchronize(b->side));
     return s;
 }
@@ -896,6 +953,7 @@ fs3d_status apply_tuning(fs3d_batch* b, const Tuning& t) {
     FS3D_CUDA(cudaStreamSynchronize(b->stream));
     b->cfg.use_smem = t.mode;
     b->promote = t.promote;
+    b->tables_stale = true;
     b->grid = sm_count_public() * t.ctas_per_sm;
     return b->cfg.use_graphs ? capture_graph(b) : FS3D_OK;
 }

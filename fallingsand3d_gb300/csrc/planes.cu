@@ -944,6 +944,21 @@ fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, 
     return FS3D_OK;
 }
 
+__global__ void k_advance_worlds(PlaneWorld* __restrict__ worlds, const int* __restrict__ meta) {
+    const int n = meta[kMetaWorlds];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        PlaneWorld& w = worlds[i];
+        w.t += (uint64_t)w.steps;
+        if (w.lflags) w.lflags_fresh = 0;
+    }
+}
+
+fs3d_status launch_advance_worlds(PlaneWorld* worlds, const int* meta, cudaStream_t st) {
+    k_advance_worlds<<<8, 256, 0, st>>>(worlds, meta);
+    FS3D_CHECK_LAUNCH("advance worlds launch");
+    return FS3D_OK;
+}
+
 // CTAs of the step kernel that fit on one SM at once
 int plane_step_ctas_per_sm() {
     static const int n = [] {

@@ -47,9 +47,10 @@ constexpr int kGmClasses = 4;
 int resident_class_gm(int X, int Y, int Z);
 // Class ids of a segment's tables: shared-memory classes 0..5, then the
 // global-memory classes 6..9.  meta = {per-step items, worlds per class,
-// offset of each class in the order array}.
+// offset of each class in the order array, worlds in the table}.
 constexpr int kAllClasses = kResidentClasses + kGmClasses;
-constexpr int kMetaInts = 1 + 2 * kAllClasses;
+constexpr int kMetaWorlds = 1 + 2 * kAllClasses;
+constexpr int kMetaInts = kMetaWorlds + 1;
 // smallest class that holds a world of these dims, -1 if none does
 int resident_class(int X, int Y, int Z);
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable
@@ -110,6 +111,10 @@ fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, 
 // exact as it steps (one-world launches of a world that renders)
 fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev, int grid,
                               int s_seg, cudaStream_t st, int* brick_counts = nullptr);
+// After a segment: every world of the table (meta[kMetaWorlds] of them) moves
+// on by its segment steps, and its layer flags count as kept, so the next
+// segment of an unchanged batch reuses the table as it stands.
+fs3d_status launch_advance_worlds(PlaneWorld* worlds, const int* meta, cudaStream_t st);
 
 // byte-grid kernels (step_bytes.cu)
 bool rows16_ok(const void* grid, int X);

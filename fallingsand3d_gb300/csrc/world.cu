@@ -40,7 +40,7 @@ struct fs3d_world {
 namespace {
 
 // layout of fs3d_world::aux (device ints)
-constexpr int kAuxMeta = 0;                              // 1 + 2*classes ints
+constexpr int kAuxMeta = 0;                              // kMetaInts ints
 constexpr int kAuxOrder = kMetaInts;      // order[0] = 0
 constexpr int kAuxCounter = kAuxOrder + 1;
 constexpr int kAuxErr = kAuxCounter + 1;

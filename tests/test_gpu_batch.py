@@ -403,3 +403,35 @@ def test_handles_used_from_several_threads(fs3d, orc):
     ref = fs3d.gen_batch_world(99, 96, 40, 72)
     orc.run(ref, 99, 0, 50, nthreads=0)
     assert results["world"] == orc.hash(ref)
+
+
+def test_tables_reused_between_changes(fs3d, orc):
+    """Segments of an unchanged batch launch on the device tables as the last
+    segment advanced them; every change (a world admitted or retired, a world
+    turning old in the hybrid mode, a last partial segment) rebuilds them.
+    All worlds, including one retired mid-run, follow the oracle."""
+    S = 16
+    worlds = [((16, 16, 16), 11, 16 * 20), ((64, 48, 32), 12, 16 * 9 + 5), ((96, 96, 96), 13, 7),
+              ((24, 128, 40), 14, 16 * 18), ((2048, 8, 6), 15, 16 * 12 + 3)]
+    with fs3d.Batch(4 * GiB, steps_per_segment=S) as b:
+        tickets = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for dims, seed, n in worlds[:4]]
+        early = b.admit(fs3d.gen_batch_world(21, 32, 32, 32), 21, 1000)
+        for _ in range(5):
+            b.run_segment()
+        dims, seed, n = worlds[4]
+        tickets.append(b.admit(fs3d.gen_batch_world(seed, *dims), seed, n, start_step=100))
+        for _ in range(3):
+            b.run_segment()
+        X, Y, Z = 32, 32, 32
+        got = b.retire(early, (Y, Z, X))
+        assert (got == oracle_final(orc, fs3d, (32, 32, 32), 21, 8 * S)).all()
+        for _ in range(20):
+            b.run_segment()
+        b.sync()
+        for t, (dims, seed, n) in zip(tickets, worlds):
+            done, h = b.poll(t)
+            assert done, dims
+            start = 100 if seed == 15 else 0
+            assert h == orc.hash(oracle_final(orc, fs3d, dims, seed, n, start=start)), dims
+        dense = b.counters()["dense_cell_steps"]
+        assert dense == sum(X * Y * Z * n for (X, Y, Z), _, n in worlds) + 32 ** 3 * 8 * S
