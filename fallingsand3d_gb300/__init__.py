@@ -43,7 +43,7 @@ EXPORTS = (
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
-    "fs3d_batch_retire_many",
+    "fs3d_batch_retire_many", "fs3d_batch_admit_many_async", "fs3d_batch_retire_many_async", "fs3d_batch_wait_copies",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
@@ -158,6 +158,9 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_admit_generated": (S, [vp, i32, i32, i32, u64, u64, i64, C.POINTER(u64)]),
         "fs3d_batch_admit_many": (S, [vp, i32, C.POINTER(WorldSpec), C.POINTER(u64), C.POINTER(i32)]),
         "fs3d_batch_retire_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
+        "fs3d_batch_admit_many_async": (S, [vp, i32, C.POINTER(WorldSpec), C.POINTER(u64), C.POINTER(i32)]),
+        "fs3d_batch_retire_many_async": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
+        "fs3d_batch_wait_copies": (S, [vp, i64]),
         "fs3d_batch_run_segment": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
@@ -455,7 +458,7 @@ class Batch:
                  ctas_per_sm: int = 0, use_smem=None):
         """use_smem: None = the library default; False/0 = per-step kernel only;
         True/1 = shared-memory resident segments; 2 = global-memory segments;
-        3 = shared memory for a world's first 256 steps, then global memory."""
+        3 = shared memory for a world's first 128 steps, then global memory."""
         cfg = lib().fs3d_default_config()
         cfg.steps_per_segment = steps_per_segment
         cfg.use_graphs = 1 if use_graphs else 0
@@ -485,12 +488,15 @@ class Batch:
         check(lib().fs3d_batch_admit_generated(self.handle, X, Y, Z, seed, start_step, n_steps, C.byref(t)))
         return int(t.value)
 
-    def admit_many(self, grids, seeds, n_steps, start_steps=None, ptrs=None, dims=None):
+    def admit_many(self, grids, seeds, n_steps, start_steps=None, ptrs=None, dims=None, wait=True):
         """Admits many grids with one host wait.  `ptrs` may give raw pointers
         (page-locked host or device buffers are gathered on the device in one
         pass) instead of the numpy arrays'; with `ptrs`, `dims` (an n x 3 array
         of X, Y, Z) may replace `grids`.  Returns the tickets of the admitted
-        worlds (in order)."""
+        worlds (in order).  wait=False (with `ptrs`) returns once the uploads
+        are enqueued: the buffers must stay unchanged until wait_copies()."""
+        if not wait and ptrs is None:
+            raise ValueError("admit_many(wait=False) needs ptrs to buffers the caller keeps alive")
         n = len(ptrs) if grids is None else len(grids)
         spec = np.zeros(max(n, 1), dtype=_SPEC_DTYPE)
         keep = None
@@ -510,15 +516,18 @@ class Batch:
             spec["n_steps"][:n] = np.asarray(n_steps, dtype=np.int64)
         tickets = np.zeros(max(n, 1), dtype=np.uint64)
         done = i32()
-        st = lib().fs3d_batch_admit_many(self.handle, n, spec.ctypes.data_as(C.POINTER(WorldSpec)),
-                                         tickets.ctypes.data_as(C.POINTER(u64)), C.byref(done))
+        fn = lib().fs3d_batch_admit_many if wait else lib().fs3d_batch_admit_many_async
+        st = fn(self.handle, n, spec.ctypes.data_as(C.POINTER(WorldSpec)), tickets.ctypes.data_as(C.POINTER(u64)),
+                C.byref(done))
         if st not in (OK, ERR_BUDGET):
             check(st)
         del keep
         return tickets[:done.value].tolist()
 
-    def retire_many(self, tickets, out_ptrs=None) -> None:
-        """Retires worlds with one host wait; out_ptrs: host (or device) buffers, or None."""
+    def retire_many(self, tickets, out_ptrs=None, wait=True) -> None:
+        """Retires worlds with one host wait; out_ptrs: host (or device) buffers, or None.
+        wait=False returns once the read-backs are enqueued: the outputs hold
+        the grids after wait_copies()."""
         n = len(tickets)
         ts = np.asarray(tickets if n else [0], dtype=np.uint64)
         outs = None
@@ -528,7 +537,12 @@ class Batch:
             except TypeError:  # None entries: those worlds are not read back
                 outs_arr = np.asarray([p or 0 for p in out_ptrs], dtype=np.uint64)
             outs = outs_arr.ctypes.data_as(C.POINTER(vp))
-        check(lib().fs3d_batch_retire_many(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)), outs))
+        fn = lib().fs3d_batch_retire_many if wait else lib().fs3d_batch_retire_many_async
+        check(fn(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)), outs))
+
+    def wait_copies(self, timeout_ns: int = -1) -> None:
+        """Waits for every admission upload and read-back enqueued so far."""
+        check(lib().fs3d_batch_wait_copies(self.handle, timeout_ns))
 
     def try_admit(self, grid: np.ndarray, seed: int, n_steps: int, start_step: int = 0) -> Optional[int]:
         try:

@@ -7,14 +7,16 @@
 // runs alone or inside any mix.
 //
 // Streams: `stream` runs segments; `side` runs admissions (upload + format
-// conversion) and retirements (conversion + download), ordered against the
-// segments with events, so requests arriving while a segment runs are
-// uploaded concurrently.
+// conversion) and single retirements, `readback` the read-backs of
+// retire_many (conversion + download), all ordered against the segments with
+// events, so uploads and downloads run over the host link in both directions
+// while a segment computes.
 #include <string.h>
 
 #include <algorithm>
 
 #include <chrono>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -44,7 +46,31 @@ struct BWorld {
     std::shared_ptr<CUevent_st> finished;  // recorded after the segment that took its last step (shared)
     bool hash_valid = false;
     uint64_t hash = 0;
+    uint64_t admit_id = 0;                       // admission whose static-material check is pending (0: none)
+    std::shared_ptr<CUevent_st> admitted;       // planes written by admit_many (shared by its worlds)
+    std::shared_ptr<CUevent_st> statics_ready;  // static byte copy written
 };
+
+// An admit_many whose conversion is enqueued and whose per-world static
+// material flags are still on their way to the host: the worlds run from
+// their planes meanwhile; a world holding a material >= 4 gets its byte copy
+// (from the staging bytes) when the flags are read.
+struct PendingAdmit {
+    uint64_t id = 0;
+    cudaEvent_t done = nullptr;  // flags copied (admission stream)
+    int* flags = nullptr;        // page-locked, one per world
+    size_t flags_cap = 0;
+    uint8_t* staging = nullptr;  // the admitted bytes on the device
+    void* table = nullptr;       // conversion and copy tables
+    std::vector<uint64_t> tickets;
+    std::vector<int64_t> byte_off, cells;
+};
+
+std::shared_ptr<CUevent_st> shared_event() {
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return {};
+    return std::shared_ptr<CUevent_st>(ev, [](CUevent_st* x) { cudaEventDestroy(x); });
+}
 
 template <class T>
 struct PinnedArray {
@@ -95,7 +121,11 @@ struct fs3d_batch {
     cudaStream_t branch[kAllClasses + 1] = {};  // capture branches of a segment: one per class, then the per-step chain
     cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
     cudaEvent_t last_segment = nullptr;
-    std::vector<cudaEvent_t> pending_ready;  // admissions the next segment must wait for
+    std::vector<std::shared_ptr<CUevent_st>> pending_ready;  // admissions the next segment must wait for
+    cudaStream_t readback = nullptr;              // read-backs of retire_many
+    std::deque<PendingAdmit> pending_admits;      // in admission order
+    uint64_t next_admit_id = 1;
+    std::vector<std::pair<int*, size_t>> flag_pool;  // page-locked flag buffers free for reuse
     // segment graphs without and with the per-step kernel's launches (the
     // second only when some world is too large to be resident)
     cudaGraphExec_t graph = nullptr, graph_steps = nullptr;
@@ -124,7 +154,10 @@ namespace {
 
 // Worlds younger than this (steps since admission) are still mostly moving:
 // the hybrid mode keeps them in shared memory, where dense steps are cheap.
-constexpr uint64_t kYoungSteps = 256;
+// (2048 mixed worlds: 64-step segments at ages 0 / 64 / 128 / 192 take
+// 5.1 / 2.7 / 1.9 / 1.9 ms in shared memory and 8.5 / 3.4 / 1.6 / 1.3 ms
+// from L2, which wins from age 128 on.)
+constexpr uint64_t kYoungSteps = 128;
 
 // Segment class of a running world (-1: the per-step kernel) under the
 // batch's mode: 1 shared-memory classes, 2 global-memory classes, 3 hybrid
@@ -178,9 +211,72 @@ void free_world(fs3d_batch* b, BWorld& w) {
     if (w.statics) cudaFreeAsync(w.statics, b->side);
     if (w.ready) cudaEventDestroy(w.ready);
     w.finished.reset();
+    w.admitted.reset();
+    w.statics_ready.reset();
     w.rows = nullptr;
     w.statics = nullptr;
     w.ready = nullptr;
+}
+
+// A page-locked buffer of at least n flags, from the batch's pool.
+int* take_flags(fs3d_batch* b, size_t n, size_t* cap) {
+    for (size_t i = 0; i < b->flag_pool.size(); ++i)
+        if (b->flag_pool[i].second >= n) {
+            const auto f = b->flag_pool[i];
+            b->flag_pool.erase(b->flag_pool.begin() + (std::ptrdiff_t)i);
+            *cap = f.second;
+            return f.first;
+        }
+    const size_t c = std::max<size_t>(n, 1024);
+    int* f = nullptr;
+    if (cudaMallocHost((void**)&f, c * sizeof(int)) != cudaSuccess) return nullptr;
+    *cap = c;
+    return f;
+}
+
+// Completes the pending admissions with id <= upto, oldest first: reads their
+// static-material flags (waiting for them with `wait`, else stopping at the
+// first not yet on the host), gives each flagged world its byte copy and
+// frees the staging bytes.
+fs3d_status finalize_admits(fs3d_batch* b, uint64_t upto, bool wait) {
+    while (!b->pending_admits.empty() && b->pending_admits.front().id <= upto) {
+        PendingAdmit& p = b->pending_admits.front();
+        const cudaError_t q = wait ? cudaEventSynchronize(p.done) : cudaEventQuery(p.done);
+        if (q == cudaErrorNotReady) break;
+        if (q != cudaSuccess) return cuda_fail(q, "admission");
+        std::vector<BWorld*> flagged;
+        fs3d_status s = FS3D_OK;
+        for (size_t a = 0; a < p.tickets.size(); ++a) {
+            auto it = b->worlds.find(p.tickets[a]);
+            if (it == b->worlds.end()) continue;
+            BWorld& w = it->second;
+            w.admit_id = 0;
+            if (!p.flags[a] || s != FS3D_OK) continue;
+            const size_t cells = (size_t)p.cells[a];
+            cudaError_t e = cudaMallocAsync((void**)&w.statics, cells, b->side);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(w.statics, p.staging + p.byte_off[a], cells, cudaMemcpyDeviceToDevice, b->side);
+            if (e != cudaSuccess) {
+                s = cuda_fail(e, "static material copy");
+                continue;
+            }
+            w.bytes += cells;
+            b->used += cells;
+            flagged.push_back(&w);
+        }
+        if (!flagged.empty()) {
+            std::shared_ptr<CUevent_st> ready = shared_event();
+            if (ready && cudaEventRecord(ready.get(), b->side) == cudaSuccess)
+                for (BWorld* w : flagged) w->statics_ready = ready;
+        }
+        cudaFreeAsync(p.staging, b->side);
+        cudaFreeAsync(p.table, b->side);
+        b->flag_pool.emplace_back(p.flags, p.flags_cap);
+        cudaEventDestroy(p.done);
+        b->pending_admits.pop_front();
+        if (s != FS3D_OK) return s;
+    }
+    return FS3D_OK;
 }
 
 // One segment on stream `a`: the resident kernel of every class (worlds that
@@ -194,8 +290,10 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
     }
     fs3d_status s = FS3D_OK;
     const int mode = b->cfg.use_smem;
+    // shared-memory classes widest first: their worlds are the largest and
+    // take the longest, and the launch order is the order the SMs fill in
     if (mode == 1 || mode == 3)
-        for (int c = 0; c < kResidentClasses && s == FS3D_OK; ++c)
+        for (int c = kResidentClasses - 1; c >= 0 && s == FS3D_OK; --c)
             s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
                                               fork ? b->branch[c] : a, b->processed_dev);
     if (mode == 2 || mode == 3)
@@ -262,6 +360,7 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     b->grid = sm_count_public() * per_sm;
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->readback, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
@@ -486,10 +585,7 @@ fs3d_status build_tables(fs3d_batch* b) {
         for (int x : v) b->to.h[si++] = x;
     }
     // admissions complete before the segment reads their planes
-    for (cudaEvent_t ev : b->pending_ready) {
-        FS3D_CUDA(cudaStreamWaitEvent(b->stream, ev, 0));
-        cudaEventDestroy(ev);
-    }
+    for (auto& ev : b->pending_ready) FS3D_CUDA(cudaStreamWaitEvent(b->stream, ev.get(), 0));
     b->pending_ready.clear();
     for (auto& kv : b->worlds)
         if (kv.second.ready) {
@@ -572,7 +668,8 @@ fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns) {
     int err = 0;
     FS3D_CUDA(cudaMemcpy(&err, b->err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
-    return wait_stream(b->side, timeout_ns);
+    s = wait_stream(b->side, timeout_ns);
+    return s == FS3D_OK ? wait_stream(b->readback, timeout_ns) : s;
 }
 
 fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash) {
@@ -582,6 +679,10 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
     BWorld& w = it->second;
     *done = 0;
     if (!w.done) return FS3D_OK;
+    if (w.admit_id && hash) {
+        const fs3d_status f = finalize_admits(b, w.admit_id, true);
+        if (f != FS3D_OK) return f;
+    }
     if (w.finished) {
         const cudaError_t q = cudaEventQuery(w.finished.get());
         if (q == cudaErrorNotReady) return FS3D_OK;
@@ -612,6 +713,10 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
     auto it = b->worlds.find(ticket);
     if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire: unknown ticket");
     BWorld& w = it->second;
+    if (w.admit_id) {
+        const fs3d_status f = finalize_admits(b, w.admit_id, true);
+        if (f != FS3D_OK) return f;
+    }
     FS3D_CUDA(cudaStreamWaitEvent(b->side, w.finished ? w.finished.get() : b->last_segment, 0));
     if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
     fs3d_status s = FS3D_OK;
@@ -637,8 +742,17 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
 
 extern "C" {
 
-fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
-                                  int* n_admitted) {
+}  // extern "C"
+
+namespace {
+
+// Admits specs[0..k) (k: as many as fit) with one upload per contiguous run,
+// one conversion launch and one flag read-back.  With `wait` it returns once
+// the callers' grids have been copied and the static-material flags read;
+// otherwise once everything is enqueued (the grids must stay unchanged until
+// the admission stream has run: fs3d_batch_wait_copies).
+fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets, int* n_admitted,
+                            bool wait) {
     if (!b || n < 0 || (n > 0 && (!specs || !tickets)) || !n_admitted)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_admit_many: bad args");
     *n_admitted = 0;
@@ -656,7 +770,14 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         used += need;
     }
     if (k == 0) return n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: nothing fits in the budget now") : FS3D_OK;
-    // one staging buffer, one copy per world, one conversion launch for all
+    // older asynchronous admissions whose flags have arrived are completed first
+    fs3d_status s = finalize_admits(b, UINT64_MAX, false);
+    if (s != FS3D_OK) return s;
+    PendingAdmit pa;
+    pa.id = b->next_admit_id++;
+    pa.flags = take_flags(b, (size_t)k, &pa.flags_cap);
+    if (!pa.flags) return set_error(FS3D_ERR_CUDA, "fs3d_batch_admit_many: page-locked flag buffer");
+    // one staging buffer, one copy per run of contiguous grids, one conversion launch for all
     std::vector<ConvJob> jobs((size_t)k);
     std::vector<int64_t> unit_off((size_t)k);
     std::vector<uint4*> rows((size_t)k, nullptr);
@@ -671,18 +792,18 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         j.Z = p.Z;
         j.nw = plane_nw(p.X);
         unit_off[(size_t)a] = units;
+        pa.tickets.push_back(0);
+        pa.byte_off.push_back(bytes_total);
+        pa.cells.push_back((int64_t)p.X * p.Y * p.Z);
         bytes_total += ((int64_t)p.X * p.Y * p.Z + 15) / 16 * 16;
         units += (int64_t)p.Y * p.Z * j.nw;
     }
-    uint8_t* staging = nullptr;
-    void* table = nullptr;
     const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k, off_bytes = sizeof(int64_t) * (size_t)k;
     const size_t flags_off = (jobs_bytes + off_bytes + 15) / 16 * 16;
     const size_t copy_off = (flags_off + sizeof(int) * (size_t)k + 15) / 16 * 16;
     const size_t copy_bytes = sizeof(CopyJob) * (size_t)k + sizeof(int64_t) * (size_t)k;
-    fs3d_status s = FS3D_OK;
-    cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
-    if (e == cudaSuccess) e = cudaMallocAsync(&table, copy_off + copy_bytes, b->side);
+    cudaError_t e = cudaMallocAsync((void**)&pa.staging, (size_t)bytes_total, b->side);
+    if (e == cudaSuccess) e = cudaMallocAsync(&pa.table, copy_off + copy_bytes, b->side);
     // grids the device can address (page-locked host or device memory) that lie
     // back to back go over in one copy-engine transfer per run (the SMs stay
     // free for segments in flight); other device-addressable grids are gathered
@@ -701,6 +822,7 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     if (e == cudaSuccess) e = cudaMallocAsync(&block, block_bytes, b->side);
     for (int a = 0; a < k; ++a)
         rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
+    uint8_t* staging = pa.staging;
     for (int a = 0; a < k && e == cudaSuccess;) {
         const int64_t cells = (int64_t)specs[a].X * specs[a].Y * specs[a].Z;
         const uint8_t* dv = device_view(specs[a].grid);
@@ -725,11 +847,11 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         a = e_run;
     }
     for (int a = 0; a < k; ++a) jobs[(size_t)a].rows = rows[(size_t)a];
-    ConvJob* jobs_dev = static_cast<ConvJob*>(table);
-    int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
-    int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(table) + flags_off);
-    CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);
-    int64_t* chunk_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
+    ConvJob* jobs_dev = static_cast<ConvJob*>(pa.table);
+    int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(pa.table) + jobs_bytes);
+    int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(pa.table) + flags_off);
+    CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(pa.table) + copy_off);
+    int64_t* chunk_dev = reinterpret_cast<int64_t*>(static_cast<char*>(pa.table) + copy_off + sizeof(CopyJob) * (size_t)k);
     // the tables are pageable: staged before the calls return
     if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
     if (e == cudaSuccess) e = cudaMemcpyAsync(off_dev, unit_off.data(), off_bytes, cudaMemcpyHostToDevice, b->side);
@@ -743,34 +865,25 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
     if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many upload");
     if (s == FS3D_OK) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side);
     if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, k, units, staging, flags_dev, b->side);
-    std::vector<int> flags((size_t)k, 0);
+    // segments may start once the planes are written
+    std::shared_ptr<CUevent_st> admitted;
     if (s == FS3D_OK) {
-        e = cudaMemcpyAsync(flags.data(), flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
-        // the callers' grids may be reused once this returns
-        if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
+        admitted = shared_event();
+        e = admitted ? cudaEventRecord(admitted.get(), b->side) : cudaErrorMemoryAllocation;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(pa.flags, flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pa.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(pa.done, b->side);
         if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many conversion");
     }
-    // worlds holding a material >= 4 keep a byte copy for read-back
-    std::vector<uint8_t*> statics((size_t)k, nullptr);
-    for (int a = 0; a < k && s == FS3D_OK; ++a) {
-        if (!flags[(size_t)a]) continue;
-        const size_t cells = (size_t)specs[a].X * specs[a].Y * specs[a].Z;
-        e = cudaMallocAsync((void**)&statics[(size_t)a], cells, b->side);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(statics[(size_t)a], staging + jobs[(size_t)a].byte_off, cells, cudaMemcpyDeviceToDevice,
-                                b->side);
-        if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many static copy");
-    }
-    if (staging) cudaFreeAsync(staging, b->side);
-    if (table) cudaFreeAsync(table, b->side);
     if (s != FS3D_OK) {
+        if (pa.staging) cudaFreeAsync(pa.staging, b->side);
+        if (pa.table) cudaFreeAsync(pa.table, b->side);
         if (block) cudaFreeAsync(block, b->side);
-        for (int a = 0; a < k; ++a)
-            if (statics[(size_t)a]) cudaFreeAsync(statics[(size_t)a], b->side);
+        if (pa.done) cudaEventDestroy(pa.done);
+        b->flag_pool.emplace_back(pa.flags, pa.flags_cap);
         return s;
     }
-    cudaEvent_t ready = nullptr;
-    if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) == cudaSuccess) cudaEventRecord(ready, b->side);
     cudaStream_t side = b->side;
     std::shared_ptr<void> arena(block, [side](void* p) { cudaFreeAsync(p, side); });
     for (int a = 0; a < k; ++a) {
@@ -788,35 +901,67 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
         w.rows = rows[(size_t)a];
         w.arena = arena;
         w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(p.X, p.Y, p.Z);
-        w.statics = statics[(size_t)a];
-        w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld) +
-                  (w.statics ? (size_t)p.X * p.Y * p.Z : 0);
+        w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld);
+        w.admit_id = pa.id;
+        w.admitted = admitted;
         b->used += w.bytes;
         tickets[a] = b->next_ticket++;
+        pa.tickets[(size_t)a] = tickets[a];
         b->worlds.emplace(tickets[a], w);
     }
     b->tables_stale = true;
-    // the next segment runs after the static copies (side stream) are done
-    if (ready) {
-        b->pending_ready.push_back(ready);
-    }
+    b->pending_ready.push_back(admitted);
+    const uint64_t id = pa.id;
+    b->pending_admits.push_back(std::move(pa));
+    // with `wait` the callers' grids may be reused once this returns; without,
+    // few admissions stay open (each holds its staging bytes)
+    s = wait ? finalize_admits(b, id, true)
+             : (b->pending_admits.size() > 4 ? finalize_admits(b, b->pending_admits.front().id, true) : FS3D_OK);
     *n_admitted = k;
+    if (s != FS3D_OK) return s;
     return k < n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: the remaining worlds do not fit now") : FS3D_OK;
 }
 
-fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
+// Retires tickets[0..n): the read-backs (conversion + copy into grids_out[a]
+// where given) run on the read-back stream after each world's last segment;
+// with `wait` it returns once the outputs hold the grids.
+fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out, bool wait) {
     if (!b || n < 0 || (n > 0 && !tickets)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: bad args");
     std::vector<std::map<uint64_t, BWorld>::iterator> its;
     its.reserve((size_t)n);
+    uint64_t need = 0;
     for (int a = 0; a < n; ++a) {
         auto it = b->worlds.find(tickets[a]);
         if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire_many: unknown ticket");
         its.push_back(it);
+        need = std::max(need, it->second.admit_id);
     }
-    // every world's planes are final after the last segment enqueued so far
-    FS3D_CUDA(cudaStreamWaitEvent(b->side, b->last_segment, 0));
-    for (cudaEvent_t ev : b->pending_ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, ev, 0));
+    // the static-material copies must exist before the read-back
+    if (need) {
+        const fs3d_status f = finalize_admits(b, need, true);
+        if (f != FS3D_OK) return f;
+    }
+    cudaStream_t rb = b->readback;
+    {
+        // each world's planes are final after its last segment (a world not
+        // done yet: the last segment enqueued so far); admissions and static
+        // copies must have run
+        std::vector<CUevent_st*> deps;
+        auto dep = [&](CUevent_st* ev) {
+            if (ev && std::find(deps.begin(), deps.end(), ev) == deps.end()) deps.push_back(ev);
+        };
+        for (auto it : its) {
+            const BWorld& w = it->second;
+            dep(w.finished ? w.finished.get() : (b->segments ? b->last_segment : nullptr));
+            dep(w.admitted.get());
+            dep(w.ready);
+            dep(w.statics_ready.get());
+        }
+        for (CUevent_st* ev : deps) FS3D_CUDA(cudaStreamWaitEvent(rb, ev, 0));
+    }
     fs3d_status s = FS3D_OK;
+    uint8_t* staging = nullptr;
+    void* table = nullptr;
     if (grids_out) {
         std::vector<ConvJob> jobs;
         std::vector<int64_t> unit_off;
@@ -841,27 +986,24 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
         }
         const int k = (int)jobs.size();
         if (k) {
-            uint8_t* staging = nullptr;
-            void* table = nullptr;
             const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k;
             const size_t copy_off = (jobs_bytes + sizeof(int64_t) * (size_t)k + 15) / 16 * 16;
-            cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, b->side);
+            cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, rb);
             if (e == cudaSuccess)
-                e = cudaMallocAsync(&table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, b->side);
+                e = cudaMallocAsync(&table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, rb);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, rb);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(off_dev, unit_off.data(), sizeof(int64_t) * (size_t)k, cudaMemcpyHostToDevice,
-                                    b->side);
+                e = cudaMemcpyAsync(off_dev, unit_off.data(), sizeof(int64_t) * (size_t)k, cudaMemcpyHostToDevice, rb);
             if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
-            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, b->side);
+            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, rb);
             // outputs the device can address are written by one copy kernel,
-            // pageable ones take a copy call each
+            // pageable ones take a copy call each; outputs lying back to back
+            // go back in one copy-engine transfer per run
             std::vector<CopyJob> copies;
             std::vector<int64_t> chunk_off;
             int64_t chunks = 0;
-            // outputs lying back to back go back in one copy-engine transfer per run
             for (int q = 0; q < k && s == FS3D_OK;) {
                 uint8_t* out = grids_out[who[(size_t)q]];
                 const BWorld& w = its[(size_t)who[(size_t)q]]->second;
@@ -880,8 +1022,7 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
                     ++e_run;
                 }
                 if (!dv || e_run - q > 1) {
-                    e = cudaMemcpyAsync(out, staging + jobs[(size_t)q].byte_off, (size_t)run_bytes, cudaMemcpyDefault,
-                                        b->side);
+                    e = cudaMemcpyAsync(out, staging + jobs[(size_t)q].byte_off, (size_t)run_bytes, cudaMemcpyDefault, rb);
                     if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
                 } else {
                     copies.push_back(CopyJob{staging + jobs[(size_t)q].byte_off, dv, cells});
@@ -895,24 +1036,64 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
                 int64_t* chunk_dev =
                     reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
                 e = cudaMemcpyAsync(copies_dev, copies.data(), sizeof(CopyJob) * copies.size(), cudaMemcpyHostToDevice,
-                                    b->side);
+                                    rb);
                 if (e == cudaSuccess)
                     e = cudaMemcpyAsync(chunk_dev, chunk_off.data(), sizeof(int64_t) * chunk_off.size(),
-                                        cudaMemcpyHostToDevice, b->side);
-                s = e == cudaSuccess ? copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side)
+                                        cudaMemcpyHostToDevice, rb);
+                s = e == cudaSuccess ? copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, rb)
                                      : cuda_fail(e, "fs3d_batch_retire_many readback table");
             }
-            if (staging) cudaFreeAsync(staging, b->side);
-            if (table) cudaFreeAsync(table, b->side);
         }
     }
+    // the worlds' memory is released on the admission stream once the
+    // read-back has read it
+    {
+        cudaEvent_t read = nullptr;
+        cudaError_t e = cudaEventCreateWithFlags(&read, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(read, rb);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, read, 0);
+        if (read) cudaEventDestroy(read);
+        if (e != cudaSuccess && s == FS3D_OK) s = cuda_fail(e, "fs3d_batch_retire_many ordering");
+    }
+    if (staging) cudaFreeAsync(staging, rb);
+    if (table) cudaFreeAsync(table, rb);
     for (auto it : its) {
         b->used -= it->second.bytes;
         free_world(b, it->second);
         b->worlds.erase(it);
     }
     if (!its.empty()) b->tables_stale = true;
-    FS3D_CUDA(cudaStreamSynchronize(b->side));
+    if (wait && s == FS3D_OK) FS3D_CUDA(cudaStreamSynchronize(rb));
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
+                                  int* n_admitted) {
+    return admit_many_impl(b, n, specs, tickets, n_admitted, true);
+}
+
+fs3d_status fs3d_batch_admit_many_async(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
+                                        int* n_admitted) {
+    return admit_many_impl(b, n, specs, tickets, n_admitted, false);
+}
+
+fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
+    return retire_many_impl(b, n, tickets, grids_out, true);
+}
+
+fs3d_status fs3d_batch_retire_many_async(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
+    return retire_many_impl(b, n, tickets, grids_out, false);
+}
+
+fs3d_status fs3d_batch_wait_copies(fs3d_batch* b, int64_t timeout_ns) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_wait_copies: NULL batch");
+    fs3d_status s = wait_stream(b->readback, timeout_ns);
+    if (s == FS3D_OK) s = wait_stream(b->side, timeout_ns);
+    if (s == FS3D_OK) s = finalize_admits(b, UINT64_MAX, false);
     return s;
 }
 
@@ -1093,12 +1274,15 @@ fs3d_status fs3d_batch_stream(fs3d_batch* b, void** stream) {
 fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_destroy: NULL batch");
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->readback) cudaStreamSynchronize(b->readback);
     if (b->side) cudaStreamSynchronize(b->side);
+    finalize_admits(b, UINT64_MAX, true);
     for (auto& kv : b->worlds) free_world(b, kv.second);
     b->worlds.clear();
-    for (cudaEvent_t ev : b->pending_ready) cudaEventDestroy(ev);
     b->pending_ready.clear();
     if (b->side) cudaStreamSynchronize(b->side);
+    for (auto& f : b->flag_pool) cudaFreeHost(f.first);
+    b->flag_pool.clear();
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->graph_steps) cudaGraphExecDestroy(b->graph_steps);
     b->tw.release();
@@ -1118,6 +1302,7 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     if (b->last_segment) cudaEventDestroy(b->last_segment);
     if (b->stream) cudaStreamDestroy(b->stream);
     if (b->side) cudaStreamDestroy(b->side);
+    if (b->readback) cudaStreamDestroy(b->readback);
     delete b;
     return FS3D_OK;
 }

@@ -81,7 +81,7 @@ typedef struct fs3d_config {
                               one launch): 1 = the planes are held in shared memory
                               (worlds that fit); 2 = the planes stay in global
                               memory (L2), one CTA per world sized by the work of
-                              one layer; 3 (default) = 1 for a world's first 256
+                              one layer; 3 (default) = 1 for a world's first 128
                               steps, then 2; 0 = the per-step kernel only          */
     int reserved[12];
 } fs3d_config;
@@ -181,6 +181,12 @@ typedef struct fs3d_world_spec {
 } fs3d_world_spec;
 fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
                                   int* n_admitted);
+/* The same, returning once the uploads and conversions are enqueued on the
+ * admission stream (no host wait): the grids must stay unchanged until
+ * fs3d_batch_wait_copies returns.  Segments wait for the conversions by
+ * themselves; uploads overlap a segment already running. */
+fs3d_status fs3d_batch_admit_many_async(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
+                                        int* n_admitted);
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream */
 fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
 /* done = 1 once the world has taken all its steps; hash valid when done */
@@ -189,6 +195,13 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
 fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out);
 /* retire n worlds with one host wait; grids_out (nullable) holds n host pointers (nullable each) */
 fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
+/* The same without the host wait: the read-backs run on their own stream after
+ * each world's last segment (downloads overlap later segments); grids_out
+ * holds the grids once fs3d_batch_wait_copies returns. */
+fs3d_status fs3d_batch_retire_many_async(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
+/* Waits (timeout_ns < 0: without limit) until every admission and read-back
+ * enqueued so far has run. */
+fs3d_status fs3d_batch_wait_copies(fs3d_batch* b, int64_t timeout_ns);
 /* Autotuner: times each candidate launch configuration on trial_segments real
  * segments of the live worlds (they advance as usual), keeps the fastest per
  * voxel-update and remembers it for batches of the same make-up (live worlds

@@ -435,3 +435,85 @@ def test_tables_reused_between_changes(fs3d, orc):
             assert h == orc.hash(oracle_final(orc, fs3d, dims, seed, n, start=start)), dims
         dense = b.counters()["dense_cell_steps"]
         assert dense == sum(X * Y * Z * n for (X, Y, Z), _, n in worlds) + 32 ** 3 * 8 * S
+
+
+def _with_statics(fs3d, worlds, every=3):
+    """Batch worlds; every `every`-th one also holds static materials (bytes
+    >= 4), which stay in place and come back unchanged on read-back."""
+    grids = []
+    for i, (dims, seed) in enumerate(worlds):
+        g = fs3d.gen_batch_world(seed, *dims)
+        if i % every == 1:
+            rng = np.random.default_rng(seed)
+            idx = rng.integers(0, g.size, 64)
+            g.reshape(-1)[idx] = rng.integers(4, 256, 64).astype(np.uint8)
+        grids.append(g)
+    return grids
+
+
+def test_pipelined_async_admit_and_retire(fs3d, orc, cuda):
+    """admit_many_async / retire_many_async pipelined on one batch the way a
+    server overlaps the host link with compute: step i+1's uploads are
+    enqueued before step i's read-backs and before segment i+1.  Worlds with
+    static materials get their byte copies once their flags reach the host.
+    Every output equals the oracle."""
+    S = 32
+    worlds = small_batch(fs3d, 41, 10, max_dim=64) + [((37, 21, 13), 904), ((5, 7, 3), 905)]
+    grids = _with_statics(fs3d, worlds[:-1]) + [orc.gen_c1(905, 5, 7, 3)]
+    sizes = [g.size for g in grids]
+    offs = [int(v) for v in np.concatenate([[0], np.cumsum(sizes)[:-1]])]
+    total = int(sum(sizes))
+    src = cuda.from_numpy(np.concatenate([g.reshape(-1) for g in grids])).pin_memory()
+    steps = 4
+    outs = [cuda.zeros(total, dtype=cuda.uint8).pin_memory() for _ in range(steps)]
+    seeds = [s for _, s in worlds]
+    dims = [d for d, _ in worlds]
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        prev = None
+        for i in range(steps):
+            ts = b.admit_many(None, seeds, S, start_steps=[1000 * i] * len(worlds),
+                              ptrs=[src.data_ptr() + o for o in offs], dims=dims, wait=False)
+            assert len(ts) == len(worlds)
+            if prev is not None:
+                b.retire_many(prev[0], [outs[prev[1]].data_ptr() + o for o in offs], wait=False)
+            b.run_segment()
+            prev = (ts, i)
+        b.retire_many(prev[0], [outs[prev[1]].data_ptr() + o for o in offs], wait=False)
+        b.wait_copies()
+        assert b.stats()["live_worlds"] == 0 and b.stats()["bytes_used"] == 0
+    for i in range(steps):
+        got = outs[i].numpy()
+        for (d, seed), g, o, n in zip(worlds, grids, offs, sizes):
+            ref = g.copy()
+            orc.run(ref, seed, 1000 * i, S, nthreads=0)
+            assert (got[o:o + n].reshape(g.shape) == ref).all(), (i, d)
+
+
+def test_async_admission_poll_and_single_retire(fs3d, orc, cuda):
+    """A world admitted without a host wait can be polled (its hash needs the
+    static copy) and retired singly before any other call completes its
+    admission; a synchronous admit_many of static worlds still reads back."""
+    worlds = small_batch(fs3d, 43, 6, max_dim=48)
+    grids = _with_statics(fs3d, worlds, every=2)
+    pinned = [cuda.from_numpy(g.copy()).pin_memory() for g in grids]
+    n = 40
+    with fs3d.Batch(GiB, steps_per_segment=64) as b:
+        ts = b.admit_many(None, [s for _, s in worlds], n, ptrs=[p.data_ptr() for p in pinned],
+                          dims=[d for d, _ in worlds], wait=False)
+        b.run_segment()
+        b.sync()
+        for t, (d, seed), g in zip(ts, worlds, grids):
+            ref = g.copy()
+            orc.run(ref, seed, 0, n, nthreads=0)
+            done, h = b.poll(t)
+            assert done and h == orc.hash(ref), d
+            X, Y, Z = d
+            assert (b.retire(t, (Y, Z, X)) == ref).all(), d
+        ts = b.admit_many(grids, [s for _, s in worlds], n)
+        b.run_segment()
+        outs = [np.zeros_like(g) for g in grids]
+        b.retire_many(ts, [o.ctypes.data for o in outs])
+        for o, (d, seed), g in zip(outs, worlds, grids):
+            ref = g.copy()
+            orc.run(ref, seed, 0, n, nthreads=0)
+            assert (o == ref).all(), d
