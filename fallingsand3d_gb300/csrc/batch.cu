@@ -47,6 +47,7 @@ struct BWorld {
     bool hash_valid = false;
     uint64_t hash = 0;
     uint64_t admit_id = 0;                       // admission whose static-material check is pending (0: none)
+    int admit_index = 0;                         // the world's place in that admission
     std::shared_ptr<CUevent_st> admitted;       // planes written by admit_many (shared by its worlds)
     std::shared_ptr<CUevent_st> statics_ready;  // static byte copy written
 };
@@ -62,6 +63,7 @@ struct PendingAdmit {
     size_t flags_cap = 0;
     uint8_t* staging = nullptr;  // the admitted bytes on the device
     void* table = nullptr;       // conversion and copy tables
+    const int* flags_dev = nullptr;  // the flags in `table`
     std::vector<uint64_t> tickets;
     std::vector<int64_t> byte_off, cells;
 };
@@ -126,6 +128,15 @@ struct fs3d_batch {
     std::deque<PendingAdmit> pending_admits;      // in admission order
     uint64_t next_admit_id = 1;
     std::vector<std::pair<int*, size_t>> flag_pool;  // page-locked flag buffers free for reuse
+    // page-locked staging of the small job tables (a copy from pageable memory
+    // would wait for the copies queued before it); a chunk is reused once the
+    // event recorded after its upload has completed
+    struct HostChunk {
+        char* p = nullptr;
+        size_t cap = 0;
+        cudaEvent_t uploaded = nullptr;
+    };
+    std::vector<HostChunk> host_chunks;
     // segment graphs without and with the per-step kernel's launches (the
     // second only when some world is too large to be resident)
     cudaGraphExec_t graph = nullptr, graph_steps = nullptr;
@@ -232,6 +243,30 @@ int* take_flags(fs3d_batch* b, size_t n, size_t* cap) {
     if (cudaMallocHost((void**)&f, c * sizeof(int)) != cudaSuccess) return nullptr;
     *cap = c;
     return f;
+}
+
+// A page-locked chunk of at least n bytes whose last upload has run (index
+// into b->host_chunks); upload_chunk copies it to the device and marks it in use.
+int take_chunk(fs3d_batch* b, size_t n) {
+    for (size_t i = 0; i < b->host_chunks.size(); ++i) {
+        auto& c = b->host_chunks[i];
+        if (c.cap >= n && cudaEventQuery(c.uploaded) == cudaSuccess) return (int)i;
+    }
+    fs3d_batch::HostChunk c;
+    c.cap = std::max<size_t>(n, (size_t)1 << 16);
+    if (cudaMallocHost((void**)&c.p, c.cap) != cudaSuccess) return -1;
+    if (cudaEventCreateWithFlags(&c.uploaded, cudaEventDisableTiming) != cudaSuccess) {
+        cudaFreeHost(c.p);
+        return -1;
+    }
+    b->host_chunks.push_back(c);
+    return (int)b->host_chunks.size() - 1;
+}
+
+cudaError_t upload_chunk(fs3d_batch* b, int i, void* dst, size_t n, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(dst, b->host_chunks[(size_t)i].p, n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->host_chunks[(size_t)i].uploaded, st);
+    return e;
 }
 
 // Completes the pending admissions with id <= upto, oldest first: reads their
@@ -786,6 +821,8 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         const fs3d_world_spec& p = specs[a];
         ConvJob& j = jobs[(size_t)a];
         j.statics = nullptr;
+        j.static_flag = nullptr;
+        j.static_src = nullptr;
         j.byte_off = bytes_total;
         j.X = p.X;
         j.Y = p.Y;
@@ -850,18 +887,28 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     ConvJob* jobs_dev = static_cast<ConvJob*>(pa.table);
     int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(pa.table) + jobs_bytes);
     int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(pa.table) + flags_off);
+    pa.flags_dev = flags_dev;
     CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(pa.table) + copy_off);
     int64_t* chunk_dev = reinterpret_cast<int64_t*>(static_cast<char*>(pa.table) + copy_off + sizeof(CopyJob) * (size_t)k);
-    // the tables are pageable: staged before the calls return
-    if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, b->side);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(off_dev, unit_off.data(), off_bytes, cudaMemcpyHostToDevice, b->side);
-    if (e == cudaSuccess) e = cudaMemsetAsync(flags_dev, 0, sizeof(int) * (size_t)k, b->side);
-    if (e == cudaSuccess && !copies.empty())
-        e = cudaMemcpyAsync(copies_dev, copies.data(), sizeof(CopyJob) * copies.size(), cudaMemcpyHostToDevice,
-                            b->side);
-    if (e == cudaSuccess && !copies.empty())
-        e = cudaMemcpyAsync(chunk_dev, chunk_off.data(), sizeof(int64_t) * chunk_off.size(), cudaMemcpyHostToDevice,
-                            b->side);
+    // the whole table (jobs, offsets, zeroed flags, copy jobs) in one upload
+    // from a page-locked image, so nothing here waits for the grid uploads
+    if (e == cudaSuccess) {
+        const size_t image = copy_off + copy_bytes;
+        const int ci = take_chunk(b, image);
+        if (ci < 0) {
+            e = cudaErrorMemoryAllocation;
+        } else {
+            char* h = b->host_chunks[(size_t)ci].p;
+            memcpy(h, jobs.data(), jobs_bytes);
+            memcpy(h + jobs_bytes, unit_off.data(), off_bytes);
+            memset(h + flags_off, 0, copy_off - flags_off);
+            if (!copies.empty()) {
+                memcpy(h + copy_off, copies.data(), sizeof(CopyJob) * copies.size());
+                memcpy(h + copy_off + sizeof(CopyJob) * (size_t)k, chunk_off.data(), sizeof(int64_t) * chunk_off.size());
+            }
+            e = upload_chunk(b, ci, pa.table, image, b->side);
+        }
+    }
     if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many upload");
     if (s == FS3D_OK) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side);
     if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, k, units, staging, flags_dev, b->side);
@@ -903,6 +950,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(p.X, p.Y, p.Z);
         w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld);
         w.admit_id = pa.id;
+        w.admit_index = a;
         w.admitted = admitted;
         b->used += w.bytes;
         tickets[a] = b->next_ticket++;
@@ -922,6 +970,18 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     return k < n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: the remaining worlds do not fit now") : FS3D_OK;
 }
 
+// The worlds' memory is freed on the admission stream: it waits until the
+// read-back stream has converted them (the download of the bytes that follows
+// does not hold up later uploads).
+fs3d_status release_after_read(fs3d_batch* b, cudaStream_t rb) {
+    cudaEvent_t read = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&read, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(read, rb);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, read, 0);
+    if (read) cudaEventDestroy(read);
+    return e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_retire_many ordering");
+}
+
 // Retires tickets[0..n): the read-backs (conversion + copy into grids_out[a]
 // where given) run on the read-back stream after each world's last segment;
 // with `wait` it returns once the outputs hold the grids.
@@ -929,18 +989,23 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
     if (!b || n < 0 || (n > 0 && !tickets)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: bad args");
     std::vector<std::map<uint64_t, BWorld>::iterator> its;
     its.reserve((size_t)n);
-    uint64_t need = 0;
     for (int a = 0; a < n; ++a) {
         auto it = b->worlds.find(tickets[a]);
         if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire_many: unknown ticket");
         its.push_back(it);
-        need = std::max(need, it->second.admit_id);
     }
-    // the static-material copies must exist before the read-back
-    if (need) {
-        const fs3d_status f = finalize_admits(b, need, true);
+    // admissions whose flags have arrived are completed (static copies made);
+    // a world whose admission is still open reads its static bytes, if its
+    // flag says it has any, straight from that admission's staging bytes
+    {
+        const fs3d_status f = finalize_admits(b, UINT64_MAX, false);
         if (f != FS3D_OK) return f;
     }
+    auto pending_of = [&](uint64_t id) -> const PendingAdmit* {
+        for (const PendingAdmit& p : b->pending_admits)
+            if (p.id == id) return &p;
+        return nullptr;
+    };
     cudaStream_t rb = b->readback;
     {
         // each world's planes are final after its last segment (a world not
@@ -962,6 +1027,7 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
     fs3d_status s = FS3D_OK;
     uint8_t* staging = nullptr;
     void* table = nullptr;
+    bool released = false;  // the admission stream (which frees the worlds) waits for the conversion
     if (grids_out) {
         std::vector<ConvJob> jobs;
         std::vector<int64_t> unit_off;
@@ -973,6 +1039,13 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
             ConvJob j;
             j.rows = w.rows;
             j.statics = w.statics;
+            j.static_flag = nullptr;
+            j.static_src = nullptr;
+            if (w.admit_id)
+                if (const PendingAdmit* pa = pending_of(w.admit_id)) {
+                    j.static_flag = pa->flags_dev + w.admit_index;
+                    j.static_src = pa->staging + pa->byte_off[(size_t)w.admit_index];
+                }
             j.byte_off = bytes_total;
             j.X = w.X;
             j.Y = w.Y;
@@ -993,17 +1066,27 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 e = cudaMallocAsync(&table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, rb);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(jobs_dev, jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, rb);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(off_dev, unit_off.data(), sizeof(int64_t) * (size_t)k, cudaMemcpyHostToDevice, rb);
+            // the copy jobs are only known below: the table goes up in one
+            // page-locked image once they are
             if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
-            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, rb);
-            // outputs the device can address are written by one copy kernel,
-            // pageable ones take a copy call each; outputs lying back to back
-            // go back in one copy-engine transfer per run
+            int ci = -1;
+            const size_t image = copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k;
+            if (s == FS3D_OK) {
+                ci = take_chunk(b, image);
+                if (ci < 0) s = set_error(FS3D_ERR_CUDA, "fs3d_batch_retire_many: page-locked table");
+            }
+            char* h = ci >= 0 ? b->host_chunks[(size_t)ci].p : nullptr;
+            if (h) {
+                memcpy(h, jobs.data(), jobs_bytes);
+                memcpy(h + jobs_bytes, unit_off.data(), sizeof(int64_t) * (size_t)k);
+            }
             std::vector<CopyJob> copies;
             std::vector<int64_t> chunk_off;
             int64_t chunks = 0;
+            std::vector<std::pair<int, int64_t>> runs;  // (first job, bytes) of each copy-engine run
+            // outputs the device can address are written by one copy kernel,
+            // pageable ones take a copy call each; outputs lying back to back
+            // go back in one copy-engine transfer per run
             for (int q = 0; q < k && s == FS3D_OK;) {
                 uint8_t* out = grids_out[who[(size_t)q]];
                 const BWorld& w = its[(size_t)who[(size_t)q]]->second;
@@ -1022,8 +1105,7 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                     ++e_run;
                 }
                 if (!dv || e_run - q > 1) {
-                    e = cudaMemcpyAsync(out, staging + jobs[(size_t)q].byte_off, (size_t)run_bytes, cudaMemcpyDefault, rb);
-                    if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+                    runs.emplace_back(q, run_bytes);
                 } else {
                     copies.push_back(CopyJob{staging + jobs[(size_t)q].byte_off, dv, cells});
                     chunk_off.push_back(chunks);
@@ -1031,29 +1113,32 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 }
                 q = e_run;
             }
-            if (s == FS3D_OK && !copies.empty()) {
-                CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);
-                int64_t* chunk_dev =
-                    reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
-                e = cudaMemcpyAsync(copies_dev, copies.data(), sizeof(CopyJob) * copies.size(), cudaMemcpyHostToDevice,
-                                    rb);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(chunk_dev, chunk_off.data(), sizeof(int64_t) * chunk_off.size(),
-                                        cudaMemcpyHostToDevice, rb);
-                s = e == cudaSuccess ? copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, rb)
-                                     : cuda_fail(e, "fs3d_batch_retire_many readback table");
+            CopyJob* copies_dev = reinterpret_cast<CopyJob*>(static_cast<char*>(table) + copy_off);
+            int64_t* chunk_dev =
+                reinterpret_cast<int64_t*>(static_cast<char*>(table) + copy_off + sizeof(CopyJob) * (size_t)k);
+            if (s == FS3D_OK) {
+                if (!copies.empty()) {
+                    memcpy(h + copy_off, copies.data(), sizeof(CopyJob) * copies.size());
+                    memcpy(h + copy_off + sizeof(CopyJob) * (size_t)k, chunk_off.data(), sizeof(int64_t) * chunk_off.size());
+                }
+                e = upload_chunk(b, ci, table, image, rb);
+                if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
             }
+            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, rb);
+            if (s == FS3D_OK) s = release_after_read(b, rb);
+            released = true;
+            for (size_t r = 0; r < runs.size() && s == FS3D_OK; ++r) {
+                const int q = runs[r].first;
+                e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off, (size_t)runs[r].second,
+                                    cudaMemcpyDefault, rb);
+                if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
+            }
+            if (s == FS3D_OK && !copies.empty()) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, rb);
         }
     }
-    // the worlds' memory is released on the admission stream once the
-    // read-back has read it
-    {
-        cudaEvent_t read = nullptr;
-        cudaError_t e = cudaEventCreateWithFlags(&read, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventRecord(read, rb);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, read, 0);
-        if (read) cudaEventDestroy(read);
-        if (e != cudaSuccess && s == FS3D_OK) s = cuda_fail(e, "fs3d_batch_retire_many ordering");
+    if (!released) {
+        const fs3d_status r = release_after_read(b, rb);
+        if (s == FS3D_OK) s = r;
     }
     if (staging) cudaFreeAsync(staging, rb);
     if (table) cudaFreeAsync(table, rb);
@@ -1283,6 +1368,12 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     if (b->side) cudaStreamSynchronize(b->side);
     for (auto& f : b->flag_pool) cudaFreeHost(f.first);
     b->flag_pool.clear();
+    for (auto& c : b->host_chunks) {
+        cudaEventSynchronize(c.uploaded);
+        cudaEventDestroy(c.uploaded);
+        cudaFreeHost(c.p);
+    }
+    b->host_chunks.clear();
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->graph_steps) cudaGraphExecDestroy(b->graph_steps);
     b->tw.release();

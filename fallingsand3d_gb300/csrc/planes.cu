@@ -134,8 +134,9 @@ __global__ void k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs, const 
         const int64_t lu = u - unit_off[j];
         const int w = (int)(lu % jb.nw);
         const int64_t r = lu / jb.nw;
-        planes_to_chunk(jb.rows[lu], jb.statics ? jb.statics + r * jb.X : nullptr, staging + jb.byte_off + r * jb.X,
-                        jb.X, w);
+        const uint8_t* st = jb.statics;
+        if (!st && jb.static_flag && *jb.static_flag) st = jb.static_src;
+        planes_to_chunk(jb.rows[lu], st ? st + r * jb.X : nullptr, staging + jb.byte_off + r * jb.X, jb.X, w);
     }
 }
 

@@ -74,6 +74,10 @@ struct ConvJob {
     const uint8_t* statics;
     int64_t byte_off;
     int32_t X, Y, Z, nw;
+    // read-back of a world whose static-material flag has not reached the
+    // host yet: when *static_flag is set, its static bytes are at static_src
+    const int* static_flag;
+    const uint8_t* static_src;
 };
 // bytes -> planes for njobs worlds in one launch; unit_off[j] = sum of Y*Z*nw
 // over jobs before j; flags[j] |= 1 when world j holds a material >= 4
