@@ -327,61 +327,75 @@ def run_fs3d(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = cells * S * world / (ms / 1e3)
-    # parity spot check of the timed run: three worlds read back now, checked
-    # against the oracle in the CPU leg
+    # the worlds as the timed segments left them, read back untimed: the e2e
+    # leg's inputs (the same world states), and a parity spot check of the
+    # timed run (three worlds, checked against the oracle in the CPU leg)
+    T0 = S * (untimed + args.steps)
+    steady = pinned_views(torch, [tuple(g.shape) for g in host])
+    b.sync()
+    b.retire_many(tickets, [v.data_ptr() for v in steady])
+    b.close()
     checks = OracleChecks() if rank == 0 and not args.no_check else None
     if checks is not None:
-        b.sync()
         for i in range(3):
-            (X, Y, Z), seed = worlds[i]
-            checks.add_run("timed batch", host[i].numpy().copy(), seed, 0, S * (untimed + args.steps),
-                           b.retire(tickets[i], (Y, Z, X)))
-    b.close()
+            checks.add_run("timed batch", host[i].numpy().copy(), worlds[i][1], 0, T0, steady[i].numpy().copy())
 
     # ---- e2e through the C ABI from pinned host buffers
     # one step = admit every world from pinned host memory (H2D + conversion),
     # one segment, retire every world into pinned host memory (conversion + D2H).
-    # The host grids sit back to back in one page-locked arena (and so do the
-    # outputs), so each direction is one copy-engine transfer over the host link.
-    # Timed steps are pipelined through the asynchronous calls, as a server
-    # runs them: step i+1's upload is enqueued before step i's read-back and
-    # before segment i+1, so both directions of the link overlap the segments;
-    # the clock stops when the last step's grids are in host memory.
+    # The inputs are the worlds as the timed segments left them (step T0), so
+    # e2e and `value` step the same world states.  The grids sit back to back
+    # in one page-locked arena (and so do the outputs), so each direction is
+    # one copy-engine transfer over the host link.  Timed steps are pipelined
+    # through the asynchronous calls, as a server runs them: step i+1's upload
+    # is enqueued before step i's read-back and before segment i+1, so both
+    # directions of the link overlap the segments; the clock stops when the
+    # last step's grids are in host memory.  e2e_fresh: the same with the
+    # freshly generated worlds at step 0 (everything still falling).
     h2d, d2h = cells, cells
     outs = pinned_views(torch, [tuple(g.shape) for g in host])
     seeds = np.array([seed for _, seed in worlds], dtype=np.uint64)
     dims_xyz = np.array([d for d, _ in worlds], dtype=np.int64)
-    in_ptrs = np.array([g.data_ptr() for g in host], dtype=np.uint64)
     out_ptrs = np.array([o.data_ptr() for o in outs], dtype=np.uint64)
-    seq_ms = []
-    with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
-        # untimed warm-up (captures the segment graph, grows the pool), then
-        # two steps through the synchronous calls, one after the other
-        for it in range(4):
+
+    def e2e_run(inputs, start):
+        in_ptrs = np.array([g.data_ptr() for g in inputs], dtype=np.uint64)
+        starts = np.full(len(worlds), start, dtype=np.uint64)
+        seq = []
+        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
+            # untimed warm-up (captures the segment graph, grows the pool),
+            # then two steps through the waiting calls, one after the other
+            for it in range(4):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                ts = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz)
+                eb.run_segment()
+                eb.retire_many(ts, out_ptrs)
+                seq.append((time.perf_counter() - t0) * 1e3)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ts = eb.admit_many(None, seeds, S, ptrs=in_ptrs, dims=dims_xyz)
-            eb.run_segment()
-            eb.retire_many(ts, out_ptrs)
-            seq_ms.append((time.perf_counter() - t0) * 1e3)
-        seq_ms = seq_ms[2:]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        prev = None
-        for it in range(args.e2e_steps):
-            ts = eb.admit_many(None, seeds, S, ptrs=in_ptrs, dims=dims_xyz, wait=False)
-            if prev is not None:
-                eb.retire_many(prev, out_ptrs, wait=False)
-            eb.run_segment()
-            prev = ts
-        eb.retire_many(prev, out_ptrs, wait=False)
-        eb.wait_copies()
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
-    e2e_val = cells * S / (e2e_ms / 1e3)
+            prev = None
+            for it in range(args.e2e_steps):
+                ts = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz, wait=False)
+                if prev is not None:
+                    eb.retire_many(prev, out_ptrs, wait=False)
+                eb.run_segment()
+                prev = ts
+            eb.retire_many(prev, out_ptrs, wait=False)
+            eb.wait_copies()
+            ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        return ms, float(np.mean(seq[2:]))
+
+    fresh_ms, fresh_seq = e2e_run(host, 0)
     if checks is not None:
-        # the round trip: each output is its input stepped S steps
         for i in (0, len(worlds) - 1):
-            checks.add_run("e2e round trip", host[i].numpy().copy(), worlds[i][1], 0, S, outs[i].numpy().copy())
+            checks.add_run("fresh e2e round trip", host[i].numpy().copy(), worlds[i][1], 0, S, outs[i].numpy().copy())
+    e2e_ms, seq_ms = e2e_run(steady, T0)
+    if checks is not None:
+        # the round trip: each output is its input stepped S steps from T0
+        for i in (0, len(worlds) - 1):
+            checks.add_run("e2e round trip", steady[i].numpy().copy(), worlds[i][1], T0, S, outs[i].numpy().copy())
+    e2e_val = cells * S / (e2e_ms / 1e3)
 
     # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
     offs, off = [], 0
@@ -526,12 +540,18 @@ def run_fs3d(args):
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(e2e_ms, 2), "steps": args.e2e_steps,
+                        "inputs": f"the {len(worlds)} worlds as the timed segments left them (step {T0}), "
+                                  f"admitted at that step every e2e step",
                         "path": "fs3d_batch_admit_many_async (pinned arena) + fs3d_batch_run_segment + "
                                 "fs3d_batch_retire_many_async (pinned arena), pipelined; fs3d_batch_wait_copies "
                                 "at the end",
-                        "sequential_ms": round(float(np.mean(seq_ms)), 2),
+                        "sequential_ms": round(seq_ms, 2),
                         "sequential_path": "fs3d_batch_admit_many + fs3d_batch_run_segment + fs3d_batch_retire_many, "
                                            "each step waited for"},
+                "e2e_fresh": {"value": cells * S / (fresh_ms / 1e3), "unit": UNIT, "ms": round(fresh_ms, 2),
+                              "sequential_ms": round(fresh_seq, 2),
+                              "inputs": "the freshly generated worlds at step 0 (everything still falling), "
+                                        "same calls and pipelining"},
                 "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
                                     "launches_per_segment": S * len(worlds),
                                     "speedup_batched_vs_plain": round(value / world / plain_val, 2)},
@@ -674,7 +694,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
-    ap.add_argument("--e2e-steps", type=int, default=10, help="timed steps of the e2e leg")
+    ap.add_argument("--e2e-steps", type=int, default=20, help="timed steps of the e2e leg")
     ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
     ap.add_argument("--worlds", type=int, default=2048)
     ap.add_argument("--master", type=int, default=1)

@@ -458,7 +458,8 @@ class Batch:
                  ctas_per_sm: int = 0, use_smem=None):
         """use_smem: None = the library default; False/0 = per-step kernel only;
         True/1 = shared-memory resident segments; 2 = global-memory segments;
-        3 = shared memory for a world's first 128 steps, then global memory."""
+        3 = shared memory while a world's step counter is below 128, then
+        global memory."""
         cfg = lib().fs3d_default_config()
         cfg.steps_per_segment = steps_per_segment
         cfg.use_graphs = 1 if use_graphs else 0

@@ -33,7 +33,6 @@ namespace {
 struct BWorld {
     int X = 0, Y = 0, Z = 0, nw = 0;
     uint64_t seed = 0, t = 0;
-    uint64_t t0 = 0;  // step at admission
     int64_t remaining = 0;
     uint4* rows = nullptr;
     std::shared_ptr<void> arena;  // set when rows live in a block shared by the worlds of one admit_many
@@ -64,6 +63,9 @@ struct PendingAdmit {
     uint8_t* staging = nullptr;  // the admitted bytes on the device
     void* table = nullptr;       // conversion and copy tables
     const int* flags_dev = nullptr;  // the flags in `table`
+    std::shared_ptr<CUevent_st> reader;  // last read-back that took static bytes from `staging`
+    int slot = -1;                       // the admission staging buffer holding the bytes
+    std::shared_ptr<CUevent_st> converted;  // after the conversion that read them
     std::vector<uint64_t> tickets;
     std::vector<int64_t> byte_off, cells;
 };
@@ -76,31 +78,45 @@ std::shared_ptr<CUevent_st> shared_event() {
 
 template <class T>
 struct PinnedArray {
-    T* h = nullptr;
+    // two page-locked host images, written in turn (one may still be being
+    // uploaded while the next segment's tables are built), and the device copy
+    T* hb[2] = {nullptr, nullptr};
+    T* h = nullptr;  // the image in use
+    int cur = 0;
     T* d = nullptr;
     size_t cap = 0;
+    void select(int i) {
+        cur = i;
+        h = hb[i];
+    }
     fs3d_status reserve(size_t n) {
         if (n <= cap) return FS3D_OK;
         size_t c = cap ? cap : 64;
         while (c < n) c *= 2;
-        T *nh = nullptr, *nd = nullptr;
-        FS3D_CUDA(cudaMallocHost((void**)&nh, sizeof(T) * c));
-        cudaError_t e = cudaMalloc((void**)&nd, sizeof(T) * c);
+        T *nh0 = nullptr, *nh1 = nullptr, *nd = nullptr;
+        FS3D_CUDA(cudaMallocHost((void**)&nh0, sizeof(T) * c));
+        cudaError_t e = cudaMallocHost((void**)&nh1, sizeof(T) * c);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&nd, sizeof(T) * c);
         if (e != cudaSuccess) {
-            cudaFreeHost(nh);
+            cudaFreeHost(nh0);
+            if (nh1) cudaFreeHost(nh1);
             return cuda_fail(e, "cudaMalloc(batch tables)");
         }
-        cudaFreeHost(h);
+        cudaFreeHost(hb[0]);
+        cudaFreeHost(hb[1]);
         cudaFree(d);
-        h = nh;
+        hb[0] = nh0;
+        hb[1] = nh1;
+        h = hb[cur];
         d = nd;
         cap = c;
         return FS3D_OK;
     }
     void release() {
-        cudaFreeHost(h);
+        cudaFreeHost(hb[0]);
+        cudaFreeHost(hb[1]);
         cudaFree(d);
-        h = d = nullptr;
+        hb[0] = hb[1] = h = d = nullptr;
         cap = 0;
     }
 };
@@ -121,10 +137,14 @@ struct fs3d_batch {
     int* err = nullptr;      // set by a kernel whose bounded wait gave up
     cudaEvent_t fork = nullptr, join[kAllClasses + 1] = {};
     cudaStream_t branch[kAllClasses + 1] = {};  // capture branches of a segment: one per class, then the per-step chain
-    cudaEvent_t tables_free = nullptr;  // last table upload has been consumed
+    cudaEvent_t tables_free[2] = {};  // the upload from each table image has run
+    int tab_cur = 0;                  // the table image of the last build
     cudaEvent_t last_segment = nullptr;
     std::vector<std::shared_ptr<CUevent_st>> pending_ready;  // admissions the next segment must wait for
     cudaStream_t readback = nullptr;              // read-backs of retire_many
+    cudaStream_t upload = nullptr;                // host -> device copies of admit_many
+    cudaStream_t download = nullptr;              // device -> host copies of retire_many
+
     std::deque<PendingAdmit> pending_admits;      // in admission order
     uint64_t next_admit_id = 1;
     std::vector<std::pair<int*, size_t>> flag_pool;  // page-locked flag buffers free for reuse
@@ -137,6 +157,28 @@ struct fs3d_batch {
         cudaEvent_t uploaded = nullptr;
     };
     std::vector<HostChunk> host_chunks;
+    // memory of retired worlds (and staging buffers) freed once the read-back
+    // that reads it has run: no stream has to wait for another
+    struct DeferredFree {
+        std::shared_ptr<CUevent_st> after;
+        std::vector<std::shared_ptr<void>> arenas;
+        std::vector<void*> ptrs;
+    };
+    std::deque<DeferredFree> deferred;
+    // Staging bytes of admit_many (uploads) and retire_many (downloads):
+    // kStagingRing persistent buffers each, used in turn.  A buffer is taken
+    // again once the events of its previous use (kStagingRing calls back) have
+    // run: no per-call allocation of hundreds of MB, and no stream waits on
+    // the calls just before.
+    struct StagingSlot {
+        uint8_t* p = nullptr;
+        size_t cap = 0;
+        std::vector<std::shared_ptr<CUevent_st>> busy;  // the uses still to run
+        uint64_t admit_id = 0;                          // admission whose bytes these are
+    };
+    static constexpr int kStagingRing = 3;
+    StagingSlot up_ring[kStagingRing], rb_ring[kStagingRing];
+    int up_turn = 0, rb_turn = 0;
     // segment graphs without and with the per-step kernel's launches (the
     // second only when some world is too large to be resident)
     cudaGraphExec_t graph = nullptr, graph_steps = nullptr;
@@ -163,8 +205,9 @@ struct fs3d_batch {
 
 namespace {
 
-// Worlds younger than this (steps since admission) are still mostly moving:
-// the hybrid mode keeps them in shared memory, where dense steps are cheap.
+// Worlds younger than this (by their own step counter: a world admitted at
+// step 500 has been stepped 500 times) are still mostly moving: the hybrid
+// mode keeps them in shared memory, where dense steps are cheap.
 // (2048 mixed worlds: 64-step segments at ages 0 / 64 / 128 / 192 take
 // 5.1 / 2.7 / 1.9 / 1.9 ms in shared memory and 8.5 / 3.4 / 1.6 / 1.3 ms
 // from L2, which wins from age 128 on.)
@@ -190,9 +233,9 @@ int segment_class(const fs3d_batch* b, const BWorld& w) {
     if (mode == 1) return smem();
     if (mode == 2) return gm();
     if (mode == 3) {
-        const int first = (w.t - w.t0 < kYoungSteps) ? smem() : gm();
+        const int first = (w.t < kYoungSteps) ? smem() : gm();
         if (first >= 0) return first;
-        return (w.t - w.t0 < kYoungSteps) ? gm() : smem();
+        return (w.t < kYoungSteps) ? gm() : smem();
     }
     return -1;
 }
@@ -229,6 +272,13 @@ void free_world(fs3d_batch* b, BWorld& w) {
     w.ready = nullptr;
 }
 
+// Stream-ordered allocation from the device's default pool (freed blocks stay
+// cached: its release threshold is raised when a batch is created).
+template <class T>
+cudaError_t pool_alloc(fs3d_batch*, T** p, size_t n, cudaStream_t st) {
+    return cudaMallocAsync(reinterpret_cast<void**>(p), n, st);
+}
+
 // A page-locked buffer of at least n flags, from the batch's pool.
 int* take_flags(fs3d_batch* b, size_t n, size_t* cap) {
     for (size_t i = 0; i < b->flag_pool.size(); ++i)
@@ -243,6 +293,48 @@ int* take_flags(fs3d_batch* b, size_t n, size_t* cap) {
     if (cudaMallocHost((void**)&f, c * sizeof(int)) != cudaSuccess) return nullptr;
     *cap = c;
     return f;
+}
+
+// The next buffer of a staging ring, of at least n bytes, for stream st: st
+// waits for the buffer's previous uses (it grows, on st, when too small).
+fs3d_batch::StagingSlot* take_slot(fs3d_batch::StagingSlot* ring, int& turn, size_t n, cudaStream_t st,
+                                   cudaError_t* e) {
+    fs3d_batch::StagingSlot& sl = ring[turn];
+    turn = (turn + 1) % fs3d_batch::kStagingRing;
+    *e = cudaSuccess;
+    for (auto& ev : sl.busy)
+        if (*e == cudaSuccess) *e = cudaStreamWaitEvent(st, ev.get(), 0);
+    sl.busy.clear();
+    if (*e == cudaSuccess && sl.cap < n) {
+        if (sl.p) cudaFreeAsync(sl.p, st);
+        sl.p = nullptr;
+        sl.cap = 0;
+        *e = cudaMallocAsync(reinterpret_cast<void**>(&sl.p), n, st);
+        if (*e == cudaSuccess) sl.cap = n;
+    }
+    return &sl;
+}
+
+// Marks a staging buffer in use until an event recorded now on st has run
+// (or, with no event, waits for st here).
+void mark_busy(fs3d_batch::StagingSlot* sl, cudaStream_t st) {
+    std::shared_ptr<CUevent_st> ev = shared_event();
+    if (ev && cudaEventRecord(ev.get(), st) == cudaSuccess)
+        sl->busy.push_back(ev);
+    else
+        cudaStreamSynchronize(st);
+}
+
+// Frees the deferred memory whose read-backs have run (all of it with `wait`).
+void drain_deferred(fs3d_batch* b, bool wait) {
+    while (!b->deferred.empty()) {
+        fs3d_batch::DeferredFree& d = b->deferred.front();
+        const cudaError_t q = wait ? cudaEventSynchronize(d.after.get()) : cudaEventQuery(d.after.get());
+        if (q == cudaErrorNotReady) break;
+        d.arenas.clear();  // a block goes back to the pool with its last world
+        for (void* p : d.ptrs) cudaFreeAsync(p, b->side);
+        b->deferred.pop_front();
+    }
 }
 
 // A page-locked chunk of at least n bytes whose last upload has run (index
@@ -288,7 +380,7 @@ fs3d_status finalize_admits(fs3d_batch* b, uint64_t upto, bool wait) {
             w.admit_id = 0;
             if (!p.flags[a] || s != FS3D_OK) continue;
             const size_t cells = (size_t)p.cells[a];
-            cudaError_t e = cudaMallocAsync((void**)&w.statics, cells, b->side);
+            cudaError_t e = pool_alloc(b, &w.statics, cells, b->side);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(w.statics, p.staging + p.byte_off[a], cells, cudaMemcpyDeviceToDevice, b->side);
             if (e != cudaSuccess) {
@@ -299,13 +391,37 @@ fs3d_status finalize_admits(fs3d_batch* b, uint64_t upto, bool wait) {
             b->used += cells;
             flagged.push_back(&w);
         }
+        std::shared_ptr<CUevent_st> ready;
         if (!flagged.empty()) {
-            std::shared_ptr<CUevent_st> ready = shared_event();
+            ready = shared_event();
             if (ready && cudaEventRecord(ready.get(), b->side) == cudaSuccess)
                 for (BWorld* w : flagged) w->statics_ready = ready;
+            else
+                ready.reset();
         }
-        cudaFreeAsync(p.staging, b->side);
-        cudaFreeAsync(p.table, b->side);
+        // the staging buffer is free again once the conversion and the static
+        // copies (admission stream) and any read-back that took static bytes
+        // from it have run; the tables (with the flags) likewise
+        if (p.slot >= 0) {
+            fs3d_batch::StagingSlot* sl = &b->up_ring[p.slot];
+            if (p.converted) sl->busy.push_back(p.converted);
+            if (!flagged.empty()) {
+                if (ready)
+                    sl->busy.push_back(ready);
+                else
+                    cudaStreamSynchronize(b->side);
+            }
+            if (p.reader) sl->busy.push_back(p.reader);
+            if (sl->admit_id == p.id) sl->admit_id = 0;
+        }
+        if (p.reader) {
+            fs3d_batch::DeferredFree d;
+            d.after = p.reader;
+            d.ptrs = {p.table};
+            b->deferred.push_back(std::move(d));
+        } else {
+            cudaFreeAsync(p.table, b->side);
+        }
         b->flag_pool.emplace_back(p.flags, p.flags_cap);
         cudaEventDestroy(p.done);
         b->pending_admits.pop_front();
@@ -396,7 +512,9 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->readback, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->tables_free, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->upload, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->download, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->tables_free[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->last_segment, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->hash_dev, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->processed_dev, sizeof(unsigned long long));
@@ -469,19 +587,18 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     w.nw = plane_nw(X);
     w.seed = seed;
     w.t = start_step;
-    w.t0 = start_step;
     w.remaining = n_steps;
     w.done = n_steps == 0;
     w.bytes = plane_bytes(X, Y, Z) + layer_flag_bytes(Y) + (stat ? n : 0) + sizeof(PlaneWorld);
     if (b->used + w.bytes > b->budget)
         return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
     uint8_t* staging = nullptr;
-    FS3D_CUDA(cudaMallocAsync((void**)&w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
+    FS3D_CUDA(pool_alloc(b, &w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
     w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(X, Y, Z);
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaSuccess;
     if (g) {
-        e = cudaMallocAsync((void**)&staging, n, b->side);
+        e = pool_alloc(b, &staging, n, b->side);
         if (e == cudaSuccess) e = cudaMemcpyAsync(staging, g, n, cudaMemcpyHostToDevice, b->side);
         s = e == cudaSuccess ? planes_from_bytes(staging, X, Y, Z, w.rows, b->side) : cuda_fail(e, "admit upload");
         if (stat)
@@ -538,8 +655,14 @@ fs3d_status build_tables(fs3d_batch* b) {
     b->table_items = 0;
     b->table_dense = b->table_stepped = 0;
     b->reuse_left = 0;
-    // the pinned tables may be rewritten once the previous upload has run
-    FS3D_CUDA(cudaEventSynchronize(b->tables_free));
+    // the other table image: it may be rewritten once its upload (two builds
+    // back) has run, while the last build's upload may still be pending
+    b->tab_cur ^= 1;
+    FS3D_CUDA(cudaEventSynchronize(b->tables_free[b->tab_cur]));
+    b->tw.select(b->tab_cur);
+    b->ti.select(b->tab_cur);
+    b->tn.select(b->tab_cur);
+    b->to.select(b->tab_cur);
     // resident class of every running world (-1: stepped by the per-step kernel)
     std::vector<std::pair<int, BWorld*>> run;
     size_t ni = 0, ns = 0;
@@ -598,7 +721,7 @@ fs3d_status build_tables(fs3d_batch* b) {
         // full segments while `remaining` lasts; in the hybrid mode a young
         // world changes class once it is kYoungSteps old
         uint64_t hold = (uint64_t)std::max<int64_t>(1, w.remaining / S);
-        const uint64_t age = w.t - w.t0;
+        const uint64_t age = w.t;
         if (b->cfg.use_smem == 3 && age < kYoungSteps) hold = std::min(hold, (kYoungSteps - age + S - 1) / S);
         reuse = std::min(reuse, hold);
         b->running.push_back(&w);
@@ -633,7 +756,7 @@ fs3d_status build_tables(fs3d_batch* b) {
     if (si) FS3D_CUDA(cudaMemcpyAsync(b->to.d, b->to.h, sizeof(int) * si, cudaMemcpyHostToDevice, b->stream));
     FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * kMetaInts, cudaMemcpyHostToDevice,
                               b->stream));
-    FS3D_CUDA(cudaEventRecord(b->tables_free, b->stream));
+    FS3D_CUDA(cudaEventRecord(b->tables_free[b->tab_cur], b->stream));
     if (b->cfg.use_graphs &&
         (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d)) {
         s = capture_graph(b);
@@ -704,7 +827,8 @@ fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns) {
     FS3D_CUDA(cudaMemcpy(&err, b->err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
     s = wait_stream(b->side, timeout_ns);
-    return s == FS3D_OK ? wait_stream(b->readback, timeout_ns) : s;
+    if (s == FS3D_OK) s = wait_stream(b->readback, timeout_ns);
+    return s == FS3D_OK ? wait_stream(b->download, timeout_ns) : s;
 }
 
 fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash) {
@@ -758,7 +882,7 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
     if (grid_out) {
         const size_t n = (size_t)w.X * w.Y * w.Z;
         uint8_t* staging = nullptr;
-        FS3D_CUDA(cudaMallocAsync((void**)&staging, n, b->side));
+        FS3D_CUDA(pool_alloc(b, &staging, n, b->side));
         s = planes_to_bytes(w.rows, w.statics, w.X, w.Y, w.Z, staging, b->side);
         cudaError_t e = cudaSuccess;
         if (s == FS3D_OK) e = cudaMemcpyAsync(grid_out, staging, n, cudaMemcpyDeviceToHost, b->side);
@@ -805,7 +929,9 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         used += need;
     }
     if (k == 0) return n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: nothing fits in the budget now") : FS3D_OK;
-    // older asynchronous admissions whose flags have arrived are completed first
+    // older asynchronous admissions whose flags have arrived are completed
+    // first, and memory whose read-backs have run is returned
+    drain_deferred(b, false);
     fs3d_status s = finalize_admits(b, UINT64_MAX, false);
     if (s != FS3D_OK) return s;
     PendingAdmit pa;
@@ -839,8 +965,27 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     const size_t flags_off = (jobs_bytes + off_bytes + 15) / 16 * 16;
     const size_t copy_off = (flags_off + sizeof(int) * (size_t)k + 15) / 16 * 16;
     const size_t copy_bytes = sizeof(CopyJob) * (size_t)k + sizeof(int64_t) * (size_t)k;
-    cudaError_t e = cudaMallocAsync((void**)&pa.staging, (size_t)bytes_total, b->side);
-    if (e == cudaSuccess) e = cudaMallocAsync(&pa.table, copy_off + copy_bytes, b->side);
+    // the grid uploads run on their own stream: the next admission's upload
+    // does not wait for this one's conversion (which waits for free SMs)
+    cudaStream_t up = b->upload;
+    {
+        // an admission still holding this turn's staging bytes (kStagingRing
+        // calls back) is completed first
+        const uint64_t holder = b->up_ring[b->up_turn].admit_id;
+        if (holder) {
+            s = finalize_admits(b, holder, true);
+            if (s != FS3D_OK) {
+                b->flag_pool.emplace_back(pa.flags, pa.flags_cap);
+                return s;
+            }
+        }
+    }
+    pa.slot = b->up_turn;
+    cudaError_t e = cudaSuccess;
+    fs3d_batch::StagingSlot* slot = take_slot(b->up_ring, b->up_turn, (size_t)bytes_total, up, &e);
+    pa.staging = slot->p;
+    slot->admit_id = pa.id;
+    if (e == cudaSuccess) e = pool_alloc(b, &pa.table, copy_off + copy_bytes, b->side);
     // grids the device can address (page-locked host or device memory) that lie
     // back to back go over in one copy-engine transfer per run (the SMs stay
     // free for segments in flight); other device-addressable grids are gathered
@@ -856,7 +1001,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         block_bytes += (plane_bytes(specs[a].X, specs[a].Y, specs[a].Z) + layer_flag_bytes(specs[a].Y) + 255) & ~(size_t)255;
     }
     void* block = nullptr;
-    if (e == cudaSuccess) e = cudaMallocAsync(&block, block_bytes, b->side);
+    if (e == cudaSuccess) e = pool_alloc(b, &block, block_bytes, b->side);
     for (int a = 0; a < k; ++a)
         rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
     uint8_t* staging = pa.staging;
@@ -875,7 +1020,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         }
         if (!dv || e_run - a > 1) {
             e = cudaMemcpyAsync(staging + jobs[(size_t)a].byte_off, specs[a].grid, (size_t)run_bytes, cudaMemcpyDefault,
-                                b->side);
+                                up);
         } else {
             copies.push_back(CopyJob{dv, staging + jobs[(size_t)a].byte_off, cells});
             chunk_off.push_back(chunks);
@@ -884,6 +1029,14 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         a = e_run;
     }
     for (int a = 0; a < k; ++a) jobs[(size_t)a].rows = rows[(size_t)a];
+    // the conversion (admission stream) follows the uploads
+    if (e == cudaSuccess) {
+        cudaEvent_t uploaded = nullptr;
+        e = cudaEventCreateWithFlags(&uploaded, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(uploaded, up);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, uploaded, 0);
+        if (uploaded) cudaEventDestroy(uploaded);
+    }
     ConvJob* jobs_dev = static_cast<ConvJob*>(pa.table);
     int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(pa.table) + jobs_bytes);
     int* flags_dev = reinterpret_cast<int*>(static_cast<char*>(pa.table) + flags_off);
@@ -917,6 +1070,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     if (s == FS3D_OK) {
         admitted = shared_event();
         e = admitted ? cudaEventRecord(admitted.get(), b->side) : cudaErrorMemoryAllocation;
+        pa.converted = admitted;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(pa.flags, flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pa.done, cudaEventDisableTiming);
@@ -924,7 +1078,9 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many conversion");
     }
     if (s != FS3D_OK) {
-        if (pa.staging) cudaFreeAsync(pa.staging, b->side);
+        cudaStreamSynchronize(b->upload);  // no copy may still be writing the staging bytes
+        cudaStreamSynchronize(b->side);
+        slot->admit_id = 0;
         if (pa.table) cudaFreeAsync(pa.table, b->side);
         if (block) cudaFreeAsync(block, b->side);
         if (pa.done) cudaEventDestroy(pa.done);
@@ -942,7 +1098,6 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         w.nw = plane_nw(p.X);
         w.seed = p.seed;
         w.t = p.start_step;
-        w.t0 = p.start_step;
         w.remaining = p.n_steps;
         w.done = p.n_steps == 0;
         w.rows = rows[(size_t)a];
@@ -970,16 +1125,11 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     return k < n ? set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit_many: the remaining worlds do not fit now") : FS3D_OK;
 }
 
-// The worlds' memory is freed on the admission stream: it waits until the
-// read-back stream has converted them (the download of the bytes that follows
-// does not hold up later uploads).
-fs3d_status release_after_read(fs3d_batch* b, cudaStream_t rb) {
-    cudaEvent_t read = nullptr;
-    cudaError_t e = cudaEventCreateWithFlags(&read, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(read, rb);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, read, 0);
-    if (read) cudaEventDestroy(read);
-    return e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_batch_retire_many ordering");
+// An event after the read-back's conversion (null if none could be recorded).
+std::shared_ptr<CUevent_st> record_read(cudaStream_t rb) {
+    std::shared_ptr<CUevent_st> ev = shared_event();
+    if (ev && cudaEventRecord(ev.get(), rb) != cudaSuccess) ev.reset();
+    return ev;
 }
 
 // Retires tickets[0..n): the read-backs (conversion + copy into grids_out[a]
@@ -1001,11 +1151,13 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
         const fs3d_status f = finalize_admits(b, UINT64_MAX, false);
         if (f != FS3D_OK) return f;
     }
-    auto pending_of = [&](uint64_t id) -> const PendingAdmit* {
-        for (const PendingAdmit& p : b->pending_admits)
+    drain_deferred(b, false);
+    auto pending_of = [&](uint64_t id) -> PendingAdmit* {
+        for (PendingAdmit& p : b->pending_admits)
             if (p.id == id) return &p;
         return nullptr;
     };
+    std::vector<PendingAdmit*> readers;  // open admissions whose staging bytes this read-back reads
     cudaStream_t rb = b->readback;
     {
         // each world's planes are final after its last segment (a world not
@@ -1027,7 +1179,8 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
     fs3d_status s = FS3D_OK;
     uint8_t* staging = nullptr;
     void* table = nullptr;
-    bool released = false;  // the admission stream (which frees the worlds) waits for the conversion
+    std::shared_ptr<CUevent_st> read;  // recorded after the conversion
+    fs3d_batch::StagingSlot* rb_slot = nullptr;  // the read-back's staging buffer
     if (grids_out) {
         std::vector<ConvJob> jobs;
         std::vector<int64_t> unit_off;
@@ -1042,9 +1195,10 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
             j.static_flag = nullptr;
             j.static_src = nullptr;
             if (w.admit_id)
-                if (const PendingAdmit* pa = pending_of(w.admit_id)) {
+                if (PendingAdmit* pa = pending_of(w.admit_id)) {
                     j.static_flag = pa->flags_dev + w.admit_index;
                     j.static_src = pa->staging + pa->byte_off[(size_t)w.admit_index];
+                    if (std::find(readers.begin(), readers.end(), pa) == readers.end()) readers.push_back(pa);
                 }
             j.byte_off = bytes_total;
             j.X = w.X;
@@ -1061,9 +1215,11 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
         if (k) {
             const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k;
             const size_t copy_off = (jobs_bytes + sizeof(int64_t) * (size_t)k + 15) / 16 * 16;
-            cudaError_t e = cudaMallocAsync((void**)&staging, (size_t)bytes_total, rb);
+            cudaError_t e = cudaSuccess;
+            rb_slot = take_slot(b->rb_ring, b->rb_turn, (size_t)bytes_total, rb, &e);
+            staging = rb_slot->p;
             if (e == cudaSuccess)
-                e = cudaMallocAsync(&table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, rb);
+                e = pool_alloc(b, &table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, rb);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
             // the copy jobs are only known below: the table goes up in one
@@ -1125,30 +1281,60 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
             }
             if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, rb);
-            if (s == FS3D_OK) s = release_after_read(b, rb);
-            released = true;
+            if (s == FS3D_OK) read = record_read(rb);
+            // the downloads run on their own stream: the next read-back's
+            // conversion does not wait for this one's copies over the host link
+            if (s == FS3D_OK && read) {
+                e = cudaStreamWaitEvent(b->download, read.get(), 0);
+                if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many ordering");
+            }
+            cudaStream_t dl = b->download;
             for (size_t r = 0; r < runs.size() && s == FS3D_OK; ++r) {
                 const int q = runs[r].first;
                 e = cudaMemcpyAsync(grids_out[who[(size_t)q]], staging + jobs[(size_t)q].byte_off, (size_t)runs[r].second,
-                                    cudaMemcpyDefault, rb);
+                                    cudaMemcpyDefault, dl);
                 if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
             }
-            if (s == FS3D_OK && !copies.empty()) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, rb);
+            if (s == FS3D_OK && !copies.empty()) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, dl);
         }
     }
-    if (!released) {
-        const fs3d_status r = release_after_read(b, rb);
-        if (s == FS3D_OK) s = r;
+    if (!read) read = record_read(rb);
+    if (!read && s == FS3D_OK) s = set_error(FS3D_ERR_CUDA, "fs3d_batch_retire_many: event");
+    // the staging buffer is free again after the downloads, the tables after the conversion
+    if (rb_slot) {
+        mark_busy(rb_slot, b->download);
+        mark_busy(rb_slot, rb);
     }
-    if (staging) cudaFreeAsync(staging, rb);
     if (table) cudaFreeAsync(table, rb);
+    // the worlds' memory goes back once the conversion has read it
+    fs3d_batch::DeferredFree d;
+    d.after = read;
+    for (PendingAdmit* pa : readers) pa->reader = read;
     for (auto it : its) {
-        b->used -= it->second.bytes;
-        free_world(b, it->second);
+        BWorld& w = it->second;
+        b->used -= w.bytes;
+        if (w.arena) d.arenas.push_back(std::move(w.arena));
+        else if (w.rows) d.ptrs.push_back(w.rows);
+        if (w.statics) d.ptrs.push_back(w.statics);
+        w.arena.reset();
+        w.rows = nullptr;
+        w.statics = nullptr;
+        free_world(b, w);
         b->worlds.erase(it);
     }
+    if (read) {
+        b->deferred.push_back(std::move(d));
+    } else {
+        // no event: the conversion is waited for here
+        cudaStreamSynchronize(rb);
+        d.arenas.clear();
+        for (void* p : d.ptrs) cudaFreeAsync(p, b->side);
+    }
     if (!its.empty()) b->tables_stale = true;
-    if (wait && s == FS3D_OK) FS3D_CUDA(cudaStreamSynchronize(rb));
+    if (wait && s == FS3D_OK) {
+        FS3D_CUDA(cudaStreamSynchronize(rb));
+        FS3D_CUDA(cudaStreamSynchronize(b->download));
+    }
     return s;
 }
 
@@ -1177,8 +1363,11 @@ fs3d_status fs3d_batch_retire_many_async(fs3d_batch* b, int n, const uint64_t* t
 fs3d_status fs3d_batch_wait_copies(fs3d_batch* b, int64_t timeout_ns) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_wait_copies: NULL batch");
     fs3d_status s = wait_stream(b->readback, timeout_ns);
+    if (s == FS3D_OK) s = wait_stream(b->download, timeout_ns);
+    if (s == FS3D_OK) s = wait_stream(b->upload, timeout_ns);
     if (s == FS3D_OK) s = wait_stream(b->side, timeout_ns);
     if (s == FS3D_OK) s = finalize_admits(b, UINT64_MAX, false);
+    if (s == FS3D_OK) drain_deferred(b, false);
     return s;
 }
 
@@ -1360,11 +1549,20 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_destroy: NULL batch");
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->readback) cudaStreamSynchronize(b->readback);
+    if (b->upload) cudaStreamSynchronize(b->upload);
+    if (b->download) cudaStreamSynchronize(b->download);
     if (b->side) cudaStreamSynchronize(b->side);
     finalize_admits(b, UINT64_MAX, true);
+    drain_deferred(b, true);
     for (auto& kv : b->worlds) free_world(b, kv.second);
     b->worlds.clear();
     b->pending_ready.clear();
+    for (fs3d_batch::StagingSlot* ring : {b->up_ring, b->rb_ring})
+        for (int i = 0; i < fs3d_batch::kStagingRing; ++i) {
+            if (ring[i].p) cudaFreeAsync(ring[i].p, b->side);
+            ring[i].p = nullptr;
+            ring[i].busy.clear();
+        }
     if (b->side) cudaStreamSynchronize(b->side);
     for (auto& f : b->flag_pool) cudaFreeHost(f.first);
     b->flag_pool.clear();
@@ -1389,11 +1587,14 @@ fs3d_status fs3d_batch_destroy(fs3d_batch* b) {
         if (b->join[c]) cudaEventDestroy(b->join[c]);
         if (b->branch[c]) cudaStreamDestroy(b->branch[c]);
     }
-    if (b->tables_free) cudaEventDestroy(b->tables_free);
+    for (cudaEvent_t ev : b->tables_free)
+        if (ev) cudaEventDestroy(ev);
     if (b->last_segment) cudaEventDestroy(b->last_segment);
     if (b->stream) cudaStreamDestroy(b->stream);
     if (b->side) cudaStreamDestroy(b->side);
     if (b->readback) cudaStreamDestroy(b->readback);
+    if (b->upload) cudaStreamDestroy(b->upload);
+    if (b->download) cudaStreamDestroy(b->download);
     delete b;
     return FS3D_OK;
 }

@@ -112,14 +112,30 @@ __device__ __forceinline__ int find_job(const int64_t* __restrict__ unit_off, in
     return lo;
 }
 
+// The job of each unit of a CTA's block of consecutive units: one binary
+// search per block (its first unit), then at most a few steps forward (a
+// world has at least 16 units per row of Z, so a block spans few jobs).
+__device__ __forceinline__ int block_job(const int64_t* __restrict__ unit_off, int njobs, int64_t base, int64_t u,
+                                         int* s_job) {
+    if (threadIdx.x == 0) *s_job = find_job(unit_off, njobs, base);
+    __syncthreads();
+    int j = *s_job;
+    while (j + 1 < njobs && __ldg(unit_off + j + 1) <= u) ++j;
+    return j;
+}
+
 __global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
                                         int njobs, int64_t total, const uint8_t* __restrict__ staging, int* flags) {
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
-        const int j = find_job(unit_off, njobs, u);
+    __shared__ int s_job;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = base + threadIdx.x;
+        const int j = block_job(unit_off, njobs, base, u < total ? u : total - 1, &s_job);
+        __syncthreads();  // s_job is rewritten by the next block
+        if (u >= total) continue;
         const ConvJob jb = jobs[j];
         const int64_t lu = u - unit_off[j];
-        const int w = (int)(lu % jb.nw);
-        const int64_t r = lu / jb.nw;
+        const int w = jb.nw == 1 ? 0 : (int)(lu % jb.nw);
+        const int64_t r = jb.nw == 1 ? lu : lu / jb.nw;
         bool big;
         jb.rows[lu] = chunk_to_planes(staging + jb.byte_off + r * jb.X, jb.X, w, big);
         if (big) atomicOr(flags + j, 1);  // holds a static material >= 4: keep its bytes
@@ -128,12 +144,16 @@ __global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const 
 
 __global__ void k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
                                         int njobs, int64_t total, uint8_t* __restrict__ staging) {
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
-        const int j = find_job(unit_off, njobs, u);
+    __shared__ int s_job;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = base + threadIdx.x;
+        const int j = block_job(unit_off, njobs, base, u < total ? u : total - 1, &s_job);
+        __syncthreads();  // s_job is rewritten by the next block
+        if (u >= total) continue;
         const ConvJob jb = jobs[j];
         const int64_t lu = u - unit_off[j];
-        const int w = (int)(lu % jb.nw);
-        const int64_t r = lu / jb.nw;
+        const int w = jb.nw == 1 ? 0 : (int)(lu % jb.nw);
+        const int64_t r = jb.nw == 1 ? lu : lu / jb.nw;
         const uint8_t* st = jb.statics;
         if (!st && jb.static_flag && *jb.static_flag) st = jb.static_src;
         planes_to_chunk(jb.rows[lu], st ? st + r * jb.X : nullptr, staging + jb.byte_off + r * jb.X, jb.X, w);

@@ -81,8 +81,9 @@ typedef struct fs3d_config {
                               one launch): 1 = the planes are held in shared memory
                               (worlds that fit); 2 = the planes stay in global
                               memory (L2), one CTA per world sized by the work of
-                              one layer; 3 (default) = 1 for a world's first 128
-                              steps, then 2; 0 = the per-step kernel only          */
+                              one layer; 3 (default) = 1 while the world's step
+                              counter is below 128, then 2; 0 = the per-step
+                              kernel only                                          */
     int reserved[12];
 } fs3d_config;
 
