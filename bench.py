@@ -656,9 +656,42 @@ def run_only(args):
     `batched` runs warmup + steps segments of the 2048-world pool, `plain512`
     runs warmup + steps x 8 steps of the drop-in byte kernel on 512^3, `large`
     runs the 1024^3 dune world with a 1920x1080 frame after each of
-    --large-steps steps."""
+    --large-steps steps, `e2e` reads the pool back after 20 segments and runs
+    --e2e-steps pipelined e2e steps on those world states (after 3 waited-for
+    warm-up steps)."""
     import torch
     import fallingsand3d_gb300 as fs3d
+    if args.only == "e2e":
+        worlds = batch_worlds(fs3d, args.master, args.worlds)
+        S = args.segment
+        shapes = [(Y, Z, X) for (X, Y, Z), _ in worlds]
+        steady, outs = pinned_views(torch, shapes), pinned_views(torch, shapes)
+        with fs3d.Batch(150 << 30, steps_per_segment=S) as b:
+            ts = [b.admit_generated(X, Y, Z, seed, S * 20) for (X, Y, Z), seed in worlds]
+            for _ in range(20):
+                b.run_segment()
+            b.retire_many(ts, [v.data_ptr() for v in steady])
+        seeds = np.array([sd for _, sd in worlds], dtype=np.uint64)
+        dims = np.array([d for d, _ in worlds], dtype=np.int64)
+        inp = np.array([g.data_ptr() for g in steady], dtype=np.uint64)
+        outp = np.array([o.data_ptr() for o in outs], dtype=np.uint64)
+        starts = np.full(len(worlds), S * 20, dtype=np.uint64)
+        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
+            for _ in range(3):
+                t = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=inp, dims=dims)
+                eb.run_segment()
+                eb.retire_many(t, outp)
+            prev = None
+            for _ in range(args.e2e_steps):
+                t = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=inp, dims=dims, wait=False)
+                if prev is not None:
+                    eb.retire_many(prev, outp, wait=False)
+                eb.run_segment()
+                prev = t
+            eb.retire_many(prev, outp, wait=False)
+            eb.wait_copies()
+        print(json.dumps({"only": args.only, "ok": True}))
+        return 0
     if args.only == "large":
         out = run_large(fs3d, torch, torch.device("cuda", 0), args)
         print(json.dumps({"only": args.only, "ok": True, "large_render": out}))
@@ -707,7 +740,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh", "e2e"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
