@@ -965,6 +965,8 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     const size_t flags_off = (jobs_bytes + off_bytes + 15) / 16 * 16;
     const size_t copy_off = (flags_off + sizeof(int) * (size_t)k + 15) / 16 * 16;
     const size_t copy_bytes = sizeof(CopyJob) * (size_t)k + sizeof(int64_t) * (size_t)k;
+    const size_t bj_off = (copy_off + copy_bytes + 15) / 16 * 16;  // the conversion's job of each unit block
+    const size_t table_bytes = bj_off + sizeof(int) * (size_t)conv_blocks(units);
     // the grid uploads run on their own stream: the next admission's upload
     // does not wait for this one's conversion (which waits for free SMs)
     cudaStream_t up = b->upload;
@@ -985,7 +987,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     fs3d_batch::StagingSlot* slot = take_slot(b->up_ring, b->up_turn, (size_t)bytes_total, up, &e);
     pa.staging = slot->p;
     slot->admit_id = pa.id;
-    if (e == cudaSuccess) e = pool_alloc(b, &pa.table, copy_off + copy_bytes, b->side);
+    if (e == cudaSuccess) e = pool_alloc(b, &pa.table, table_bytes, b->side);
     // grids the device can address (page-locked host or device memory) that lie
     // back to back go over in one copy-engine transfer per run (the SMs stay
     // free for segments in flight); other device-addressable grids are gathered
@@ -1046,7 +1048,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     // the whole table (jobs, offsets, zeroed flags, copy jobs) in one upload
     // from a page-locked image, so nothing here waits for the grid uploads
     if (e == cudaSuccess) {
-        const size_t image = copy_off + copy_bytes;
+        const size_t image = table_bytes;
         const int ci = take_chunk(b, image);
         if (ci < 0) {
             e = cudaErrorMemoryAllocation;
@@ -1059,12 +1061,14 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
                 memcpy(h + copy_off, copies.data(), sizeof(CopyJob) * copies.size());
                 memcpy(h + copy_off + sizeof(CopyJob) * (size_t)k, chunk_off.data(), sizeof(int64_t) * chunk_off.size());
             }
+            conv_block_jobs(unit_off.data(), k, units, reinterpret_cast<int*>(h + bj_off));
             e = upload_chunk(b, ci, pa.table, image, b->side);
         }
     }
     if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many upload");
     if (s == FS3D_OK) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side);
-    if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, k, units, staging, flags_dev, b->side);
+    const int* bj_dev = reinterpret_cast<const int*>(static_cast<char*>(pa.table) + bj_off);
+    if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, bj_dev, k, units, staging, flags_dev, b->side);
     // segments may start once the planes are written
     std::shared_ptr<CUevent_st> admitted;
     if (s == FS3D_OK) {
@@ -1215,18 +1219,19 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
         if (k) {
             const size_t jobs_bytes = sizeof(ConvJob) * (size_t)k;
             const size_t copy_off = (jobs_bytes + sizeof(int64_t) * (size_t)k + 15) / 16 * 16;
+            const size_t bj_off = (copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k + 15) / 16 * 16;
+            const size_t table_bytes = bj_off + sizeof(int) * (size_t)conv_blocks(units);
             cudaError_t e = cudaSuccess;
             rb_slot = take_slot(b->rb_ring, b->rb_turn, (size_t)bytes_total, rb, &e);
             staging = rb_slot->p;
-            if (e == cudaSuccess)
-                e = pool_alloc(b, &table, copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k, rb);
+            if (e == cudaSuccess) e = pool_alloc(b, &table, table_bytes, rb);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
             // the copy jobs are only known below: the table goes up in one
             // page-locked image once they are
             if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
             int ci = -1;
-            const size_t image = copy_off + (sizeof(CopyJob) + sizeof(int64_t)) * (size_t)k;
+            const size_t image = table_bytes;
             if (s == FS3D_OK) {
                 ci = take_chunk(b, image);
                 if (ci < 0) s = set_error(FS3D_ERR_CUDA, "fs3d_batch_retire_many: page-locked table");
@@ -1235,6 +1240,7 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
             if (h) {
                 memcpy(h, jobs.data(), jobs_bytes);
                 memcpy(h + jobs_bytes, unit_off.data(), sizeof(int64_t) * (size_t)k);
+                conv_block_jobs(unit_off.data(), k, units, reinterpret_cast<int*>(h + bj_off));
             }
             std::vector<CopyJob> copies;
             std::vector<int64_t> chunk_off;
@@ -1280,7 +1286,8 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 e = upload_chunk(b, ci, table, image, rb);
                 if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many upload");
             }
-            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, k, units, staging, rb);
+            const int* bj_dev = reinterpret_cast<const int*>(static_cast<char*>(table) + bj_off);
+            if (s == FS3D_OK) s = planes_to_bytes_multi(jobs_dev, off_dev, bj_dev, k, units, staging, rb);
             if (s == FS3D_OK) read = record_read(rb);
             // the downloads run on their own stream: the next read-back's
             // conversion does not wait for this one's copies over the host link

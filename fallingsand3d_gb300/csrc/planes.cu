@@ -112,26 +112,23 @@ __device__ __forceinline__ int find_job(const int64_t* __restrict__ unit_off, in
     return lo;
 }
 
-// The job of each unit of a CTA's block of consecutive units: one binary
-// search per block (its first unit), then at most a few steps forward (a
-// world has at least 16 units per row of Z, so a block spans few jobs).
-__device__ __forceinline__ int block_job(const int64_t* __restrict__ unit_off, int njobs, int64_t base, int64_t u,
-                                         int* s_job) {
-    if (threadIdx.x == 0) *s_job = find_job(unit_off, njobs, base);
-    __syncthreads();
-    int j = *s_job;
+// The job of a unit: the job of its block's first unit (block_job, from the
+// host), then at most a few steps forward (a block of kConvBlock consecutive
+// units spans few worlds).
+__device__ __forceinline__ int unit_job(const int64_t* __restrict__ unit_off, const int* __restrict__ block_job,
+                                        int njobs, int64_t u) {
+    int j = __ldg(block_job + u / kConvBlock);
     while (j + 1 < njobs && __ldg(unit_off + j + 1) <= u) ++j;
     return j;
 }
 
-__global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
-                                        int njobs, int64_t total, const uint8_t* __restrict__ staging, int* flags) {
-    __shared__ int s_job;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t u = base + threadIdx.x;
-        const int j = block_job(unit_off, njobs, base, u < total ? u : total - 1, &s_job);
-        __syncthreads();  // s_job is rewritten by the next block
-        if (u >= total) continue;
+__global__ void __launch_bounds__(kConvBlock) k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs,
+                                                                      const int64_t* __restrict__ unit_off,
+                                                                      const int* __restrict__ block_job, int njobs,
+                                                                      int64_t total, const uint8_t* __restrict__ staging,
+                                                                      int* flags) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int j = unit_job(unit_off, block_job, njobs, u);
         const ConvJob jb = jobs[j];
         const int64_t lu = u - unit_off[j];
         const int w = jb.nw == 1 ? 0 : (int)(lu % jb.nw);
@@ -142,14 +139,12 @@ __global__ void k_bytes_to_planes_multi(const ConvJob* __restrict__ jobs, const 
     }
 }
 
-__global__ void k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs, const int64_t* __restrict__ unit_off,
-                                        int njobs, int64_t total, uint8_t* __restrict__ staging) {
-    __shared__ int s_job;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t u = base + threadIdx.x;
-        const int j = block_job(unit_off, njobs, base, u < total ? u : total - 1, &s_job);
-        __syncthreads();  // s_job is rewritten by the next block
-        if (u >= total) continue;
+__global__ void __launch_bounds__(kConvBlock) k_planes_to_bytes_multi(const ConvJob* __restrict__ jobs,
+                                                                      const int64_t* __restrict__ unit_off,
+                                                                      const int* __restrict__ block_job, int njobs,
+                                                                      int64_t total, uint8_t* __restrict__ staging) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int j = unit_job(unit_off, block_job, njobs, u);
         const ConvJob jb = jobs[j];
         const int64_t lu = u - unit_off[j];
         const int w = jb.nw == 1 ? 0 : (int)(lu % jb.nw);
@@ -856,11 +851,11 @@ fs3d_status planes_from_bytes(const uint8_t* g, int X, int Y, int Z, uint4* rows
     return FS3D_OK;
 }
 
-fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
-                                    const uint8_t* staging, int* flags, cudaStream_t st) {
+fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, const int* block_job, int njobs,
+                                    int64_t total_units, const uint8_t* staging, int* flags, cudaStream_t st) {
     if (njobs <= 0 || total_units <= 0) return FS3D_OK;
-    k_bytes_to_planes_multi<<<conv_grid(total_units), 256, 0, st>>>(jobs, unit_off, njobs, total_units, staging,
-                                                                     flags);
+    k_bytes_to_planes_multi<<<conv_grid(total_units), kConvBlock, 0, st>>>(jobs, unit_off, block_job, njobs,
+                                                                            total_units, staging, flags);
     FS3D_CHECK_LAUNCH("bytes->planes (many worlds) launch");
     return FS3D_OK;
 }
@@ -925,10 +920,11 @@ uint8_t* device_view(const void* p) {
     return nullptr;
 }
 
-fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
-                                  uint8_t* staging, cudaStream_t st) {
+fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, const int* block_job, int njobs,
+                                  int64_t total_units, uint8_t* staging, cudaStream_t st) {
     if (njobs <= 0 || total_units <= 0) return FS3D_OK;
-    k_planes_to_bytes_multi<<<conv_grid(total_units), 256, 0, st>>>(jobs, unit_off, njobs, total_units, staging);
+    k_planes_to_bytes_multi<<<conv_grid(total_units), kConvBlock, 0, st>>>(jobs, unit_off, block_job, njobs,
+                                                                            total_units, staging);
     FS3D_CHECK_LAUNCH("planes->bytes (many worlds) launch");
     return FS3D_OK;
 }

@@ -80,11 +80,21 @@ struct ConvJob {
     const uint8_t* static_src;
 };
 // bytes -> planes for njobs worlds in one launch; unit_off[j] = sum of Y*Z*nw
-// over jobs before j; flags[j] |= 1 when world j holds a material >= 4
-fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
-                                    const uint8_t* staging, int* flags, cudaStream_t st);
-fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, int njobs, int64_t total_units,
-                                  uint8_t* staging, cudaStream_t st);
+// over jobs before j; block_job[i] = the job of unit kConvBlock*i (from
+// conv_block_jobs); flags[j] |= 1 when world j holds a material >= 4
+constexpr int kConvBlock = 256;  // units per CTA pass of the conversion kernels
+inline int64_t conv_blocks(int64_t total_units) { return (total_units + kConvBlock - 1) / kConvBlock; }
+inline void conv_block_jobs(const int64_t* unit_off, int njobs, int64_t total_units, int* block_job) {
+    int j = 0;
+    for (int64_t i = 0; i < conv_blocks(total_units); ++i) {
+        while (j + 1 < njobs && unit_off[j + 1] <= i * kConvBlock) ++j;
+        block_job[i] = j;
+    }
+}
+fs3d_status planes_from_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, const int* block_job, int njobs,
+                                    int64_t total_units, const uint8_t* staging, int* flags, cudaStream_t st);
+fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, const int* block_job, int njobs,
+                                  int64_t total_units, uint8_t* staging, cudaStream_t st);
 
 // Many byte copies in one launch (each thread moves a 16-byte chunk): used
 // instead of one cudaMemcpyAsync per world when both sides are addressable
