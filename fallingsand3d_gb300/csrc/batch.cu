@@ -228,14 +228,22 @@ int segment_class(const fs3d_batch* b, const BWorld& w) {
     };
     auto gm = [&]() {
         const int c = resident_class_gm(w.X, w.Y, w.Z);
-        return c < 0 ? -1 : kResidentClasses + std::min(c + b->promote, kGmClasses - 1);
+        return c < 0 ? -1 : kResidentClasses + std::min(c + b->promote, kGmDense - 1);
     };
     if (mode == 1) return smem();
     if (mode == 2) return gm();
     if (mode == 3) {
-        const int first = (w.t < kYoungSteps) ? smem() : gm();
-        if (first >= 0) return first;
-        return (w.t < kYoungSteps) ? gm() : smem();
+        if (w.t < kYoungSteps) {
+            // a young world that needs a cluster runs instead from L2 with a
+            // whole SM (768 threads): dense steps keep its warps busy, and no
+            // cluster barrier or y-slab imbalance holds it up
+            const int c = smem();
+            if (c >= 0 && c < kSingleCtaClasses) return c;
+            if (w.Y <= 4096) return kResidentClasses + kGmDense;
+            return c >= 0 ? c : gm();
+        }
+        const int first = gm();
+        return first >= 0 ? first : smem();
     }
     return -1;
 }
@@ -441,16 +449,22 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
     }
     fs3d_status s = FS3D_OK;
     const int mode = b->cfg.use_smem;
-    // shared-memory classes widest first: their worlds are the largest and
-    // take the longest, and the launch order is the order the SMs fill in
+    // The launch order is the order the SMs fill in.  Young worlds: the large
+    // ones first (the dense global-memory class, then the shared-memory
+    // classes widest first), since they take the longest; settled worlds: the
+    // global-memory classes smallest CTA first, whose chains are the longest.
+    auto gm = [&](int c) {
+        return launch_plane_segment_gm(c, b->tw.d, b->to.d, b->tn.d, b->counter + kResidentClasses + c, b->err,
+                                       fork ? b->branch[kResidentClasses + c] : a, b->processed_dev);
+    };
+    if (mode == 3) s = gm(kGmDense);
     if (mode == 1 || mode == 3)
         for (int c = kResidentClasses - 1; c >= 0 && s == FS3D_OK; --c)
             s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
                                               fork ? b->branch[c] : a, b->processed_dev);
     if (mode == 2 || mode == 3)
         for (int c = 0; c < kGmClasses && s == FS3D_OK; ++c)
-            s = launch_plane_segment_gm(c, b->tw.d, b->to.d, b->tn.d, b->counter + kResidentClasses + c, b->err,
-                                        fork ? b->branch[kResidentClasses + c] : a, b->processed_dev);
+            if (c != kGmDense || mode == 2) s = gm(c);
     for (int k = 0; with_steps && k < b->cfg.steps_per_segment && s == FS3D_OK; ++k)
         s = launch_plane_step(b->tw.d, b->ti.d, b->tn.d, b->grid, k, fork ? b->branch[kAllClasses] : a);
     if (s != FS3D_OK) return s;

@@ -730,16 +730,16 @@ int resident_class(int X, int Y, int Z) {
 // step's barrier.  Each class caps the layers it holds flags for so that its
 // CTAs per SM (24 warps in all) fit in shared memory.
 namespace {
-constexpr int kGmThreads[kGmClasses] = {32, 64, 128, 256};
-constexpr int kGmMaxY[kGmClasses] = {1024, 1024, 2048, 4096};
+constexpr int kGmThreads[kGmClasses] = {32, 64, 128, 256, 768};
+constexpr int kGmMaxY[kGmClasses] = {1024, 1024, 2048, 4096, 4096};
 std::once_flag g_gm_once;
 }  // namespace
 
 int resident_class_gm(int X, int Y, int Z) {
     const int lanes = nblocks(Z, 1) << plane_lg(plane_nw(X));  // lane tasks of one layer pair
     int c = lanes <= 16 ? 0 : (lanes <= 48 ? 1 : (lanes <= 96 ? 2 : 3));
-    while (c < kGmClasses && Y > kGmMaxY[c]) ++c;
-    return c < kGmClasses ? c : -1;
+    while (c < kGmDense && Y > kGmMaxY[c]) ++c;
+    return c < kGmDense ? c : -1;
 }
 
 template <int NT>
@@ -759,7 +759,8 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
         const void* fns[kGmClasses] = {reinterpret_cast<const void*>(&k_plane_segment_resident<32, false, true>),
                                        reinterpret_cast<const void*>(&k_plane_segment_resident<64, false, true>),
                                        reinterpret_cast<const void*>(&k_plane_segment_resident<128, false, true>),
-                                       reinterpret_cast<const void*>(&k_plane_segment_resident<256, false, true>)};
+                                       reinterpret_cast<const void*>(&k_plane_segment_resident<256, false, true>),
+                                       reinterpret_cast<const void*>(&k_plane_segment_resident<768, false, true>)};
         for (const void* fn : fns) cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 50);
         cudaGetLastError();
     });
@@ -774,8 +775,10 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
         e = launch_gm<64>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
     else if (nt == 128)
         e = launch_gm<128>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
-    else
+    else if (nt == 256)
         e = launch_gm<256>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+    else
+        e = launch_gm<768>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
     if (e != cudaSuccess) return cuda_fail(e, "global-memory segment launch");
     note_launch();
     return FS3D_OK;

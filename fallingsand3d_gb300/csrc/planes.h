@@ -41,9 +41,11 @@ constexpr int kPlaneMaxX = 2048;  // lane groups of at most 32 words
 constexpr int kResidentClasses = 6;
 constexpr int kSingleCtaClasses = 3;  // classes 0..2 hold a world in one CTA
 // Global-memory segment classes (the world stays in L2/HBM; one CTA of
-// 32/64/128/256 threads per world, by the work of one layer pair); -1 if the
-// world has too many layers.
-constexpr int kGmClasses = 4;
+// 32/64/128/256 threads per world, by the work of one layer pair; -1 if the
+// world has too many layers), and kGmDense: one CTA of 768 threads per SM
+// for a young (dense) world too large for one CTA's shared memory.
+constexpr int kGmClasses = 5;
+constexpr int kGmDense = 4;
 int resident_class_gm(int X, int Y, int Z);
 // Class ids of a segment's tables: shared-memory classes 0..5, then the
 // global-memory classes 6..9.  meta = {per-step items, worlds per class,
