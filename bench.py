@@ -656,11 +656,25 @@ def run_only(args):
     `batched` runs warmup + steps segments of the 2048-world pool, `plain512`
     runs warmup + steps x 8 steps of the drop-in byte kernel on 512^3, `large`
     runs the 1024^3 dune world with a 1920x1080 frame after each of
-    --large-steps steps, `e2e` reads the pool back after 20 segments and runs
+    --large-steps steps, `fresh` runs one segment of the 2048 freshly
+    generated worlds, `e2e` reads the pool back after 20 segments and runs
     --e2e-steps pipelined e2e steps on those world states (after 3 waited-for
     warm-up steps)."""
     import torch
     import fallingsand3d_gb300 as fs3d
+    if args.only == "fresh":
+        # one segment of the freshly generated worlds (everything still falling)
+        worlds = batch_worlds(fs3d, args.master, args.worlds)
+        host = gen_grids(fs3d, worlds, pinned_torch=torch)
+        seeds = np.array([sd for _, sd in worlds], dtype=np.uint64)
+        dims = np.array([d for d, _ in worlds], dtype=np.int64)
+        ptrs = np.array([g.data_ptr() for g in host], dtype=np.uint64)
+        with fs3d.Batch(150 << 30, steps_per_segment=args.segment) as b:
+            ts = b.admit_many(None, seeds, args.segment, ptrs=ptrs, dims=dims)
+            b.run_segment()
+            b.retire_many(ts)
+        print(json.dumps({"only": args.only, "ok": True}))
+        return 0
     if args.only == "e2e":
         worlds = batch_worlds(fs3d, args.master, args.worlds)
         S = args.segment
@@ -740,7 +754,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh", "e2e"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh", "e2e", "fresh"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
