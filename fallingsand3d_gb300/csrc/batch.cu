@@ -1024,11 +1024,12 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     for (int a = 0; a < k && e == cudaSuccess;) {
         const int64_t cells = (int64_t)specs[a].X * specs[a].Y * specs[a].Z;
         const uint8_t* dv = device_view(specs[a].grid);
-        int e_run = a + 1;  // [a, e_run): sources and staging both contiguous
+        int e_run = a + 1;  // [a, e_run): sources and staging both contiguous, no padding between
         int64_t run_bytes = cells;
         while (dv && e_run < k) {
             const int64_t c = (int64_t)specs[e_run].X * specs[e_run].Y * specs[e_run].Z;
-            if (specs[e_run].grid != specs[e_run - 1].grid + (jobs[(size_t)e_run].byte_off - jobs[(size_t)e_run - 1].byte_off) ||
+            const int64_t c_prev = (int64_t)specs[e_run - 1].X * specs[e_run - 1].Y * specs[e_run - 1].Z;
+            if (specs[e_run].grid != specs[e_run - 1].grid + c_prev ||
                 run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)a].byte_off || !device_view(specs[e_run].grid))
                 break;
             run_bytes += c;
@@ -1272,8 +1273,11 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 int64_t run_bytes = cells;
                 while (dv && e_run < k) {
                     const BWorld& w2 = its[(size_t)who[(size_t)e_run]]->second;
-                    const int64_t d = jobs[(size_t)e_run].byte_off - jobs[(size_t)e_run - 1].byte_off;
-                    if (grids_out[who[(size_t)e_run]] != grids_out[who[(size_t)e_run - 1]] + d ||
+                    const BWorld& w1 = its[(size_t)who[(size_t)e_run - 1]]->second;
+                    // back to back in both, with no staging padding in between
+                    // (a run copy must not write the caller's bytes between grids)
+                    const int64_t c1 = (int64_t)w1.X * w1.Y * w1.Z;
+                    if (grids_out[who[(size_t)e_run]] != grids_out[who[(size_t)e_run - 1]] + c1 ||
                         run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)q].byte_off ||
                         !device_view(grids_out[who[(size_t)e_run]]))
                         break;
