@@ -287,7 +287,7 @@ def run_fs3d(args):
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
     # untimed: warm-up segments (at least five, so the worlds are past their
-    # first 256 steps, the phase where everything still falls), then the
+    # first steps, the phase where everything still falls), then the
     # launch configuration is chosen on real segments, then one more segment
     pre = max(args.warmup, 5)
     total_steps = S * (pre + 1 + args.steps + 1 + 32)
