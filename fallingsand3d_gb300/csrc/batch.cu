@@ -1024,13 +1024,18 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     for (int a = 0; a < k && e == cudaSuccess;) {
         const int64_t cells = (int64_t)specs[a].X * specs[a].Y * specs[a].Z;
         const uint8_t* dv = device_view(specs[a].grid);
-        int e_run = a + 1;  // [a, e_run): sources and staging both contiguous, no padding between
+        int e_run = a + 1;  // [a, e_run): sources and staging both contiguous, no padding between,
+                            // all in the first source's allocation
         int64_t run_bytes = cells;
-        while (dv && e_run < k) {
+        uintptr_t rs = 0;
+        size_t rn = 0;
+        const bool ranged = dv && alloc_range(specs[a].grid, &rs, &rn);
+        while (ranged && e_run < k) {
             const int64_t c = (int64_t)specs[e_run].X * specs[e_run].Y * specs[e_run].Z;
             const int64_t c_prev = (int64_t)specs[e_run - 1].X * specs[e_run - 1].Y * specs[e_run - 1].Z;
+            const uintptr_t g = reinterpret_cast<uintptr_t>(specs[e_run].grid);
             if (specs[e_run].grid != specs[e_run - 1].grid + c_prev ||
-                run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)a].byte_off || !device_view(specs[e_run].grid))
+                run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)a].byte_off || g + (uintptr_t)c > rs + rn)
                 break;
             run_bytes += c;
             ++e_run;
@@ -1271,15 +1276,21 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                 uint8_t* dv = device_view(out);
                 int e_run = q + 1;
                 int64_t run_bytes = cells;
-                while (dv && e_run < k) {
+                uintptr_t rs = 0;
+                size_t rn = 0;
+                const bool ranged = dv && alloc_range(out, &rs, &rn);
+                while (ranged && e_run < k) {
                     const BWorld& w2 = its[(size_t)who[(size_t)e_run]]->second;
                     const BWorld& w1 = its[(size_t)who[(size_t)e_run - 1]]->second;
                     // back to back in both, with no staging padding in between
-                    // (a run copy must not write the caller's bytes between grids)
+                    // (a run copy must not write the caller's bytes between
+                    // grids), and inside the first output's allocation (one copy
+                    // may not span two)
                     const int64_t c1 = (int64_t)w1.X * w1.Y * w1.Z;
+                    const uintptr_t g = reinterpret_cast<uintptr_t>(grids_out[who[(size_t)e_run]]);
                     if (grids_out[who[(size_t)e_run]] != grids_out[who[(size_t)e_run - 1]] + c1 ||
                         run_bytes != jobs[(size_t)e_run].byte_off - jobs[(size_t)q].byte_off ||
-                        !device_view(grids_out[who[(size_t)e_run]]))
+                        g + (uintptr_t)((int64_t)w2.X * w2.Y * w2.Z) > rs + rn)
                         break;
                     run_bytes += (int64_t)w2.X * w2.Y * w2.Z;
                     ++e_run;

@@ -998,6 +998,30 @@ uint8_t* device_view(const void* p) {
     return nullptr;
 }
 
+bool alloc_range(const void* p, uintptr_t* start, size_t* bytes) {
+    // cuPointerGetAttributes, looked up once through the runtime (no link
+    // dependency on the driver library)
+    using GetAttrs = int (*)(unsigned int, int*, void**, unsigned long long);
+    static GetAttrs fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<GetAttrs>(f);
+    }();
+    if (!fn || !p) return false;
+    unsigned long long base = 0, size = 0;
+    int attrs[2] = {11, 12};  // CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, CU_POINTER_ATTRIBUTE_RANGE_SIZE
+    void* data[2] = {&base, &size};
+    if (fn(2, attrs, data, (unsigned long long)reinterpret_cast<uintptr_t>(p)) != 0 || size == 0) return false;
+    if (reinterpret_cast<uintptr_t>(p) < base || reinterpret_cast<uintptr_t>(p) >= base + size) return false;
+    *start = (uintptr_t)base;
+    *bytes = (size_t)size;
+    return true;
+}
+
 fs3d_status planes_to_bytes_multi(const ConvJob* jobs, const int64_t* unit_off, const int* block_job, int njobs,
                                   int64_t total_units, uint8_t* staging, cudaStream_t st) {
     if (njobs <= 0 || total_units <= 0) return FS3D_OK;

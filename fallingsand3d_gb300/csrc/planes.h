@@ -111,6 +111,9 @@ fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, 
 // A device-addressable alias of p (itself for device or managed memory, the
 // mapped address for page-locked host memory), or nullptr for pageable memory.
 uint8_t* device_view(const void* p);
+// The allocation that holds p (start, bytes), as the driver reports it; false
+// if it cannot tell.  A copy over several grids must stay inside one.
+bool alloc_range(const void* p, uintptr_t* start, size_t* bytes);
 
 int plane_lg(int nw);
 int plane_items_for(int Y, int Z, int nw);

@@ -517,3 +517,47 @@ def test_async_admission_poll_and_single_retire(fs3d, orc, cuda):
             ref = g.copy()
             orc.run(ref, seed, 0, n, nthreads=0)
             assert (o == ref).all(), d
+
+
+def test_pipelined_steps_of_changing_sizes(fs3d, orc, cuda):
+    """Seven pipelined steps, each admitting a different set of worlds (the
+    staging buffers are reused round-robin and grow when a step needs more),
+    with static materials in some worlds and pageable as well as page-locked
+    inputs.  Every step's outputs equal the oracle."""
+    S = 16
+    rng = np.random.default_rng(7)
+    steps = []
+    for i in range(7):
+        count = [3, 9, 2, 14, 5, 11, 4][i]
+        worlds = small_batch(fs3d, 200 + i, count, max_dim=48 + 16 * (i % 3))
+        grids = _with_statics(fs3d, worlds, every=2 + i % 2)
+        pinned = i % 2 == 0
+        if pinned:
+            arena = cuda.from_numpy(np.concatenate([g.reshape(-1) for g in grids])).pin_memory()
+            offs = np.concatenate([[0], np.cumsum([g.size for g in grids])[:-1]]).astype(np.int64)
+            ptrs = [arena.data_ptr() + int(o) for o in offs]
+            keep = arena
+        else:
+            keep = [g.copy() for g in grids]
+            ptrs = [k.ctypes.data for k in keep]
+        outs = [cuda.zeros(g.shape, dtype=cuda.uint8).pin_memory() for g in grids]
+        start = int(rng.integers(0, 1000))
+        steps.append((worlds, grids, ptrs, keep, outs, start))
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        prev = None
+        for worlds, grids, ptrs, keep, outs, start in steps:
+            ts = b.admit_many(None, [s for _, s in worlds], S, start_steps=[start] * len(worlds), ptrs=ptrs,
+                              dims=[d for d, _ in worlds], wait=False)
+            assert len(ts) == len(worlds)
+            if prev is not None:
+                b.retire_many(prev[0], [o.data_ptr() for o in prev[1]], wait=False)
+            b.run_segment()
+            prev = (ts, outs)
+        b.retire_many(prev[0], [o.data_ptr() for o in prev[1]], wait=False)
+        b.wait_copies()
+        assert b.stats()["live_worlds"] == 0
+    for worlds, grids, ptrs, keep, outs, start in steps:
+        for (d, seed), g, o in zip(worlds, grids, outs):
+            ref = g.copy()
+            orc.run(ref, seed, start, S, nthreads=0)
+            assert (o.numpy() == ref).all(), (d, start)
