@@ -283,7 +283,7 @@ void free_world(fs3d_batch* b, BWorld& w) {
 // Stream-ordered allocation from the device's default pool (freed blocks stay
 // cached: its release threshold is raised when a batch is created).
 template <class T>
-cudaError_t pool_alloc(fs3d_batch*, T** p, size_t n, cudaStream_t st) {
+cudaError_t stream_alloc(T** p, size_t n, cudaStream_t st) {
     return cudaMallocAsync(reinterpret_cast<void**>(p), n, st);
 }
 
@@ -388,7 +388,7 @@ fs3d_status finalize_admits(fs3d_batch* b, uint64_t upto, bool wait) {
             w.admit_id = 0;
             if (!p.flags[a] || s != FS3D_OK) continue;
             const size_t cells = (size_t)p.cells[a];
-            cudaError_t e = pool_alloc(b, &w.statics, cells, b->side);
+            cudaError_t e = stream_alloc(&w.statics, cells, b->side);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(w.statics, p.staging + p.byte_off[a], cells, cudaMemcpyDeviceToDevice, b->side);
             if (e != cudaSuccess) {
@@ -607,12 +607,12 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     if (b->used + w.bytes > b->budget)
         return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
     uint8_t* staging = nullptr;
-    FS3D_CUDA(pool_alloc(b, &w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
+    FS3D_CUDA(stream_alloc(&w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
     w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(X, Y, Z);
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaSuccess;
     if (g) {
-        e = pool_alloc(b, &staging, n, b->side);
+        e = stream_alloc(&staging, n, b->side);
         if (e == cudaSuccess) e = cudaMemcpyAsync(staging, g, n, cudaMemcpyHostToDevice, b->side);
         s = e == cudaSuccess ? planes_from_bytes(staging, X, Y, Z, w.rows, b->side) : cuda_fail(e, "admit upload");
         if (stat)
@@ -896,7 +896,7 @@ fs3d_status retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out, bool sync)
     if (grid_out) {
         const size_t n = (size_t)w.X * w.Y * w.Z;
         uint8_t* staging = nullptr;
-        FS3D_CUDA(pool_alloc(b, &staging, n, b->side));
+        FS3D_CUDA(stream_alloc(&staging, n, b->side));
         s = planes_to_bytes(w.rows, w.statics, w.X, w.Y, w.Z, staging, b->side);
         cudaError_t e = cudaSuccess;
         if (s == FS3D_OK) e = cudaMemcpyAsync(grid_out, staging, n, cudaMemcpyDeviceToHost, b->side);
@@ -1001,7 +1001,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     fs3d_batch::StagingSlot* slot = take_slot(b->up_ring, b->up_turn, (size_t)bytes_total, up, &e);
     pa.staging = slot->p;
     slot->admit_id = pa.id;
-    if (e == cudaSuccess) e = pool_alloc(b, &pa.table, table_bytes, b->side);
+    if (e == cudaSuccess) e = stream_alloc(&pa.table, table_bytes, b->side);
     // grids the device can address (page-locked host or device memory) that lie
     // back to back go over in one copy-engine transfer per run (the SMs stay
     // free for segments in flight); other device-addressable grids are gathered
@@ -1017,7 +1017,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         block_bytes += (plane_bytes(specs[a].X, specs[a].Y, specs[a].Z) + layer_flag_bytes(specs[a].Y) + 255) & ~(size_t)255;
     }
     void* block = nullptr;
-    if (e == cudaSuccess) e = pool_alloc(b, &block, block_bytes, b->side);
+    if (e == cudaSuccess) e = stream_alloc(&block, block_bytes, b->side);
     for (int a = 0; a < k; ++a)
         rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
     uint8_t* staging = pa.staging;
@@ -1244,7 +1244,7 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
             cudaError_t e = cudaSuccess;
             rb_slot = take_slot(b->rb_ring, b->rb_turn, (size_t)bytes_total, rb, &e);
             staging = rb_slot->p;
-            if (e == cudaSuccess) e = pool_alloc(b, &table, table_bytes, rb);
+            if (e == cudaSuccess) e = stream_alloc(&table, table_bytes, rb);
             ConvJob* jobs_dev = static_cast<ConvJob*>(table);
             int64_t* off_dev = reinterpret_cast<int64_t*>(static_cast<char*>(table) + jobs_bytes);
             // the copy jobs are only known below: the table goes up in one
