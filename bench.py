@@ -353,36 +353,51 @@ def run_fs3d(args):
     # last step's grids are in host memory.  e2e_fresh: the same with the
     # freshly generated worlds at step 0 (everything still falling).
     h2d, d2h = cells, cells
-    outs = pinned_views(torch, [tuple(g.shape) for g in host])
+    # two output arenas: the two pipelined batches below write their results
+    # into their own
+    outs2 = [pinned_views(torch, [tuple(g.shape) for g in host]) for _ in range(2)]
+    outs = outs2[0]
     seeds = np.array([seed for _, seed in worlds], dtype=np.uint64)
     dims_xyz = np.array([d for d, _ in worlds], dtype=np.int64)
-    out_ptrs = np.array([o.data_ptr() for o in outs], dtype=np.uint64)
+    out_ptrs2 = [np.array([o.data_ptr() for o in ob], dtype=np.uint64) for ob in outs2]
+    out_ptrs = out_ptrs2[0]
 
     def e2e_run(inputs, start):
+        """Two batches take alternate steps, as a double-buffered server would:
+        one step's chain (upload, conversion, segment, conversion, download)
+        is longer than a step, and a batch cannot take the next step's worlds
+        before its segment is enqueued (the segment would step them too), so
+        two batches keep twice as many steps in flight."""
         in_ptrs = np.array([g.data_ptr() for g in inputs], dtype=np.uint64)
         starts = np.full(len(worlds), start, dtype=np.uint64)
         seq = []
-        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb:
-            # untimed warm-up (captures the segment graph, grows the pool),
+        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb0, fs3d.Batch(150 << 30, steps_per_segment=S) as eb1:
+            ebs = (eb0, eb1)
+            # untimed warm-up (captures the segment graphs, grows the pools),
             # then two steps through the waiting calls, one after the other
             for it in range(4):
+                eb = ebs[it % 2]
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 ts = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz)
                 eb.run_segment()
-                eb.retire_many(ts, out_ptrs)
+                eb.retire_many(ts, out_ptrs2[it % 2])
                 seq.append((time.perf_counter() - t0) * 1e3)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            prev = None
+            prev = [None, None]
             for it in range(args.e2e_steps):
-                ts = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz, wait=False)
-                if prev is not None:
-                    eb.retire_many(prev, out_ptrs, wait=False)
-                eb.run_segment()
-                prev = ts
-            eb.retire_many(prev, out_ptrs, wait=False)
-            eb.wait_copies()
+                k = it % 2
+                ts = ebs[k].admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz, wait=False)
+                if prev[k] is not None:
+                    ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
+                ebs[k].run_segment()
+                prev[k] = ts
+            for k in (0, 1):
+                if prev[k] is not None:
+                    ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
+            for eb in ebs:
+                eb.wait_copies()
             ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
         return ms, float(np.mean(seq[2:]))
 
@@ -543,8 +558,8 @@ def run_fs3d(args):
                         "inputs": f"the {len(worlds)} worlds as the timed segments left them (step {T0}), "
                                   f"admitted at that step every e2e step",
                         "path": "fs3d_batch_admit_many_async (pinned arena) + fs3d_batch_run_segment + "
-                                "fs3d_batch_retire_many_async (pinned arena), pipelined; fs3d_batch_wait_copies "
-                                "at the end",
+                                "fs3d_batch_retire_many_async (pinned arena), pipelined over two batches taking "
+                                "alternate steps; fs3d_batch_wait_copies at the end",
                         "sequential_ms": round(seq_ms, 2),
                         "sequential_path": "fs3d_batch_admit_many + fs3d_batch_run_segment + fs3d_batch_retire_many, "
                                            "each step waited for"},
