@@ -89,3 +89,19 @@ def test_object_render_rejects_before_launch(fs3d):
     with pytest.raises(fs3d.Fs3dError):
         fs3d.render_object_device(fs3d.object_view_scene(), np.concatenate([tri] * 5), 64, 32, fake)
     assert fs3d.mesh_cube().shape == (12, 3, 3)
+
+
+def test_no_cpu_fallback_without_a_gpu(fs3d):
+    """The product library has no CPU path for the step: on a machine with no
+    usable GPU, creating a world or a batch fails with FS3D_ERR_CUDA instead
+    of stepping on the host."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    g = fs3d.gen_parity(1)
+    with pytest.raises(fs3d.Fs3dError) as e:
+        fs3d.World(g, 1)
+    assert e.value.status == fs3d.ERR_CUDA
+    with pytest.raises(fs3d.Fs3dError) as e:
+        fs3d.Batch(1 << 30)
+    assert e.value.status == fs3d.ERR_CUDA
