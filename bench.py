@@ -363,42 +363,45 @@ def run_fs3d(args):
     out_ptrs = out_ptrs2[0]
 
     def e2e_run(inputs, start):
-        """Two batches take alternate steps, as a double-buffered server would:
-        one step's chain (upload, conversion, segment, conversion, download)
-        is longer than a step, and a batch cannot take the next step's worlds
-        before its segment is enqueued (the segment would step them too), so
-        two batches keep twice as many steps in flight."""
+        """--e2e-batches batches take steps in turn (default 1; with 2, as a
+        double-buffered server would, twice as many steps are in flight: a
+        batch cannot take the next step's worlds before its segment is
+        enqueued, since the segment would step them too)."""
         in_ptrs = np.array([g.data_ptr() for g in inputs], dtype=np.uint64)
         starts = np.full(len(worlds), start, dtype=np.uint64)
         seq = []
-        with fs3d.Batch(150 << 30, steps_per_segment=S) as eb0, fs3d.Batch(150 << 30, steps_per_segment=S) as eb1:
-            ebs = (eb0, eb1)
+        nb = max(1, min(2, args.e2e_batches))
+        ebs = [fs3d.Batch(150 << 30, steps_per_segment=S) for _ in range(nb)]
+        try:
             # untimed warm-up (captures the segment graphs, grows the pools),
             # then two steps through the waiting calls, one after the other
             for it in range(4):
-                eb = ebs[it % 2]
+                eb = ebs[it % nb]
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 ts = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz)
                 eb.run_segment()
-                eb.retire_many(ts, out_ptrs2[it % 2])
+                eb.retire_many(ts, out_ptrs2[it % nb])
                 seq.append((time.perf_counter() - t0) * 1e3)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            prev = [None, None]
+            prev = [None] * nb
             for it in range(args.e2e_steps):
-                k = it % 2
+                k = it % nb
                 ts = ebs[k].admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz, wait=False)
                 if prev[k] is not None:
                     ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
                 ebs[k].run_segment()
                 prev[k] = ts
-            for k in (0, 1):
+            for k in range(nb):
                 if prev[k] is not None:
                     ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
             for eb in ebs:
                 eb.wait_copies()
             ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+        finally:
+            for eb in ebs:
+                eb.close()
         return ms, float(np.mean(seq[2:]))
 
     fresh_ms, fresh_seq = e2e_run(host, 0)
@@ -558,8 +561,9 @@ def run_fs3d(args):
                         "inputs": f"the {len(worlds)} worlds as the timed segments left them (step {T0}), "
                                   f"admitted at that step every e2e step",
                         "path": "fs3d_batch_admit_many_async (pinned arena) + fs3d_batch_run_segment + "
-                                "fs3d_batch_retire_many_async (pinned arena), pipelined over two batches taking "
-                                "alternate steps; fs3d_batch_wait_copies at the end",
+                                "fs3d_batch_retire_many_async (pinned arena), pipelined; fs3d_batch_wait_copies "
+                                "at the end",
+                        "batches": max(1, min(2, args.e2e_batches)),
                         "sequential_ms": round(seq_ms, 2),
                         "sequential_path": "fs3d_batch_admit_many + fs3d_batch_run_segment + fs3d_batch_retire_many, "
                                            "each step waited for"},
@@ -757,6 +761,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--e2e-steps", type=int, default=20, help="timed steps of the e2e leg")
+    ap.add_argument("--e2e-batches", type=int, default=1, help="batches taking the e2e steps in turn (1 or 2)")
     ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
     ap.add_argument("--worlds", type=int, default=2048)
     ap.add_argument("--master", type=int, default=1)
