@@ -1168,6 +1168,12 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
         if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_retire_many: unknown ticket");
         its.push_back(it);
     }
+    {
+        std::vector<uint64_t> sorted(tickets, tickets + n);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+            return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: a ticket appears twice");
+    }
     // admissions whose flags have arrived are completed (static copies made);
     // a world whose admission is still open reads its static bytes, if its
     // flag says it has any, straight from that admission's staging bytes

@@ -561,3 +561,20 @@ def test_pipelined_steps_of_changing_sizes(fs3d, orc, cuda):
             ref = g.copy()
             orc.run(ref, seed, start, S, nthreads=0)
             assert (o.numpy() == ref).all(), (d, start)
+
+
+def test_retire_many_rejects_a_repeated_ticket(fs3d, orc):
+    """A ticket listed twice in one retire_many is an argument error; nothing
+    is retired and the batch stays usable."""
+    worlds = small_batch(fs3d, 51, 3, max_dim=32)
+    with fs3d.Batch(GiB, steps_per_segment=32) as b:
+        ts = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, 32) for dims, seed in worlds]
+        b.run_segment()
+        with pytest.raises(fs3d.Fs3dError) as e:
+            b.retire_many([ts[0], ts[1], ts[0]])
+        assert e.value.status == fs3d.ERR_INVALID_ARG
+        assert b.stats()["live_worlds"] == 3
+        outs = [np.zeros((Y, Z, X), dtype=np.uint8) for (X, Y, Z), _ in worlds]
+        b.retire_many(ts, [o.ctypes.data for o in outs])
+        for o, (dims, seed) in zip(outs, worlds):
+            assert (o == oracle_final(orc, fs3d, dims, seed, 32)).all()
