@@ -39,14 +39,6 @@ UNIT = "voxel-updates/s"
 L2_FLUSH_BYTES = 512 << 20
 
 
-def baseline_metric():
-    try:
-        with open(os.path.join(ROOT, "BASELINE.json")) as f:
-            return json.load(f).get("metric", METRIC)
-    except OSError:
-        return METRIC
-
-
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -252,7 +244,7 @@ def run_reference(args):
         v, info = cpu_sample(worlds, args.cpu_budget / max(args.steps, 1), threads)
         vals.append(v)
     v = float(np.mean(vals))
-    line = {"metric": baseline_metric(), "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
             "config": {"workload": f"batched: {args.worlds} mixed worlds (bounded CPU sample)",
@@ -545,7 +537,7 @@ def run_fs3d(args):
             mesh.update(res["mesh"])
 
     if rank == 0:
-        line = {"metric": baseline_metric(), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "u8", "data": "synthetic",
                 "config": {"workload": f"batched: {args.worlds} worlds, dims iid from {{16,24,32,48,64,96,128}}^3, "
