@@ -1,16 +1,20 @@
 // fs3d_batch: many independent worlds of mixed sizes in one device pool (bit
-// plane format), stepped together.  A segment is `steps_per_segment` launches
-// of the multi-world step kernel captured once as a CUDA graph; the graph
-// reads the world and work-item tables from device memory, so worlds join
-// (admit) and leave (retire) between segments without a re-capture.  Each
-// world keeps its own step counter, so its trajectory is the same whether it
-// runs alone or inside any mix.
+// plane format), stepped together.  A segment is one CUDA graph: a persistent
+// kernel per size class runs each of its worlds through all of the segment's
+// steps (plus, for worlds too large for any class, steps_per_segment launches
+// of the per-step kernel), then a small kernel advances every world's step
+// counter in the device table.  The graph reads the world and work-item
+// tables from device memory, so worlds join (admit) and leave (retire)
+// between segments without a re-capture, and an unchanged batch reuses the
+// tables as they stand.  Each world keeps its own step counter, so its
+// trajectory is the same whether it runs alone or inside any mix.
 //
-// Streams: `stream` runs segments; `side` runs admissions (upload + format
-// conversion) and single retirements, `readback` the read-backs of
-// retire_many (conversion + download), all ordered against the segments with
-// events, so uploads and downloads run over the host link in both directions
-// while a segment computes.
+// Streams: `stream` runs segments; `upload` the host-to-device copies of
+// admit_many; `side` the admission conversions and single retirements;
+// `readback` the read-back conversions of retire_many; `download` their
+// device-to-host copies.  Events order them against the segments and each
+// other, and no stream waits for work its next item does not need, so both
+// directions of the host link run while a segment computes.
 #include <string.h>
 
 #include <algorithm>
