@@ -736,6 +736,12 @@ def run_only(args):
             for _ in range(args.steps):
                 b.run_segment()
             b.sync()
+    elif args.only == "plain512p":
+        # the same world in the plane layout (per-step plane kernel), 8 steps per warm-up/step
+        g = fs3d.gen_pillars(1, 512, 512, 512)
+        with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
+            w.step(8 * (args.warmup + args.steps))
+            w.sync()
     else:
         g = fs3d.gen_pillars(1, 512, 512, 512)
         d = torch.from_numpy(g).cuda()
@@ -766,7 +772,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "large", "mesh", "e2e", "fresh"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "plain512p", "large", "mesh", "e2e", "fresh"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:

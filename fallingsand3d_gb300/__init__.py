@@ -39,7 +39,7 @@ ERR_IO = -9
 EXPORTS = (
     "fs3d_abi_version", "fs3d_status_string", "fs3d_last_error", "fs3d_kernel_launch_count",
     "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_run_device",
-    "fs3d_run_device_noalloc", "fs3d_hash_device", "fs3d_first_diff_device",
+    "fs3d_run_device_noalloc", "fs3d_run_device_check", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
@@ -48,7 +48,7 @@ EXPORTS = (
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
     "fs3d_render_object", "fs3d_render_meshes", "fs3d_gen_parity", "fs3d_gen_pillars",
-    "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes",
+    "fs3d_gen_batch_dims", "fs3d_gen_batch_world", "fs3d_gen_dunes", "fs3d_test_inject",
 )
 
 
@@ -67,7 +67,8 @@ class Camera(C.Structure):
 class ServeParams(C.Structure):
     _fields_ = [("lambda_", C.c_double), ("duration_s", C.c_double), ("max_requests", C.c_int64),
                 ("master_seed", C.c_uint64), ("hbm_budget", C.c_size_t), ("steps_per_segment", C.c_int),
-                ("min_steps", C.c_int), ("max_steps", C.c_int), ("with_hash", C.c_int), ("reserved", C.c_int * 8)]
+                ("min_steps", C.c_int), ("max_steps", C.c_int), ("with_hash", C.c_int),
+                ("segment_timeout_ms", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class ServeRequest(C.Structure):
@@ -138,6 +139,8 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_step_device_simple": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_run_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_run_device_noalloc": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_run_device_check": (S, [vp, i64]),
+        "fs3d_test_inject": (S, [i32, i32]),
         "fs3d_hash_device": (S, [vp, i64, vp, C.POINTER(u64)]),
         "fs3d_first_diff_device": (S, [vp, vp, i64, vp, C.POINTER(i64)]),
         "fs3d_world_create": (S, [vp, i32, i32, i32, u64, u64, i32, C.POINTER(vp)]),
@@ -326,6 +329,20 @@ def step_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_ste
 def run_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
     """n steps of a device grid through the bit-plane kernels (device scratch)."""
     check(lib().fs3d_run_device(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
+
+
+def run_device_check(stream: int = 0, timeout_ns: int = -1) -> None:
+    """Waits for `stream`, then raises Fs3dError(ERR_TIMEOUT) if a drop-in run on
+    this device gave up a bounded copy wait since the last check (and clears it)."""
+    check(lib().fs3d_run_device_check(stream, timeout_ns))
+
+
+INJECT_NONE, INJECT_COPY_STALL, INJECT_ALLOC_FAIL = 0, 1, 2
+
+
+def inject(what: int, count: int = 1) -> None:
+    """Failure injection for tests (fs3d_test_inject); INJECT_NONE clears it."""
+    check(lib().fs3d_test_inject(what, count))
 
 
 def step_device_simple(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int,
@@ -617,8 +634,9 @@ class Batch:
 # ---------------------------------------------------------------- serving
 def serve_params(lam: float, duration_s: float, master_seed: int = 1, max_requests: int = 0,
                  hbm_budget: int = 0, steps_per_segment: int = 64, min_steps: int = 10, max_steps: int = 1000,
-                 with_hash: bool = True) -> ServeParams:
+                 with_hash: bool = True, segment_timeout_ms: int = 0) -> ServeParams:
     p = ServeParams()
+    p.segment_timeout_ms = segment_timeout_ms
     p.lambda_, p.duration_s, p.max_requests, p.master_seed = lam, duration_s, max_requests, master_seed
     p.hbm_budget, p.steps_per_segment, p.min_steps, p.max_steps = hbm_budget, steps_per_segment, min_steps, max_steps
     p.with_hash = 1 if with_hash else 0

@@ -5,8 +5,10 @@
 
 #include <atomic>
 #include <string>
+#include <utility>
 
 #include "fs3d_common.h"
+#include "planes.h"
 
 namespace fs3d {
 
@@ -25,6 +27,29 @@ fs3d_status cuda_fail(cudaError_t e, const char* what) {
 }
 
 void note_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+bool current_context_id(unsigned long long* id) {
+    // cuCtxGetCurrent and cuCtxGetId, looked up once through the runtime (no
+    // link dependency on the driver library)
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static const std::pair<GetCurrent, GetId> fns = [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            a = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            b = nullptr;
+        cudaGetLastError();
+        return std::make_pair(reinterpret_cast<GetCurrent>(a), reinterpret_cast<GetId>(b));
+    }();
+    if (!fns.first || !fns.second) return false;
+    void* ctx = nullptr;  // null: no context is current on this thread yet
+    if (fns.first(&ctx) != 0 || !ctx) return false;
+    return fns.second(ctx, id) == 0;
+}
 
 }  // namespace fs3d
 
@@ -51,6 +76,21 @@ const char* fs3d_status_string(fs3d_status s) {
 const char* fs3d_last_error(void) { return fs3d::g_last_error.c_str(); }
 
 uint64_t fs3d_kernel_launch_count(void) { return fs3d::g_launches.load(); }
+
+fs3d_status fs3d_test_inject(int what, int count) {
+    switch (what) {
+        case FS3D_INJECT_NONE:
+            fs3d::set_inject_alloc_failures(0);
+            return fs3d::set_inject_tx_extra(0u);
+        case FS3D_INJECT_COPY_STALL:
+            return fs3d::set_inject_tx_extra(count > 0 ? 16u : 0u);
+        case FS3D_INJECT_ALLOC_FAIL:
+            fs3d::set_inject_alloc_failures(count);
+            return FS3D_OK;
+        default:
+            return fs3d::set_error(FS3D_ERR_INVALID_ARG, "fs3d_test_inject: unknown injection");
+    }
+}
 
 fs3d_config fs3d_default_config(void) {
     fs3d_config c;

@@ -18,7 +18,7 @@
 #include <string.h>
 
 #include <algorithm>
-
+#include <atomic>
 #include <chrono>
 #include <deque>
 #include <map>
@@ -291,6 +291,20 @@ cudaError_t stream_alloc(T** p, size_t n, cudaStream_t st) {
     return cudaMallocAsync(reinterpret_cast<void**>(p), n, st);
 }
 
+// Test hook (fs3d_test_inject): admissions whose world memory allocation is
+// refused as out of memory, without asking the device.
+std::atomic<int> g_inject_alloc_failures{0};
+
+// The allocation of an admission's world memory (planes and layer flags).
+template <class T>
+cudaError_t admission_alloc(T** p, size_t n, cudaStream_t st) {
+    int left = g_inject_alloc_failures.load();
+    while (left > 0 && !g_inject_alloc_failures.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left > 0) return cudaErrorMemoryAllocation;
+    return stream_alloc(p, n, st);
+}
+
 // A page-locked buffer of at least n flags, from the batch's pool.
 int* take_flags(fs3d_batch* b, size_t n, size_t* cap) {
     for (size_t i = 0; i < b->flag_pool.size(); ++i)
@@ -514,6 +528,10 @@ fs3d_status capture_graph(fs3d_batch* b) {
 
 }  // namespace
 
+namespace fs3d {
+void set_inject_alloc_failures(int n) { g_inject_alloc_failures.store(n > 0 ? n : 0); }
+}  // namespace fs3d
+
 extern "C" {
 
 fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch** out) {
@@ -538,8 +556,8 @@ fs3d_status fs3d_batch_create(size_t budget, const fs3d_config* cfg, fs3d_batch*
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->processed_dev, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->processed_dev, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counter, sizeof(int) * kAllClasses);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int) * kErrInts);
+    if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int) * kErrInts);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     for (int c = 0; c <= kAllClasses && e == cudaSuccess; ++c) {
         e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming);
@@ -611,7 +629,7 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     if (b->used + w.bytes > b->budget)
         return set_error(FS3D_ERR_BUDGET, "fs3d_batch_admit: world does not fit in the memory budget now");
     uint8_t* staging = nullptr;
-    FS3D_CUDA(stream_alloc(&w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
+    FS3D_CUDA(admission_alloc(&w.rows, plane_bytes(X, Y, Z) + layer_flag_bytes(Y), b->side));
     w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(X, Y, Z);
     fs3d_status s = FS3D_OK;
     cudaError_t e = cudaSuccess;
@@ -843,7 +861,10 @@ fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns) {
     if (s != FS3D_OK) return s;
     int err = 0;
     FS3D_CUDA(cudaMemcpy(&err, b->err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
+    if (err)
+        return set_error(FS3D_ERR_TIMEOUT,
+                         "a shared-memory bulk copy did not complete in time: the segments from that one on "
+                         "stepped nothing, so the worlds' states no longer match their step counters");
     s = wait_stream(b->side, timeout_ns);
     if (s == FS3D_OK) s = wait_stream(b->readback, timeout_ns);
     return s == FS3D_OK ? wait_stream(b->download, timeout_ns) : s;
@@ -1021,7 +1042,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         block_bytes += (plane_bytes(specs[a].X, specs[a].Y, specs[a].Z) + layer_flag_bytes(specs[a].Y) + 255) & ~(size_t)255;
     }
     void* block = nullptr;
-    if (e == cudaSuccess) e = stream_alloc(&block, block_bytes, b->side);
+    if (e == cudaSuccess) e = admission_alloc(&block, block_bytes, b->side);
     for (int a = 0; a < k; ++a)
         rows[(size_t)a] = reinterpret_cast<uint4*>(static_cast<char*>(block) + row_off[(size_t)a]);
     uint8_t* staging = pa.staging;
@@ -1213,7 +1234,8 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
     fs3d_status s = FS3D_OK;
     uint8_t* staging = nullptr;
     void* table = nullptr;
-    std::shared_ptr<CUevent_st> read;  // recorded after the conversion
+    std::shared_ptr<CUevent_st> read;    // recorded after the conversion
+    std::shared_ptr<CUevent_st> copied;  // recorded after the copy kernel (download stream), if one ran
     fs3d_batch::StagingSlot* rb_slot = nullptr;  // the read-back's staging buffer
     if (grids_out) {
         std::vector<ConvJob> jobs;
@@ -1341,17 +1363,37 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
                                     cudaMemcpyDefault, dl);
                 if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_retire_many readback");
             }
-            if (s == FS3D_OK && !copies.empty()) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, dl);
+            if (s == FS3D_OK && !copies.empty()) {
+                s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, dl);
+                // the copy kernel reads its jobs from `table` on the download
+                // stream, which the read-back stream never waits for: the table
+                // is freed once an event after that kernel has run
+                if (s == FS3D_OK) {
+                    copied = shared_event();
+                    if (copied && cudaEventRecord(copied.get(), dl) != cudaSuccess) copied.reset();
+                    if (!copied) cudaStreamSynchronize(dl);
+                }
+            }
         }
     }
     if (!read) read = record_read(rb);
     if (!read && s == FS3D_OK) s = set_error(FS3D_ERR_CUDA, "fs3d_batch_retire_many: event");
-    // the staging buffer is free again after the downloads, the tables after the conversion
+    // the staging buffer is free again after the downloads, the tables after
+    // the conversion (and after the copy kernel, when one reads them)
     if (rb_slot) {
         mark_busy(rb_slot, b->download);
         mark_busy(rb_slot, rb);
     }
-    if (table) cudaFreeAsync(table, rb);
+    if (table && copied) {
+        // the conversion (read-back stream) precedes the copy kernel
+        // (download stream waits for `read`), so `copied` covers both readers
+        fs3d_batch::DeferredFree df;
+        df.after = copied;
+        df.ptrs = {table};
+        b->deferred.push_back(std::move(df));
+    } else if (table) {
+        cudaFreeAsync(table, rb);
+    }
     // the worlds' memory goes back once the conversion has read it
     fs3d_batch::DeferredFree d;
     d.after = read;

@@ -60,6 +60,11 @@ FS3D_HD int nblocks(int n, int o) { return (n + o + 1) >> 1; }
 fs3d_status set_error(fs3d_status s, const std::string& msg);
 fs3d_status cuda_fail(cudaError_t e, const char* what);
 void note_launch(uint64_t n = 1);
+// Unique id of the calling thread's current CUDA context; false if no context
+// is current yet (the runtime makes one current on its first device call) or
+// the driver cannot tell.  A device address cached for one context is stale
+// in another (after cudaDeviceReset, for example).
+bool current_context_id(unsigned long long* id);
 
 }  // namespace fs3d
 

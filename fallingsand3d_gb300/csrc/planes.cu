@@ -396,9 +396,18 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Waits for the mbarrier phase with an iteration limit; false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the mbarrier phase for at most limit_ns nanoseconds of the global
+// timer (try_wait itself may suspend for a while, so the bound is on time, not
+// on tries); false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint64_t limit_ns) {
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0;; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -409,13 +418,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
             : "memory");
         if (done) return true;
         if (it > 64) __nanosleep(64);
+        if ((it & 63u) == 63u && global_ns() - t0 > limit_ns) return false;
     }
-    return false;
 }
 
+// The bulk-copy wait's limit: two seconds, far beyond any copy's time (one
+// slab of at most a few hundred KB); 20 ms under the copy-stall test hook, so
+// a test that makes every wait run out stays short.
+constexpr uint64_t kCopyWaitNs = 2000000000ull, kCopyWaitInjectedNs = 20000000ull;
+
+// Test hook (fs3d_test_inject): extra bytes every resident kernel announces
+// on its mbarrier beyond what its bulk copy delivers.  With it set, the copy
+// lands in full but the barrier's phase never completes, so each wait runs to
+// its iteration limit and reports a timeout; nothing else changes.  0 in
+// normal operation.
+static __device__ uint32_t g_inject_tx_extra;
+
 // TMA bulk copy global -> shared, completion counted in bytes on `bar`
-__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+// (`expect` = bytes, or more under the test hook above)
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint32_t bytes, uint32_t expect,
+                                          uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(expect)
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(smem_dst)),
@@ -582,6 +605,7 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
     };
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
+    const uint32_t tx_extra = g_inject_tx_extra;
     uint32_t phase = 0;
     const int lane = threadIdx.x & 31;
     uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
@@ -614,7 +638,7 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
         v.fmine = reinterpret_cast<uint8_t*>(srows) + slab_flag_offset(bytes);
         v.fleft = left ? reinterpret_cast<uint8_t*>(left) + slab_flag_offset((uint32_t)(v.lo - v.left_lo) * row_bytes)
                        : nullptr;
-        if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, &bar);
+        if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, bytes + tx_extra, &bar);
         // change buffers from the kept flags (the low 8 bits of the last step
         // that changed the layer), or every layer changed at t0 - 1 and t0 - 2
         {
@@ -630,15 +654,17 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
         }
         bool ok = true;
         if (bytes) {
-            ok = mbar_wait(&bar, phase);
-            if (!ok) ok = mbar_wait(&bar, phase);  // a second bounded chance for a late copy
+            ok = mbar_wait(&bar, phase, tx_extra ? kCopyWaitInjectedNs : kCopyWaitNs);
             phase ^= 1u;
         }
-        // A copy that never landed poisons the world: the error flag is
-        // raised, this CTA still takes part in every barrier of its group but
-        // touches no memory, and the group stops before its next world.
+        // A copy that never landed poisons the world: the error record is
+        // set (err[0] = 1, err[2..3] = the world's step at the start of this
+        // launch, by the first group to fail), this CTA still takes part in
+        // every barrier of its group but touches no memory, and the group
+        // stops before its next world.
         const bool poisoned = __syncthreads_or(!ok) != 0;
-        if (poisoned && threadIdx.x == 0) atomicExch(err, 1);
+        if (poisoned && threadIdx.x == 0 && atomicCAS(err, 0, 1) == 0)
+            *reinterpret_cast<unsigned long long*>(err + 2) = (unsigned long long)w.t;
         group_sync();  // every slab is loaded before a neighbour reads it
         const int G = 1 << w.lg, per = NT >> w.lg;
         const int gl = lane & (G - 1);
@@ -856,6 +882,11 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
         e = launch_gm<768>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
     if (e != cudaSuccess) return cuda_fail(e, "global-memory segment launch");
     note_launch();
+    return FS3D_OK;
+}
+
+fs3d_status set_inject_tx_extra(uint32_t bytes) {
+    FS3D_CUDA(cudaMemcpyToSymbol(g_inject_tx_extra, &bytes, sizeof(bytes)));
     return FS3D_OK;
 }
 

@@ -57,9 +57,17 @@ constexpr int kMetaInts = kMetaWorlds + 1;
 int resident_class(int X, int Y, int Z);
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable
 int smem_world_limit();
+constexpr int kErrInts = 4;  // size of the error record a resident launch is given
+// test hook: resident kernels announce `bytes` more than each bulk copy delivers
+fs3d_status set_inject_tx_extra(uint32_t bytes);
+// test hook: the next n stream-ordered allocations of batch admissions fail as out of memory
+void set_inject_alloc_failures(int n);
 // One launch steps every world of class `cls` (order[meta[1+K+cls] ...],
-// meta[1+cls] of them) through its segment steps in shared memory.  *err is
-// set to 1 if a bulk copy does not complete within the wait limit.  Row
+// meta[1+cls] of them) through its segment steps in shared memory.  err
+// points to 4 ints (8-byte aligned): a bulk copy that does not complete
+// within the wait limit sets err[0] = 1 and err[2..3] = the failing world's
+// step at the start of the launch (first failure only); while err[0] is set,
+// launches given it step nothing.  Row
 // pairs whose rows are settled are skipped; the cell-steps actually evaluated
 // are added to *processed_cells when it is not null.
 fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, const int* order, const int* meta,

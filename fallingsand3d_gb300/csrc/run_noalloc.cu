@@ -18,11 +18,16 @@
 //  * every GPU that loads this library holds the array (64 MiB + 1 MiB) until
 //    the process exits;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that
-//    first call before any stream capture;
+//    cudaGetSymbolAddress (with that device current) and caches it for the
+//    device's current context (a new context after cudaDeviceReset looks it
+//    up again); make that first call before any stream capture;
 //  * every call shares the array and it keeps the last call's contents; the
 //    call clears what must start at zero itself.  Calls that overlap on the
-//    GPU (two streams, or two host threads) race on the array: serialise them.
+//    GPU (two streams, or two host threads) race on the array: serialise them;
+//  * one word of the array records a bulk copy whose bounded wait gave up
+//    (the run leaves the grid as it was).  It is not cleared by the calls, so
+//    later runs on the device also leave their grids unchanged until
+//    fs3d_run_device_check reads and clears it.
 #include <mutex>
 
 #include "fs3d_common.h"
@@ -35,21 +40,28 @@ constexpr size_t kNoAllocPlaneBytes = (size_t)64 << 20;
 constexpr size_t kNoAllocMaxItems = 1u << 17;  // per-step work items (1 MiB)
 constexpr int kMaxDevices = 64;
 
-// scratch layout: [planes][one-world descriptor][ints][work items]
+// scratch layout: [planes][one-world descriptor][ints][sticky error word][work items]
 constexpr size_t kDescOff = kNoAllocPlaneBytes;
 constexpr size_t kIntsOff = kDescOff + 256;
-constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kErr = kCounter + 1, kInts = kErr + 1;
-constexpr size_t kItemsOff = kIntsOff + 256;
+constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kInts = kCounter + 1;
+constexpr size_t kErrOff = kIntsOff + 256;  // set by a timed-out copy, cleared by fs3d_run_device_check only
+constexpr size_t kItemsOff = kErrOff + 256;
 constexpr size_t kScratchBytes = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
 static_assert(kInts * sizeof(int) <= 256, "ints region");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-unsigned char* g_scratch_addr[kMaxDevices] = {};
+// the array's device address per device, for the context it was looked up in
+struct ScratchAddr {
+    unsigned long long ctx = 0;  // 0: unknown, look it up again
+    unsigned char* p = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_mu;
 
 // Writes the one-world tables into the scratch and clears the work counter
-// and the error flag (the array keeps whatever the previous call left).
+// (the array keeps whatever the previous call left; the sticky error word is
+// left alone).
 __global__ void k_noalloc_tables(PlaneWorld d, int cls, int n_items, int per, unsigned char* base) {
     PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
     int* ints = reinterpret_cast<int*>(base + kIntsOff);
@@ -64,21 +76,38 @@ __global__ void k_noalloc_tables(PlaneWorld d, int cls, int n_items, int per, un
     for (int a = tid; a < n_items; a += gridDim.x * blockDim.x) items[a] = PlaneItem{0, a * per};
 }
 
-fs3d_status scratch_base(unsigned char** out) {
+}  // namespace
+
+// The array's device address on the current device.  Host code cannot use
+// the array's name as a device address (it names a host-side stand-in), so
+// the address is looked up with cudaGetSymbolAddress, with the device
+// current, and kept per device for the context it belongs to.
+fs3d_status noalloc_scratch_base(unsigned char** out) {
     int dev = 0;
     FS3D_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: device index");
+    unsigned long long ctx = 0;
+    const bool known = current_context_id(&ctx);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    ScratchAddr& c = g_scratch_addr[dev];
+    if (!known || !c.p || !c.ctx || c.ctx != ctx) {
         void* p = nullptr;
         FS3D_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+        c.p = static_cast<unsigned char*>(p);
+        // the lookup made the device's context current if none was
+        c.ctx = current_context_id(&ctx) ? ctx : 0;
     }
-    *out = g_scratch_addr[dev];
+    *out = c.p;
     return FS3D_OK;
 }
 
-}  // namespace
+fs3d_status noalloc_error_word(int** out) {
+    unsigned char* base = nullptr;
+    const fs3d_status s = noalloc_scratch_base(&base);
+    if (s == FS3D_OK) *out = reinterpret_cast<int*>(base + kErrOff);
+    return s;
+}
+
 }  // namespace fs3d
 
 using namespace fs3d;
@@ -97,7 +126,7 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: too many row-pairs for the static scratch");
     if (n_steps == 0) return FS3D_OK;
     unsigned char* base = nullptr;
-    fs3d_status s = scratch_base(&base);
+    fs3d_status s = noalloc_scratch_base(&base);
     if (s != FS3D_OK) return s;
     cudaStream_t st = (cudaStream_t)stream;
     uint4* rows = reinterpret_cast<uint4*>(base);
@@ -119,7 +148,8 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
     s = planes_from_bytes(grid_dev, X, Y, Z, rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
-            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, ints + kErr, st);
+            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter,
+                                              reinterpret_cast<int*>(base + kErrOff), st);
         } else {
             const int grid = plane_step_grid(n_items);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) s = launch_plane_step(desc, items, ints, grid, a, st);

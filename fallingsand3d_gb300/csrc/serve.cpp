@@ -88,6 +88,7 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
             return s;
         }
     }
+    const int64_t seg_timeout_ns = (int64_t)(p->segment_timeout_ms > 0 ? p->segment_timeout_ms : 10000) * 1000000;
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
     auto now_s = [&] { return std::chrono::duration<double>(clk::now() - t0).count(); };
@@ -124,8 +125,9 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
         peak_live = std::max(peak_live, lw);
         peak_bytes = std::max(peak_bytes, used);
         if (segment_in_flight) {
-            // arrivals during the segment were admitted above; now wait for it
-            s = fs3d_batch_sync(b, -1);
+            // arrivals during the segment were admitted above; now wait for it,
+            // within the deadline (a segment that does not end in time ends the run)
+            s = fs3d_batch_sync(b, seg_timeout_ns);
             segment_in_flight = false;
             if (s != FS3D_OK) break;
             for (auto it = live.begin(); it != live.end();) {
@@ -160,6 +162,17 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
         }
     }
     st->wall_s = now_s();
+    if (s == FS3D_ERR_TIMEOUT) {
+        // A segment still running past the deadline: the batch is not torn
+        // down (its teardown would wait for that work) and its memory stays
+        // allocated.  A segment that ended but reported a kernel's bounded
+        // wait giving up leaves nothing running, so the batch is released.
+        void* stream = nullptr;
+        fs3d_batch_stream(b, &stream);
+        if (cudaStreamQuery((cudaStream_t)stream) == cudaSuccess) fs3d_batch_destroy(b);
+        cudaGetLastError();
+        return s;
+    }
     fs3d_batch_destroy(b);
     if (s != FS3D_OK) return s;
     st->requests = n;

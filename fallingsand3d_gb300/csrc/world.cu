@@ -43,8 +43,8 @@ namespace {
 constexpr int kAuxMeta = 0;                              // kMetaInts ints
 constexpr int kAuxOrder = kMetaInts;      // order[0] = 0
 constexpr int kAuxCounter = kAuxOrder + 1;
-constexpr int kAuxErr = kAuxCounter + 1;
-constexpr int kAuxInts = kAuxErr + 1;
+constexpr int kAuxErr = (kAuxCounter + 2) & ~1;   // kErrInts ints, 8-byte aligned
+constexpr int kAuxInts = kAuxErr + kErrInts;
 
 bool dims_ok(int X, int Y, int Z) {
     return X > 0 && Y > 0 && Z > 0 && X <= (1 << 16) && Y <= (1 << 16) && Z <= (1 << 16);
@@ -220,10 +220,23 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
 fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
     if (!w) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_sync: NULL world");
     fs3d_status s = bounded_wait(w->stream, timeout_ns);
-    if (s != FS3D_OK || !w->aux) return s;
-    int err = 0;
-    FS3D_CUDA(cudaMemcpy(&err, w->aux + kAuxErr, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) return set_error(FS3D_ERR_TIMEOUT, "a shared-memory bulk copy did not complete in time");
+    if (s != FS3D_OK) return s;
+    if (w->aux) {
+        int err[kErrInts] = {};
+        FS3D_CUDA(cudaMemcpy(err, w->aux + kAuxErr, sizeof(err), cudaMemcpyDeviceToHost));
+        if (err[0]) {
+            // the failed launch and every launch after it stepped nothing: the
+            // state is the one the failed launch started from
+            uint64_t t_fail = 0;
+            memcpy(&t_fail, err + 2, sizeof(t_fail));
+            FS3D_CUDA(cudaMemset(w->aux + kAuxErr, 0, sizeof(err)));
+            w->step = t_fail;
+            w->counts_valid = false;
+            return set_error(FS3D_ERR_TIMEOUT,
+                             "a shared-memory bulk copy did not complete in time; the world was set back to the "
+                             "step its state holds");
+        }
+    }
     return FS3D_OK;
 }
 

@@ -123,6 +123,15 @@ fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t see
  * project (it has no step). */
 fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,
                                     uint64_t t0, int n_steps, void* stream);
+/* Waits for `stream` (timeout_ns < 0: without limit; FS3D_ERR_TIMEOUT when
+ * the limit passes first), then reports whether a drop-in run on the current
+ * device (fs3d_run_device or fs3d_run_device_noalloc) met a bulk copy that
+ * did not complete within its bounded wait since the last check:
+ * FS3D_ERR_TIMEOUT if so, and the record is cleared.  Such a run leaves its
+ * grid as it was, and so does every drop-in run on the device after it until
+ * this check.  The runs are asynchronous, so this is where a caller learns of
+ * it.  No counterpart in the upstream project (it has no step). */
+fs3d_status fs3d_run_device_check(void* stream, int64_t timeout_ns);
 /* Same contract, one thread per 2x2x2 block and byte loads: the plain
  * reference kernel the vectorised one is checked against. */
 fs3d_status fs3d_step_device_simple(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed,
@@ -139,7 +148,12 @@ fs3d_status fs3d_first_diff_device(const uint8_t* a_dev, const uint8_t* b_dev, i
 fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uint64_t seed,
                               uint64_t start_step, int layout, fs3d_world** out);
 fs3d_status fs3d_world_step(fs3d_world* w, int n_steps);           /* async */
-fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns);     /* bounded wait */
+/* Bounded wait (timeout_ns < 0: without limit).  FS3D_ERR_TIMEOUT also when a
+ * step launch of the world met a bulk copy that did not complete within its
+ * bounded wait: that launch and the ones after it stepped nothing, so the
+ * world's step counter is set back to the step its state holds, and the
+ * world is usable again. */
+fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns);
 fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* grid_host_out); /* canonical layout */
 fs3d_status fs3d_world_write(fs3d_world* w, const uint8_t* grid_host); /* replace contents */
 fs3d_status fs3d_world_hash(fs3d_world* w, uint64_t* out);
@@ -246,7 +260,9 @@ typedef struct fs3d_serve_params {
     int min_steps;           /* 0 = 10                                             */
     int max_steps;           /* 0 = 1000                                           */
     int with_hash;           /* 1 = hash every finished world (request.hash)       */
-    int reserved[8];
+    int segment_timeout_ms;  /* bound on the wait for one segment (0 = 10000); the
+                                run ends with FS3D_ERR_TIMEOUT when it passes       */
+    int reserved[7];
 } fs3d_serve_params;
 
 typedef struct fs3d_serve_request {
@@ -344,6 +360,19 @@ typedef struct fs3d_mesh_draw {
 /* n_draws <= 65536, fewer than 2^30 triangles in all */
 fs3d_status fs3d_render_meshes(const fs3d_object_view* view, const fs3d_mesh_draw* draws, int n_draws, int W, int H,
                                float* rgba_dev, void* stream);
+
+/* ---- test hooks (failure injection without a GPU fault) ----
+ * COPY_STALL (count > 0: on, 0: off): the resident step kernels announce 16
+ * bytes more on their mbarrier than each bulk copy delivers; the copy lands
+ * in full, the barrier's phase never completes, and every such wait runs to
+ * its iteration limit (about a second) and reports a timeout.
+ * ALLOC_FAIL: the next `count` world-memory allocations of batch admissions
+ * fail as out of device memory (decided on the host; nothing is launched).
+ * NONE clears both.  For tests only. */
+#define FS3D_INJECT_NONE 0
+#define FS3D_INJECT_COPY_STALL 1
+#define FS3D_INJECT_ALLOC_FAIL 2
+fs3d_status fs3d_test_inject(int what, int count);
 
 /* ---- synthetic worlds (seeded, bit-reproducible) ---- */
 fs3d_status fs3d_gen_parity(uint64_t seed, int X, int Y, int Z, uint8_t* grid_host);

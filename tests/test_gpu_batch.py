@@ -578,3 +578,29 @@ def test_retire_many_rejects_a_repeated_ticket(fs3d, orc):
         b.retire_many(ts, [o.ctypes.data for o in outs])
         for o, (dims, seed) in zip(outs, worlds):
             assert (o == oracle_final(orc, fs3d, dims, seed, 32)).all()
+
+
+def test_back_to_back_async_retires_into_scattered_pinned_outputs(fs3d, orc, cuda):
+    """Four retire_many_async calls in a row, with no segment between them,
+    into separately page-locked outputs (each its own allocation, so the
+    device-side copy kernel writes them) of different world sizes.  Each
+    call's copy jobs stay readable until its copy kernel has run, whatever the
+    calls after it allocate; every output equals the oracle."""
+    S = 24
+    groups = [small_batch(fs3d, 300 + i, c, max_dim=m) for i, (c, m) in enumerate([(7, 96), (3, 32), (12, 64),
+                                                                                   (5, 128)])]
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        tickets = []
+        for worlds in groups:
+            tickets.append([b.admit(fs3d.gen_batch_world(seed, *dims), seed, S) for dims, seed in worlds])
+        b.run_segment()
+        outs = []
+        for worlds, ts in zip(groups, tickets):
+            o = [cuda.zeros((Y, Z, X), dtype=cuda.uint8).pin_memory() for (X, Y, Z), _ in worlds]
+            b.retire_many(ts, [t.data_ptr() for t in o], wait=False)
+            outs.append(o)
+        b.wait_copies()
+        assert b.stats()["live_worlds"] == 0
+    for worlds, o in zip(groups, outs):
+        for (dims, seed), t in zip(worlds, o):
+            assert (t.numpy() == oracle_final(orc, fs3d, dims, seed, S)).all(), dims
