@@ -133,20 +133,10 @@ static int draw(int n, uint32_t rk, int i, int s) {
     return u < 85u ? 0 : (u < 170u ? 1 : 2);
 }
 
-/* Update block (i,j,k) of step t in place.  Returns 1 if anything moved. */
-static int block_update(uint8_t* grid, int X, int Y, int Z, int o, uint32_t rk, int i, int j,
-                        int k, int dry) {
-    const int bx = 2 * i - o, by = 2 * j - o, bz = 2 * k - o;
-    int64_t idx[8];
-    int inb[8];
-    uint8_t v[8];
-    for (int s = 0; s < 8; ++s) {
-        const int L = s >> 2, q = s & 3;
-        const int x = bx + (q & 1), y = by + (1 - L), z = bz + (q >> 1);
-        inb[s] = (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z);
-        idx[s] = inb[s] ? (int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * (int64_t)y) : -1;
-        v[s] = inb[s] ? grid[idx[s]] : (uint8_t)1; /* out of bounds acts as solid */
-    }
+/* The rule on one block held as 8 values v[s] (slot s; out-of-grid slots
+ * have inb[s] = 0 and hold 1, solid).  Updates v in place; returns 1 if
+ * anything moved (with `dry`, returns at the first move without applying it). */
+static int block_rule8(uint8_t* v, const int* inb, uint32_t rk, int i, int dry) {
     unsigned moved = 0;
     int changed = 0;
     for (int s = 0; s < 8; ++s) {
@@ -180,7 +170,25 @@ static int block_update(uint8_t* grid, int X, int Y, int Z, int o, uint32_t rk, 
             changed = 1;
         }
     }
-    if (changed)
+    return changed;
+}
+
+/* Update block (i,j,k) of step t in place.  Returns 1 if anything moved. */
+static int block_update(uint8_t* grid, int X, int Y, int Z, int o, uint32_t rk, int i, int j,
+                        int k, int dry) {
+    const int bx = 2 * i - o, by = 2 * j - o, bz = 2 * k - o;
+    int64_t idx[8];
+    int inb[8];
+    uint8_t v[8];
+    for (int s = 0; s < 8; ++s) {
+        const int L = s >> 2, q = s & 3;
+        const int x = bx + (q & 1), y = by + (1 - L), z = bz + (q >> 1);
+        inb[s] = (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z);
+        idx[s] = inb[s] ? (int64_t)x + (int64_t)X * ((int64_t)z + (int64_t)Z * (int64_t)y) : -1;
+        v[s] = inb[s] ? grid[idx[s]] : (uint8_t)1; /* out of bounds acts as solid */
+    }
+    const int changed = block_rule8(v, inb, rk, i, dry);
+    if (changed && !dry)
         for (int s = 0; s < 8; ++s)
             if (inb[s]) grid[idx[s]] = v[s];
     return changed;
@@ -188,15 +196,68 @@ static int block_update(uint8_t* grid, int X, int Y, int Z, int o, uint32_t rk, 
 
 static inline int nblocks(int n, int o) { return (n + o + 1) / 2; }
 
+/* One block row (j, k) of step t: the same rule as block_update for every i,
+ * with the four rows addressed once.  A block changes only if it holds a
+ * particle (2 or 3) and an empty cell (the stability property above), so
+ * blocks without both are passed over. */
+static void block_row(uint8_t* grid, int X, int Y, int Z, int o, uint32_t sk, int j, int k) {
+    const int by = 2 * j - o, bz = 2 * k - o;
+    uint8_t* row[4]; /* slot column q = dz*2 + dx: rows (layer, dz) -> index (1-L)*2 + dz */
+    int rin[4];
+    for (int r = 0; r < 4; ++r) {
+        const int L = r >> 1, dz = r & 1;
+        const int y = by + (1 - L), z = bz + dz;
+        rin[r] = y >= 0 && y < Y && z >= 0 && z < Z;
+        row[r] = rin[r] ? grid + (int64_t)X * ((int64_t)z + (int64_t)Z * (int64_t)y) : NULL;
+    }
+    const uint32_t rk = orc_rowkey(sk, (uint32_t)j, (uint32_t)k);
+    const int NBX = nblocks(X, o);
+    for (int i = 0; i < NBX; ++i) {
+        const int x0 = 2 * i - o;
+        if ((i & 3) == 0 && x0 >= 0 && x0 + 8 <= X) {
+            /* four blocks at once (x0 .. x0+7 of the four rows): none can change
+             * unless their cells hold both a particle and an empty cell */
+            int part = 0, empty = 0;
+            for (int r = 0; r < 4; ++r) {
+                if (!rin[r]) continue; /* outside the grid: solid */
+                uint64_t c;
+                memcpy(&c, row[r] + x0, 8);
+                const uint64_t lo = 0x0101010101010101ull, hi = 0x8080808080808080ull;
+                const uint64_t p = (c & 0xFEFEFEFEFEFEFEFEull) ^ 0x0202020202020202ull; /* 0 byte: 2 or 3 */
+                part |= ((p - lo) & ~p & hi) != 0;
+                empty |= ((c - lo) & ~c & hi) != 0;
+            }
+            if (!part || !empty) {
+                i += 3;
+                continue;
+            }
+        }
+        uint8_t v[8];
+        int inb[8];
+        int part = 0, empty = 0;
+        for (int s = 0; s < 8; ++s) {
+            const int L = s >> 2, q = s & 3;
+            const int r = L * 2 + (q >> 1), x = x0 + (q & 1);
+            inb[s] = rin[r] && x >= 0 && x < X;
+            v[s] = inb[s] ? row[r][x] : (uint8_t)1;
+            part |= v[s] == 2 || v[s] == 3;
+            empty |= v[s] == 0;
+        }
+        if (!part || !empty) continue;
+        if (block_rule8(v, inb, rk, i, 0))
+            for (int s = 0; s < 8; ++s) {
+                const int L = s >> 2, q = s & 3;
+                if (inb[s]) row[L * 2 + (q >> 1)][x0 + (q & 1)] = v[s];
+            }
+    }
+}
+
 void orc_step(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t) {
     const int o = (int)(t & 1u);
     const uint32_t sk = orc_stepkey(seed, t);
-    const int NBX = nblocks(X, o), NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
+    const int NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
     for (int j = 0; j < NBY; ++j)
-        for (int k = 0; k < NBZ; ++k) {
-            const uint32_t rk = orc_rowkey(sk, (uint32_t)j, (uint32_t)k);
-            for (int i = 0; i < NBX; ++i) block_update(grid, X, Y, Z, o, rk, i, j, k, 0);
-        }
+        for (int k = 0; k < NBZ; ++k) block_row(grid, X, Y, Z, o, sk, j, k);
 }
 
 void orc_step_shuffled(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t,
@@ -230,7 +291,7 @@ void orc_step_shuffled(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64
 void orc_step_omp(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t, int nthreads) {
     const int o = (int)(t & 1u);
     const uint32_t sk = orc_stepkey(seed, t);
-    const int NBX = nblocks(X, o), NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
+    const int NBY = nblocks(Y, o), NBZ = nblocks(Z, o);
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for schedule(static) num_threads(nthreads) collapse(2)
@@ -238,10 +299,7 @@ void orc_step_omp(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t,
     (void)nthreads;
 #endif
     for (int j = 0; j < NBY; ++j)
-        for (int k = 0; k < NBZ; ++k) {
-            const uint32_t rk = orc_rowkey(sk, (uint32_t)j, (uint32_t)k);
-            for (int i = 0; i < NBX; ++i) block_update(grid, X, Y, Z, o, rk, i, j, k, 0);
-        }
+        for (int k = 0; k < NBZ; ++k) block_row(grid, X, Y, Z, o, sk, j, k);
 }
 
 void orc_run(uint8_t* grid, int X, int Y, int Z, uint64_t seed, uint64_t t0, int n,
@@ -1020,7 +1078,7 @@ int orc_render_meshes(const orc_object_view* view, const orc_mesh_draw* draws, i
             mat4_mul(vp, draws[d].model, mvp);
             scr_tri st[3];
             setup_prim(mvp, draws[d].vertices + 15 * (prim - base), W, H, st);
-            float l[3];
+            float l[3] = {0.0f, 0.0f, 0.0f}; /* the winner covers this pixel centre: tri_cover sets them */
             tri_cover(&st[q], (float)px + 0.5f, (float)py + 0.5f, l);
             const orc_mesh_draw* dr = &draws[d];
             float r = dr->color[0], g = dr->color[1], b = dr->color[2], a = dr->color[3];
