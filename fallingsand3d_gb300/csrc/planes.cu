@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "fs3d_common.h"
@@ -28,6 +29,7 @@
 #include "planes.h"
 #include "conv_device.cuh"
 #include "rule_device.cuh"
+#include "bricks_device.cuh"
 
 namespace fs3d {
 
@@ -70,7 +72,8 @@ __device__ __forceinline__ uint32_t cell_value(const uint4& q, int m, int odd, c
 }
 
 __global__ void k_planes_to_bytes(const uint4* __restrict__ rows, const uint8_t* __restrict__ statics, int X,
-                                  int Y, int Z, int nw, uint8_t* __restrict__ g) {
+                                  int Y, int Z, int nw, uint8_t* __restrict__ g, const int* skip_if_set) {
+    if (skip_if_set && *(volatile const int*)skip_if_set) return;
     const int64_t n = (int64_t)Y * Z * nw;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
         const int w = (int)(u % nw);
@@ -273,64 +276,6 @@ __global__ void k_gen_batch_planes(int X, int Y, int Z, int nw, BatchWorldGen p,
 // ---------------------------------------------------------------------------
 // One block row-pair of one world; lane gl of a group of G lanes.  Every lane
 // of the warp calls this (valid = false for groups past the last row-pair).
-// Non-empty cells of each 8-cell group of a plane word, as bytes: lo byte k
-// counts group 2k, hi byte k group 2k + 1 (at most 8 each).
-__device__ __forceinline__ void group_counts(const uint4& q, uint32_t& lo, uint32_t& hi) {
-    uint32_t e = q.x | q.z, o = q.y | q.w;  // bit m of nibble i: a non-empty cell of group i
-    e = e - ((e >> 1) & 0x55555555u);
-    e = (e & 0x33333333u) + ((e >> 2) & 0x33333333u);
-    o = o - ((o >> 1) & 0x55555555u);
-    o = (o & 0x33333333u) + ((o >> 2) & 0x33333333u);
-    lo = (e & 0x0F0F0F0Fu) + (o & 0x0F0F0F0Fu);
-    hi = ((e >> 4) & 0x0F0F0F0Fu) + ((o >> 4) & 0x0F0F0F0Fu);
-}
-
-// Adds one row pair's net change of non-empty cells to the per-brick counts
-// (bricks of 8x8x8 cells, index bx + BX*(bz + BZ*by)).  The four rows are
-// split by the brick they lie in (they share one unless the pair straddles a
-// brick face in y or z); per part the group counts are summed bytewise,
-// before and after, and only the groups whose sum moved reach an atomic, so
-// cells moving within a brick cost none.  The counts stay exact: a brick is
-// empty exactly when its count is 0.
-__device__ __forceinline__ void count_bricks(int* __restrict__ counts, const PlaneWorld& w, int y0, int z0, int gl,
-                                             const uint4 (&q)[4], const uint4 (&q0)[4], const bool (&in)[4]) {
-    const int BX = (w.X + 7) >> 3, BZ = (w.Z + 7) >> 3;
-    const bool ysplit = ((y0 + 1) & 7) == 0, zsplit = ((z0 + 1) & 7) == 0;
-#pragma unroll
-    for (int part = 0; part < 4; ++part) {
-        if ((part & 1) && !ysplit) continue;
-        if ((part & 2) && !zsplit) continue;
-        uint32_t nlo = 0, nhi = 0, olo = 0, ohi = 0;
-        bool any = false;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            // rows a = 0, 1 are layer y0 + 1 (part bit 0 when the pair straddles y),
-            // rows a = 1, 3 are z0 + 1 (part bit 1 when it straddles z)
-            const int pa = (ysplit && a < 2 ? 1 : 0) | (zsplit && (a & 1) ? 2 : 0);
-            if (pa != part || !in[a]) continue;
-            uint32_t l, h;
-            group_counts(q[a], l, h);
-            nlo += l;
-            nhi += h;
-            group_counts(q0[a], l, h);
-            olo += l;
-            ohi += h;
-            any = true;
-        }
-        if (!any || (nlo == olo && nhi == ohi)) continue;
-        const int y = (part & 1) ? y0 + 1 : (ysplit ? y0 : y0 + 1);
-        const int z = (part & 2) ? z0 + 1 : z0;
-        const int64_t row = (int64_t)BX * ((z >> 3) + (int64_t)BZ * (y >> 3));
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const uint32_t nb = (((i & 1) ? nhi : nlo) >> (8 * (i >> 1))) & 0xFFu;
-            const uint32_t ob = (((i & 1) ? ohi : olo) >> (8 * (i >> 1))) & 0xFFu;
-            const int bx = 8 * gl + i;
-            if (nb != ob && bx < BX) atomicAdd(counts + row + bx, (int)nb - (int)ob);
-        }
-    }
-}
-
 __device__ __forceinline__ void plane_rowpair(const PlaneWorld& w, int o, uint32_t sk, int rp, bool valid, int gl,
                                               int G, int* counts) {
     const int NBZ = nblocks(w.Z, o);
@@ -885,10 +830,17 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
     return FS3D_OK;
 }
 
+namespace {
+std::atomic<uint32_t> g_inject_tx_extra_host{0};  // the same value, for kernels that take it as an argument
+}  // namespace
+
 fs3d_status set_inject_tx_extra(uint32_t bytes) {
     FS3D_CUDA(cudaMemcpyToSymbol(g_inject_tx_extra, &bytes, sizeof(bytes)));
+    g_inject_tx_extra_host.store(bytes);
     return FS3D_OK;
 }
+
+uint32_t inject_tx_extra() { return g_inject_tx_extra_host.load(); }
 
 int smem_world_limit() {
     init_classes();
@@ -1071,9 +1023,9 @@ fs3d_status planes_generate_batch_world(uint64_t world_seed, int X, int Y, int Z
 }
 
 fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, uint8_t* g,
-                            cudaStream_t st) {
+                            cudaStream_t st, const int* skip_if_set) {
     const int nw = plane_nw(X);
-    k_planes_to_bytes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, statics, X, Y, Z, nw, g);
+    k_planes_to_bytes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, statics, X, Y, Z, nw, g, skip_if_set);
     FS3D_CHECK_LAUNCH("planes->bytes launch");
     return FS3D_OK;
 }

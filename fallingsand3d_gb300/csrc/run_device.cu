@@ -76,18 +76,25 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     if (n_steps == 0) return FS3D_OK;
     if (X > kPlaneMaxX) return launch_step_bytes(grid_dev, X, Y, Z, seed, t0, n_steps, st);
     const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
-    const int n_items = cls >= 0 ? 0 : plane_items_for(Y, Z, nw);
+    // worlds too large for shared memory: the tiled per-step kernel (rows of
+    // 2..32 words), else the per-step kernel with its work items
+    const bool tiled = cls < 0 && tiled_supported(X, Y, Z);
+    const int n_items = cls >= 0 || tiled ? 0 : plane_items_for(Y, Z, nw);
     int* err = nullptr;
-    if (cls >= 0) {
+    if (cls >= 0 || tiled) {
         const fs3d_status se = run_error_word(&err);
         if (se != FS3D_OK) return se;
     }
     RunScratch sc;
+    uint32_t* flags = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&sc.rows, plane_bytes(X, Y, Z), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.desc, sizeof(PlaneWorld), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.ints, sizeof(int) * kInts, st);
     if (e == cudaSuccess && n_items) e = cudaMallocAsync((void**)&sc.items, sizeof(PlaneItem) * n_items, st);
+    if (e == cudaSuccess && tiled) e = cudaMallocAsync((void**)&flags, tiled_flag_bytes(Y, Z), st);
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_run_device scratch");
+    alignas(64) unsigned char tmap[128];
+    if (s == FS3D_OK && tiled) s = tiled_encode(sc.rows, X, Y, Z, tmap);
     PlaneWorld d{};
     d.rows = sc.rows;
     d.seed = seed;
@@ -113,17 +120,25 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     if (s == FS3D_OK) {
         if (cls >= 0) {
             s = launch_plane_segment_resident(cls, sc.desc, sc.ints + kOrder, sc.ints, sc.ints + kCounter, err, st);
+        } else if (tiled) {
+            s = tiled_init_flags(flags, Y, Z, t0, st);
+            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
+                d.t = t0 + (uint64_t)a;
+                s = launch_plane_step_tiled(tmap, d, flags, nullptr, err, st);
+            }
         } else {
             const int grid = plane_step_grid(n_items);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
                 s = launch_plane_step(sc.desc, sc.items, sc.ints, grid, a, st);
         }
     }
-    if (s == FS3D_OK) s = planes_to_bytes(sc.rows, grid_dev, X, Y, Z, grid_dev, st);
+    // a recorded failure (this run's or an earlier one's) leaves the grid as it was
+    if (s == FS3D_OK) s = planes_to_bytes(sc.rows, grid_dev, X, Y, Z, grid_dev, st, err);
     cudaFreeAsync(sc.rows, st);
     cudaFreeAsync(sc.desc, st);
     cudaFreeAsync(sc.ints, st);
     if (sc.items) cudaFreeAsync(sc.items, st);
+    if (flags) cudaFreeAsync(flags, st);
     return s;
 }
 

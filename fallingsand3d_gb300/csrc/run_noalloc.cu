@@ -15,8 +15,8 @@
 //  * the world's planes must fit kNoAllocPlaneBytes (64 MiB: about 268 M
 //    cells, e.g. 512^3), and rows wider than 2048 cells are refused; larger
 //    worlds are rejected with FS3D_ERR_INVALID_ARG and a message;
-//  * every GPU that loads this library holds the array (64 MiB + 1 MiB) until
-//    the process exits;
+//  * every GPU that loads this library holds the array (64 MiB of planes +
+//    3 MiB of tables and flags) until the process exits;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it for the
 //    device's current context (a new context after cudaDeviceReset looks it
@@ -40,13 +40,15 @@ constexpr size_t kNoAllocPlaneBytes = (size_t)64 << 20;
 constexpr size_t kNoAllocMaxItems = 1u << 17;  // per-step work items (1 MiB)
 constexpr int kMaxDevices = 64;
 
-// scratch layout: [planes][one-world descriptor][ints][sticky error word][work items]
+// scratch layout: [planes][one-world descriptor][ints][sticky error word][work items][row change flags]
 constexpr size_t kDescOff = kNoAllocPlaneBytes;
 constexpr size_t kIntsOff = kDescOff + 256;
 constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kInts = kCounter + 1;
 constexpr size_t kErrOff = kIntsOff + 256;  // set by a timed-out copy, cleared by fs3d_run_device_check only
 constexpr size_t kItemsOff = kErrOff + 256;
-constexpr size_t kScratchBytes = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
+constexpr size_t kFlagsOff = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
+constexpr size_t kNoAllocFlagBytes = (size_t)2 << 20;  // row change flags of the tiled per-step kernel
+constexpr size_t kScratchBytes = kFlagsOff + kNoAllocFlagBytes;
 static_assert(kInts * sizeof(int) <= 256, "ints region");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -121,7 +123,8 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
                          "fs3d_run_device_noalloc: world too large for the static scratch (planes of at most "
                          "64 MiB, about 268 M cells, and rows of at most 2048 cells)");
     const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
-    const int n_items = cls >= 0 ? 0 : plane_items_for(Y, Z, nw);
+    const bool tiled = cls < 0 && tiled_supported(X, Y, Z) && tiled_flag_bytes(Y, Z) <= kNoAllocFlagBytes;
+    const int n_items = cls >= 0 || tiled ? 0 : plane_items_for(Y, Z, nw);
     if ((size_t)n_items > kNoAllocMaxItems)
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: too many row-pairs for the static scratch");
     if (n_steps == 0) return FS3D_OK;
@@ -145,17 +148,28 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
     PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
     int* ints = reinterpret_cast<int*>(base + kIntsOff);
     PlaneItem* items = reinterpret_cast<PlaneItem*>(base + kItemsOff);
+    int* err = reinterpret_cast<int*>(base + kErrOff);
     s = planes_from_bytes(grid_dev, X, Y, Z, rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
-            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter,
-                                              reinterpret_cast<int*>(base + kErrOff), st);
+            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, err, st);
+        } else if (tiled) {
+            // the tensor map is a host-side description: encoding it allocates nothing
+            alignas(64) unsigned char tmap[128];
+            uint32_t* flags = reinterpret_cast<uint32_t*>(base + kFlagsOff);
+            s = tiled_encode(rows, X, Y, Z, tmap);
+            if (s == FS3D_OK) s = tiled_init_flags(flags, Y, Z, t0, st);
+            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
+                d.t = t0 + (uint64_t)a;
+                s = launch_plane_step_tiled(tmap, d, flags, nullptr, err, st);
+            }
         } else {
             const int grid = plane_step_grid(n_items);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) s = launch_plane_step(desc, items, ints, grid, a, st);
         }
     }
-    // static cells never change: their values are read back from the grid itself
-    if (s == FS3D_OK) s = planes_to_bytes(rows, grid_dev, X, Y, Z, grid_dev, st);
+    // static cells never change: their values are read back from the grid
+    // itself; a recorded failure leaves the grid as it was
+    if (s == FS3D_OK) s = planes_to_bytes(rows, grid_dev, X, Y, Z, grid_dev, st, err);
     return s;
 }

@@ -34,6 +34,13 @@ struct fs3d_world {
     uint32_t* brickmap = nullptr;  // render: per-frame occupancy of 8x8x8 bricks
     int* brick_counts = nullptr;   // PLANES render: non-empty cells per brick, kept by the per-step kernel
     bool counts_valid = false;     // brick_counts match the planes
+    // PLANES worlds stepped by the tiled per-step kernel: its tensor map and row change flags
+    bool tiled = false;
+    alignas(64) unsigned char tmap[128] = {};
+    uint32_t* tflags = nullptr;
+    bool flags_ok = false;  // tflags describe the state at step flags_t
+    uint64_t flags_t = 0;
+    bool broken = false;    // a per-step launch failed part-way: the state must be rewritten
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
 
@@ -85,6 +92,7 @@ void destroy(fs3d_world* w) {
     cudaFree(w->hash_dev);
     cudaFree(w->brickmap);
     cudaFree(w->brick_counts);
+    cudaFree(w->tflags);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
 }
@@ -168,6 +176,16 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
             e = cudaMemcpy(w->items, items.data(), sizeof(PlaneItem) * items.size(), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(w->n_items_dev, &w->n_items, sizeof(int), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return fail(e, "cudaMalloc/copy(step tables)");
+        if (w->cls < 0 && tiled_supported(X, Y, Z)) {
+            e = cudaMalloc((void**)&w->tflags, tiled_flag_bytes(Y, Z));
+            if (e != cudaSuccess) return fail(e, "cudaMalloc(row change flags)");
+            s = tiled_encode(w->rows, X, Y, Z, w->tmap);
+            if (s != FS3D_OK) {
+                destroy(w);
+                return s;
+            }
+            w->tiled = true;
+        }
     }
     s = upload(w, grid_host);
     if (s != FS3D_OK) {
@@ -180,6 +198,7 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
 
 fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
     if (!w || n_steps < 0) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_step: bad args");
+    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_step: the world must be rewritten (fs3d_world_write)");
     if (n_steps == 0) return FS3D_OK;
     fs3d_status s;
     if (w->layout == FS3D_LAYOUT_BYTES) {
@@ -196,9 +215,29 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
         d.nw = nw;
         d.steps = n_steps;
         d.lg = plane_lg(nw);
+        s = FS3D_OK;
+        if (w->tiled) {
+            // one launch per step; the row change flags carry over from the
+            // previous call when nothing else touched the world since
+            if (!w->flags_ok || w->flags_t != w->step) {
+                s = tiled_init_flags(w->tflags, w->Y, w->Z, w->step, w->stream);
+                w->flags_ok = s == FS3D_OK;
+            }
+            int* counts = w->counts_valid ? w->brick_counts : nullptr;
+            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
+                d.t = w->step + (uint64_t)a;
+                s = launch_plane_step_tiled(w->tmap, d, w->tflags, counts, w->aux + kAuxErr, w->stream);
+            }
+            if (s == FS3D_OK) {
+                w->flags_t = w->step + (uint64_t)n_steps;
+                w->step += (uint64_t)n_steps;
+            } else {
+                w->flags_ok = false;
+            }
+            return s;
+        }
         // pageable source: staged before the call returns
         FS3D_CUDA(cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream));
-        s = FS3D_OK;
         if (w->cls >= 0) {
             // the world fits in shared memory (one CTA or a cluster): all n steps in one launch
             s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
@@ -225,13 +264,22 @@ fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
         int err[kErrInts] = {};
         FS3D_CUDA(cudaMemcpy(err, w->aux + kAuxErr, sizeof(err), cudaMemcpyDeviceToHost));
         if (err[0]) {
-            // the failed launch and every launch after it stepped nothing: the
-            // state is the one the failed launch started from
             uint64_t t_fail = 0;
             memcpy(&t_fail, err + 2, sizeof(t_fail));
             FS3D_CUDA(cudaMemset(w->aux + kAuxErr, 0, sizeof(err)));
-            w->step = t_fail;
             w->counts_valid = false;
+            w->flags_ok = false;
+            if (w->tiled) {
+                // the per-step kernel stores each tile as it goes: the failed
+                // step left some tiles stepped and others not
+                w->broken = true;
+                return set_error(FS3D_ERR_TIMEOUT,
+                                 "a tile copy of the per-step kernel did not complete in time; the world holds a "
+                                 "partly stepped state and must be rewritten (fs3d_world_write)");
+            }
+            // the failed launch and every launch after it stepped nothing: the
+            // state is the one the failed launch started from
+            w->step = t_fail;
             return set_error(FS3D_ERR_TIMEOUT,
                              "a shared-memory bulk copy did not complete in time; the world was set back to the "
                              "step its state holds");
@@ -242,6 +290,7 @@ fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
 
 fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* out) {
     if (!w || !out) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_read: bad args");
+    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_read: the world must be rewritten (fs3d_world_write)");
     const size_t n = (size_t)w->cells();
     if (w->layout == FS3D_LAYOUT_BYTES) {
         FS3D_CUDA(cudaMemcpyAsync(out, w->bytes, n, cudaMemcpyDeviceToHost, w->stream));
@@ -262,11 +311,15 @@ fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* out) {
 fs3d_status fs3d_world_write(fs3d_world* w, const uint8_t* g) {
     if (!w || !g) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_write: bad args");
     w->counts_valid = false;
-    return upload(w, g);
+    w->flags_ok = false;
+    const fs3d_status s = upload(w, g);
+    if (s == FS3D_OK) w->broken = false;
+    return s;
 }
 
 fs3d_status fs3d_world_hash(fs3d_world* w, uint64_t* out) {
     if (!w || !out) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_hash: bad args");
+    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_hash: the world must be rewritten (fs3d_world_write)");
     fs3d_status s = (w->layout == FS3D_LAYOUT_BYTES)
                         ? hash_bytes_async(w->bytes, w->cells(), w->hash_dev, w->stream)
                         : planes_hash_async(w->rows, w->statics, w->X, w->Y, w->Z, w->hash_dev, w->stream);
@@ -361,6 +414,7 @@ fs3d_status fs3d_render(fs3d_world* w, const fs3d_camera* cam, int W, int H, int
                         int out_on_device) {
     if (!w || !cam || !rgba || W <= 0 || H <= 0 || (mode != FS3D_RENDER_DDA && mode != FS3D_RENDER_SDF_SPHERE))
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render: bad args");
+    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_render: the world must be rewritten (fs3d_world_write)");
     float* dst = rgba;
     const size_t bytes = (size_t)W * H * 4 * sizeof(float);
     if (mode == FS3D_RENDER_DDA && !w->brickmap)

@@ -87,30 +87,6 @@ def test_parity_odd_dims_all_paths(fs3d, orc, cuda, dims):
         w.close()
 
 
-def test_pillars_512_full_size(fs3d, orc, cuda):
-    """512^3 pillar world: the first steps against the threaded oracle, then
-    size-independent checks over 1000 steps (per-material mass, stone fixed,
-    byte kernel and plane kernel agree)."""
-    X = Y = Z = 512
-    g = fs3d.gen_pillars(1, X, Y, Z)
-    assert (g == orc.gen_c2(1, X, Y, Z)).all()
-    d = to_device(cuda, g)
-    st = stream_ptr(cuda)
-    ref = g.copy()
-    for t in range(3):
-        orc.step_omp(ref, 1, t, 0)
-        fs3d.step_device(d.data_ptr(), X, Y, Z, 1, t, 1, st)
-        assert fs3d.hash_device(d.data_ptr(), d.numel(), st) == orc.hash(ref), describe_diff(d.cpu().numpy(), ref, t)
-    with fs3d.World(ref, 1, 3, fs3d.LAYOUT_PLANES) as w:
-        fs3d.step_device(d.data_ptr(), X, Y, Z, 1, 3, 997, st)
-        w.step(997)
-        cuda.cuda.synchronize()
-        out = d.cpu().numpy()
-        assert w.hash() == fs3d.hash_device(d.data_ptr(), d.numel(), st)
-    assert (np.bincount(out.reshape(-1), minlength=4) == np.bincount(g.reshape(-1), minlength=4)).all()
-    assert ((out == 1) == (g == 1)).all()
-
-
 def test_hash_and_first_diff_device(fs3d, orc, cuda):
     rng = np.random.default_rng(5)
     for n in (1, 15, 16, 17, 1000, 4097, 1 << 20):
