@@ -146,6 +146,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def profile_values(name: str, keys):
+    """Named figures (`key: value` lines) from a summary under profiles/, or None."""
+    try:
+        txt = open(os.path.join(ROOT, "profiles", f"{name}.md")).read()
+    except OSError:
+        return None
+    out = {}
+    for k in keys:
+        m = re.search(rf"{k}:\s*([0-9.eE+]+)", txt)
+        if not m:
+            return None
+        out[k] = float(m.group(1))
+    return out
+
+
 def profile_traffic(kernel: str):
     """Per-launch DRAM bytes recorded from an ncu capture under profiles/."""
     path = os.path.join(ROOT, "profiles", f"{kernel}.md")
@@ -161,35 +176,68 @@ def profile_traffic(kernel: str):
 
 
 # ------------------------------------------------------------------ CPU leg: oracle timing and checks
-def cpu_sample(worlds, budget_s: float, threads: int):
-    """Times the oracle step on a bounded sample of the batch workload: worlds
-    are stepped concurrently (one thread each) until ~budget_s has passed."""
+def load_oracle():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    orc = oracle_lib.load()
-    import fallingsand3d_gb300 as fs3d
-    sample = worlds[: max(threads * 4, 64)]
-    grids = gen_grids(fs3d, sample)
-    cells = [g.size for g in grids]
-    steps_each = 4
+    return oracle_lib.load()
 
-    def run(i):
-        (X, Y, Z), seed = sample[i]
-        orc.L.orc_run(grids[i].ctypes.data, X, Y, Z, seed, 0, steps_each, None, 1)
-        return cells[i] * steps_each
 
-    done = 0
-    t0 = time.perf_counter()
+def oracle_worlds(orc, master: int, count: int):
+    """The batch's dims and seeds from the oracle's own generator."""
+    dims, seeds = orc.gen_c3_dims(master, count)
+    return [(tuple(int(v) for v in dims[w]), int(seeds[w])) for w in range(count)]
+
+
+def oracle_sample_index(count: int):
+    """The CPU legs' bounded sample: every 16th world of the batch."""
+    return list(range(0, count, 16))
+
+
+def run_parallel(fn, items, threads):
+    """fn over items on `threads` host threads (largest items first when they
+    are (grid, ...) tuples); the oracle releases the interpreter while it runs."""
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        rounds = 0
-        while True:
-            done += sum(ex.map(run, range(len(sample))))
-            rounds += 1
-            if time.perf_counter() - t0 > budget_s:
-                break
+        return list(ex.map(fn, items))
+
+
+def oracle_rate(orc, states, budget_s: float, threads: int, steps_each: int = 4):
+    """Times the oracle step on `states` ([grid, seed, step] each, stepped in
+    place from its own step counter) for about budget_s: a queue of worlds,
+    largest first; a thread takes a world, steps it steps_each steps and puts
+    it back, so no world is held by two threads and no thread waits for a
+    round to end.  Returns voxel-updates/s and a description."""
+    import queue
+    import threading
+    q = queue.Queue()
+    for i in sorted(range(len(states)), key=lambda i: -states[i][0].size):
+        q.put(i)
+    deadline = time.perf_counter() + budget_s
+    done = []
+
+    def worker():
+        n = 0
+        while time.perf_counter() < deadline:
+            i = q.get()
+            g, seed, t = states[i]
+            Y, Z, X = g.shape
+            orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, t, steps_each, None, 1)
+            states[i][2] = t + steps_each
+            n += g.size * steps_each
+            q.put(i)
+        done.append(n)
+
+    t0 = time.perf_counter()
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
     dt = time.perf_counter() - t0
-    return done / dt, {"worlds": len(sample), "steps_per_round": steps_each, "rounds": rounds,
-                       "voxel_updates": done, "seconds": round(dt, 3)}
+    return sum(done) / dt, {"worlds": len(states), "steps_per_take": steps_each, "voxel_updates": int(sum(done)),
+                            "seconds": round(dt, 3)}
+
+
+ORACLE_FLAGS = "gcc -O3 -fopenmp -ffp-contract=off (oracle/Makefile), one world per thread, work queue"
 
 
 class OracleChecks:
@@ -204,19 +252,26 @@ class OracleChecks:
     def add_run(self, label, grid, seed, t0, n, got):
         self.runs.setdefault(label, []).append((grid, seed, t0, n, got))
 
-    def check(self):
-        """Returns {"parity": str, "large": {...}, "mesh": {...}}."""
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
+    def check(self, threads):
+        """Returns {"parity": str, "large": {...}, "mesh": {...}}.  Every
+        recorded world is stepped by the oracle (one thread each, in
+        parallel) and compared whole."""
         import oracle_lib
-        orc = oracle_lib.load()
+        orc = load_oracle()
         out, notes = {}, []
+
+        def one(item):
+            grid, seed, t0, n, got = item
+            g = np.ascontiguousarray(grid).copy()
+            Y, Z, X = g.shape
+            orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, t0, n, None, 1)
+            return bool(np.array_equal(np.asarray(got), g))
+
         for label, items in self.runs.items():
-            ok = True
-            for grid, seed, t0, n, got in items:
-                g = grid.copy()
-                orc.run(g, seed, t0, n, nthreads=0)
-                ok &= bool((got == g).all())
-            notes.append(f"{len(items)} worlds of the {label} bit-exact" if ok else f"MISMATCH ({label})")
+            items = sorted(items, key=lambda it: -it[0].size)
+            ok = run_parallel(one, items, threads)
+            bad = len(ok) - sum(ok)
+            notes.append(f"{label}: {sum(ok)} of {len(ok)} worlds bit-exact" + (f" ({bad} MISMATCH)" if bad else ""))
         out["parity"] = "; ".join(notes) if notes else None
         if self.dda is not None:
             grid, cam, W, H, got, tol = self.dda
@@ -231,28 +286,55 @@ class OracleChecks:
 
 
 def run_reference(args):
+    """The reference arm: the upstream project has no step of its own, so the
+    CPU oracle (FS3D-rule v1) stands in, on the batch's worlds made by the
+    oracle's own generators.  `value` times the states the GPU arm's timed
+    segments step (every world advanced untimed to --timed-from first);
+    `value_fresh` the freshly generated worlds from step 0."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    import fallingsand3d_gb300 as fs3d
+    orc = load_oracle()
     threads = os.cpu_count() or 1
-    worlds = batch_worlds(fs3d, args.master, args.worlds)
-    vals = []
+    worlds = oracle_worlds(orc, args.master, args.worlds)
+    sample = [worlds[i] for i in oracle_sample_index(args.worlds)]
+
+    def gen(w):
+        (X, Y, Z), seed = w
+        return [orc.gen_c3_world(seed, X, Y, Z), seed, 0]
+
+    fresh = run_parallel(gen, sample, threads)
+    settled = [[g.copy(), seed, 0] for g, seed, _ in fresh]
+
+    def advance(st):
+        g, seed, _ = st
+        Y, Z, X = g.shape
+        orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, 0, args.timed_from, None, 1)
+        st[2] = args.timed_from
+
+    t0 = time.perf_counter()
+    run_parallel(advance, sorted(settled, key=lambda st: -st[0].size), threads)
+    advance_s = time.perf_counter() - t0
     for _ in range(args.warmup):
-        cpu_sample(worlds, 1.0, threads)
+        oracle_rate(orc, settled, 0.5, threads)
+    vals = []
     for _ in range(args.steps):
-        v, info = cpu_sample(worlds, args.cpu_budget / max(args.steps, 1), threads)
+        v, info = oracle_rate(orc, settled, args.cpu_budget / max(args.steps, 1), threads)
         vals.append(v)
     v = float(np.mean(vals))
+    vf, info_f = oracle_rate(orc, fresh, args.cpu_budget / 2, threads)
+    sample_txt = (f"{len(sample)} of the {args.worlds} worlds (every 16th), advanced untimed to step "
+                  f"{args.timed_from} ({advance_s:.1f} s), then stepped from there in 4-step takes for "
+                  f"{args.cpu_budget:g} s over {args.steps} timed steps; {ORACLE_FLAGS}")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"batched: {args.worlds} mixed worlds (bounded CPU sample)",
-                       "master_seed": args.master},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{info['worlds']} of the {args.worlds} worlds, {info['steps_per_round']} "
-                                       f"steps per round, one world per thread; the upstream project has no step "
-                                       f"of its own, so the CPU oracle (FS3D-rule v1) stands in"},
+            "config": {"workload": f"batched: {args.worlds} mixed worlds (bounded CPU sample), the states from "
+                                   f"step {args.timed_from} on, as the GPU arm's timed segments",
+                       "master_seed": args.master, "timed_from_step": args.timed_from},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_txt},
+            "value_fresh": {"value": vf, "unit": UNIT, "states": "the same worlds freshly generated, from step 0",
+                            "seconds": info_f["seconds"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -272,25 +354,39 @@ def run_fs3d(args):
     master = args.master + rank  # weak scaling: each rank steps its own 2048-world batch
     worlds = batch_worlds(fs3d, master, args.worlds)
     cells = int(sum(X * Y * Z for (X, Y, Z), _ in worlds))
+    shapes = [(Y, Z, X) for (X, Y, Z), _ in worlds]
     S = args.segment
+    threads = os.cpu_count() or 1
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    if args.timed_from % S:
+        raise SystemExit("--timed-from must be a multiple of --segment")
 
     # ---- headline: batched pool, device-resident
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
     # untimed: warm-up segments (at least five, so the worlds are past their
-    # first steps, the phase where everything still falls), then the
-    # launch configuration is chosen on real segments, then one more segment
+    # first steps, the phase where everything still falls), the launch
+    # configuration chosen on real segments, then plain segments up to step
+    # --timed-from, where the timed segments start (the reference arm steps
+    # the same states)
     pre = max(args.warmup, 5)
-    total_steps = S * (pre + 1 + args.steps + 1 + 32)
+    untimed = args.timed_from // S
+    total_steps = S * (untimed + args.steps + 1 + 32)
     tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
     bstream = torch.cuda.ExternalStream(b.stream())
     for _ in range(pre):
         b.run_segment()
     tune = b.autotune(trial_segments=1) if not args.no_autotune else {"segments": 0}
-    b.run_segment()
+    done_untimed = pre + tune["segments"]
+    if done_untimed > untimed:
+        raise SystemExit(f"warm-up and tuning took {done_untimed} segments, more than --timed-from allows")
+    for _ in range(untimed - done_untimed):
+        b.run_segment()
     b.sync()
-    untimed = pre + tune["segments"] + 1
+    checks = OracleChecks() if rank == 0 and not args.no_check else None
+    # the worlds' states before the last timed segment (read back untimed):
+    # the oracle checks that segment for every world
+    before = pinned_views(torch, shapes) if checks is not None else None
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -298,7 +394,11 @@ def run_fs3d(args):
     ctr0 = b.counters()
     launches0 = fs3d.kernel_launches()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for k in range(args.steps):
+            if before is not None and k == args.steps - 1:
+                launches_snap = fs3d.kernel_launches()
+                b.read_many(tickets, [v.data_ptr() for v in before])
+                launches0 += fs3d.kernel_launches() - launches_snap
             flush.fill_(1)  # L2 flush between timed segments (outside the events)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -319,18 +419,36 @@ def run_fs3d(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = cells * S * world / (ms / 1e3)
-    # the worlds as the timed segments left them, read back untimed: the e2e
-    # leg's inputs (the same world states), and a parity spot check of the
-    # timed run (three worlds, checked against the oracle in the CPU leg)
-    T0 = S * (untimed + args.steps)
-    steady = pinned_views(torch, [tuple(g.shape) for g in host])
+    T0 = S * (untimed + args.steps)  # the step the timed segments left the worlds at
+    steady = pinned_views(torch, shapes)
     b.sync()
     b.retire_many(tickets, [v.data_ptr() for v in steady])
     b.close()
-    checks = OracleChecks() if rank == 0 and not args.no_check else None
     if checks is not None:
-        for i in range(3):
-            checks.add_run("timed batch", host[i].numpy().copy(), worlds[i][1], 0, T0, steady[i].numpy().copy())
+        for i in range(len(worlds)):
+            checks.add_run("last timed segment", before[i].numpy(), worlds[i][1], T0 - S, S, steady[i].numpy())
+        for i in range(3):  # three worlds from their first step to the last
+            checks.add_run("timed batch from step 0", host[i].numpy(), worlds[i][1], 0, T0, steady[i].numpy())
+
+    # ---- fresh: the same worlds generated anew, one segment from step 0 (device-timed)
+    fresh_ms = []
+    for rep in range(3 + args.steps):
+        fb = fs3d.Batch(150 << 30, steps_per_segment=S)
+        fstream = torch.cuda.ExternalStream(fb.stream())
+        fts = [fb.admit_generated(X, Y, Z, seed, S) for (X, Y, Z), seed in worlds]
+        fb.sync()
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(fstream)
+        fb.run_segment()
+        e1.record(fstream)
+        e1.synchronize()
+        if rep >= 3:
+            fresh_ms.append(e0.elapsed_time(e1))
+        fb.retire_many(fts)
+        fb.close()
+    fresh_seg_ms = float(np.mean(fresh_ms))
 
     # ---- e2e through the C ABI from pinned host buffers
     # one step = admit every world from pinned host memory (H2D + conversion),
@@ -345,14 +463,11 @@ def run_fs3d(args):
     # last step's grids are in host memory.  e2e_fresh: the same with the
     # freshly generated worlds at step 0 (everything still falling).
     h2d, d2h = cells, cells
-    # two output arenas: the two pipelined batches below write their results
-    # into their own
-    outs2 = [pinned_views(torch, [tuple(g.shape) for g in host]) for _ in range(2)]
+    outs2 = [pinned_views(torch, shapes) for _ in range(2)]
     outs = outs2[0]
     seeds = np.array([seed for _, seed in worlds], dtype=np.uint64)
     dims_xyz = np.array([d for d, _ in worlds], dtype=np.int64)
     out_ptrs2 = [np.array([o.data_ptr() for o in ob], dtype=np.uint64) for ob in outs2]
-    out_ptrs = out_ptrs2[0]
 
     def e2e_run(inputs, start):
         """--e2e-batches batches take steps in turn (default 1; with 2, as a
@@ -396,40 +511,40 @@ def run_fs3d(args):
                 eb.close()
         return ms, float(np.mean(seq[2:]))
 
-    fresh_ms, fresh_seq = e2e_run(host, 0)
+    # every output of a round trip is its input stepped S steps (each e2e
+    # step admits the same inputs, so the arena holds that result): all
+    # worlds are checked against the oracle
+    fresh_e2e_ms, fresh_seq = e2e_run(host, 0)
     if checks is not None:
-        for i in (0, len(worlds) - 1):
-            checks.add_run("fresh e2e round trip", host[i].numpy().copy(), worlds[i][1], 0, S, outs[i].numpy().copy())
+        for i in range(len(worlds)):
+            checks.add_run("fresh e2e round trip", host[i].numpy(), worlds[i][1], 0, S, outs[i].numpy().copy())
     e2e_ms, seq_ms = e2e_run(steady, T0)
     if checks is not None:
-        # the round trip: each output is its input stepped S steps from T0
-        for i in (0, len(worlds) - 1):
-            checks.add_run("e2e round trip", steady[i].numpy().copy(), worlds[i][1], T0, S, outs[i].numpy().copy())
+        for i in range(len(worlds)):
+            checks.add_run("e2e round trip", steady[i].numpy(), worlds[i][1], T0, S, outs[i].numpy().copy())
     e2e_val = cells * S / (e2e_ms / 1e3)
 
-    # ---- plain per-world launches of the drop-in kernel (same worlds, device-resident)
+    # ---- plain per-world launches of the drop-in kernel: one launch per world
+    # per step from native code (fs3d_step_device_many), on the same states
+    # as the timed segments' (step T0), device-resident
     offs, off = [], 0
     for (X, Y, Z), _ in worlds:
         offs.append(off)
         off += (X * Y * Z + 255) // 256 * 256
     pool = torch.empty(off, dtype=torch.uint8, device=dev)
-    for o, g in zip(offs, host):
+    for o, g in zip(offs, steady):
         pool[o:o + g.numel()].copy_(g.reshape(-1), non_blocking=True)
     torch.cuda.synchronize()
     st = torch.cuda.current_stream(dev)
     sp = st.cuda_stream
-    base = pool.data_ptr()
-
-    def plain_segment(t0):
-        for s in range(S):
-            for o, ((X, Y, Z), seed) in zip(offs, worlds):
-                fs3d.lib().fs3d_step_device(base + o, X, Y, Z, seed, t0 + s, 1, sp)
-
-    plain_segment(0)
+    ptrs = [pool.data_ptr() + o for o in offs]
+    wseeds = [seed for _, seed in worlds]
+    wdims = [d for d, _ in worlds]
+    fs3d.step_device_many(ptrs, wdims, wseeds, T0, 2, sp)  # warm-up
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    plain_segment(S)
+    fs3d.step_device_many(ptrs, wdims, wseeds, T0 + 2, S, sp)
     e1.record(st)
     e1.synchronize()
     plain_ms = e0.elapsed_time(e1)
@@ -456,8 +571,14 @@ def run_fs3d(args):
         p512 = {"workload": "512^3 pillars, drop-in byte kernel, steps 8..1007 (1000 steps)", "us_per_step": round(t512 * 1e3, 2),
                 "voxel_updates_per_s": X * Y * Z / (t512 / 1e3), "algorithmic_gbs": round(gbs, 1),
                 "hbm_frac": round(gbs / hbm, 3), "peak_gbs": hbm, "peak_source": src,
-                "note": "134 MB grid read+written per step, in place (comparable to the 126 MB L2)"}
-        # same world through the plane layout (the batched kernel, one world)
+                "note": "134 MB grid read+written per step, in place (comparable to the 126 MB L2): the "
+                        "algorithmic figure counts 2 B per cell; dram_* are the DRAM bytes ncu measured"}
+        warm = profile_values("k_step_rows64_pillars512_warm", ("dram_bytes_per_launch", "duration_ns"))
+        if warm:
+            dram_gbs = warm["dram_bytes_per_launch"] / warm["duration_ns"]
+            p512.update({"dram_gbs": round(dram_gbs, 1), "dram_frac": round(dram_gbs / hbm, 3),
+                         "dram_source": "ncu, 3 warm launches at steps ~990 (profiles/k_step_rows64_pillars512_warm.md)"})
+        # same world through the plane layout (the tiled per-step kernel)
         with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
             w.step(8)
             ws = torch.cuda.ExternalStream(w.stream())
@@ -475,18 +596,35 @@ def run_fs3d(args):
     served = None
     if not args.skip_serve:
         served = {}
-        for lam in (500.0, 2000.0, 8000.0):
-            p = fs3d.serve_params(lam, args.serve_seconds, master_seed=args.master + 100)
+
+        def serve_one(lam, seconds, **kw):
+            p = fs3d.serve_params(lam, seconds, master_seed=args.master + 100, **kw)
             st_, reqs = fs3d.serve(p)
-            served[str(int(lam))] = {
-                "requests": st_["requests"], "completed": st_["completed"], "p50_ms": round(st_["p50_ms"], 3),
-                "p99_ms": round(st_["p99_ms"], 3), "max_ms": round(st_["max_ms"], 3),
-                "voxel_updates_per_s": st_["voxel_updates_per_s"],
-                "offered_voxel_updates_per_s": st_["offered_voxel_updates_per_s"],
-                "peak_live_worlds": st_["peak_live_worlds"], "segments": st_["segments"], "wall_s": round(st_["wall_s"], 3)}
-        served["config"] = (f"{args.serve_seconds:g} s of arrivals per rate; dims iid from {{16..128}}^3, n_steps "
-                            "log-uniform in [10, 1000], 150 GiB budget, 64-step segments; latency = arrival to "
-                            "hash visible on the host")
+            return {"requests": st_["requests"], "completed": st_["completed"], "p50_ms": round(st_["p50_ms"], 3),
+                    "p99_ms": round(st_["p99_ms"], 3), "max_ms": round(st_["max_ms"], 3),
+                    "voxel_updates_per_s": st_["voxel_updates_per_s"],
+                    "offered_voxel_updates_per_s": st_["offered_voxel_updates_per_s"],
+                    "served_fraction_of_offered": round(st_["voxel_updates_per_s"] /
+                                                        max(st_["offered_voxel_updates_per_s"], 1.0), 3),
+                    "peak_live_worlds": st_["peak_live_worlds"], "peak_bytes": st_["peak_bytes"],
+                    "segments": st_["segments"], "wall_s": round(st_["wall_s"], 3)}
+
+        for lam in (500.0, 2000.0, 8000.0):
+            served[str(int(lam))] = serve_one(lam, args.serve_seconds)
+        # past the headline rates, until the loop no longer keeps up: the
+        # served rate falls below the offered one and the latency grows
+        sweep = {}
+        for lam in (32000.0, 128000.0, 512000.0):
+            sweep[str(int(lam))] = serve_one(lam, args.serve_seconds / 2.5)
+        served["saturation"] = sweep
+        # a budget that binds: 64 MiB of pool for 8000 req/s (the 150 GiB pool
+        # holds about 300 000 of the largest requests, so at these request
+        # sizes it never binds)
+        served["budget_64MiB_8000"] = serve_one(8000.0, args.serve_seconds / 2.5, hbm_budget=64 << 20)
+        served["config"] = (f"{args.serve_seconds:g} s of arrivals per headline rate ({args.serve_seconds / 2.5:g} s "
+                            "for the saturation sweep and the tight budget); dims iid from {16..128}^3, n_steps "
+                            "log-uniform in [10, 1000], 150 GiB budget unless stated, 64-step segments; latency = "
+                            "arrival to hash visible on the host")
 
     # ---- large world + render: 1024^3 dunes, every step followed by a 1920x1080 DDA frame
     large = None
@@ -497,12 +635,12 @@ def run_fs3d(args):
     mesh = None if args.skip_large else run_mesh(fs3d, torch, args, checks)
 
     # ---- roofline of the dominant work: the segment graph, whose time is the
-    # resident kernels (one launch per size class steps its worlds 64 times in
-    # shared memory).  Algorithmic bytes = the 2-bit state read and written by
-    # every EVALUATED cell-step (0.5 B each; row pairs whose rows are settled are
-    # skipped exactly and counted in the dense-equivalent figures only), per
-    # segment with the events above; `traffic` = DRAM bytes per segment from the
-    # ncu capture in profiles/.
+    # resident kernels (one launch per size class steps its worlds 64 times).
+    # Algorithmic bytes = the 2-bit state read and written by every EVALUATED
+    # cell-step (0.5 B each; layer pairs whose rows are settled are skipped
+    # exactly and counted in the dense-equivalent figures only), per segment
+    # with the events above; `traffic` = DRAM bytes per segment from the ncu
+    # capture in profiles/.
     hbm, src = peaks()
     alg_bytes = 0.5 * cells * S * proc_frac
     achieved = alg_bytes / (ms / 1e3) / 1e9
@@ -519,17 +657,29 @@ def run_fs3d(args):
                         "exactly); the worlds stay in L2, so DRAM sees a few MB per segment; the kernels are "
                         "latency-bound: each world's steps are a serial chain (see profiles/)"}
 
-    # ---- CPU leg (rank 0): the oracle timed (N=1), then the recorded GPU results checked against it
+    # ---- CPU leg (rank 0): the oracle timed (N=1) on the same world states
+    # the GPU stepped, then the recorded GPU results checked against it
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        v, info = cpu_sample(worlds, args.cpu_budget, threads)
+        orc = load_oracle()
+        idx = oracle_sample_index(len(worlds))
+        if before is not None:
+            settled = [[before[i].numpy().copy(), worlds[i][1], T0 - S] for i in idx]
+            settled_txt = f"the states the last timed segment started from (step {T0 - S})"
+        else:
+            settled = [[steady[i].numpy().copy(), worlds[i][1], T0] for i in idx]
+            settled_txt = f"the states the timed segments left (step {T0})"
+        v, info = oracle_rate(orc, settled, args.cpu_budget, threads)
+        fresh_states = [[host[i].numpy().copy(), worlds[i][1], 0] for i in idx]
+        vf, info_f = oracle_rate(orc, fresh_states, args.cpu_budget / 2, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{info['worlds']} of the {args.worlds} worlds x {info['steps_per_round']} steps x "
-                         f"{info['rounds']} rounds, one world per thread ({info['seconds']} s)"}
+               "sample": f"{len(idx)} of the {args.worlds} worlds (every 16th), {settled_txt}, stepped in "
+                         f"4-step takes for {info['seconds']} s; {ORACLE_FLAGS}",
+               "fresh": {"value": vf, "unit": UNIT, "states": "the same worlds freshly generated, from step 0",
+                         "seconds": info_f["seconds"]}}
     parity = None
     if checks is not None:
-        res = checks.check()
+        res = checks.check(threads)
         parity = res["parity"]
         if large is not None and "large" in res:
             large.update(res["large"])
@@ -537,16 +687,18 @@ def run_fs3d(args):
             mesh.update(res["mesh"])
 
     if rank == 0:
+        fresh_value = cells * S / (fresh_seg_ms / 1e3)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "u8", "data": "synthetic",
                 "config": {"workload": f"batched: {args.worlds} worlds, dims iid from {{16,24,32,48,64,96,128}}^3, "
-                                       f"{S}-step CUDA-graph segments (one step = one segment)",
+                                       f"{S}-step CUDA-graph segments (one step = one segment), timed from step "
+                                       f"{args.timed_from}",
                            "worlds_per_gpu": args.worlds, "cells_per_gpu": cells, "steps_per_segment": S,
                            "master_seed": args.master, "l2": "flushed between timed segments (512 MB write)",
                            "layout": "2-bit planes", "parallelism": f"replicas x{world}",
                            "launch_config": {k: tune.get(k) for k in ("mode", "promote", "ctas_per_sm", "trials")},
-                           "untimed_segments": untimed},
+                           "timed_from_step": args.timed_from, "untimed_segments": untimed},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(e2e_ms, 2), "steps": args.e2e_steps,
@@ -559,18 +711,27 @@ def run_fs3d(args):
                         "sequential_ms": round(seq_ms, 2),
                         "sequential_path": "fs3d_batch_admit_many + fs3d_batch_run_segment + fs3d_batch_retire_many, "
                                            "each step waited for"},
-                "e2e_fresh": {"value": cells * S / (fresh_ms / 1e3), "unit": UNIT, "ms": round(fresh_ms, 2),
+                "value_fresh": {"value": fresh_value, "unit": UNIT, "ms_per_segment": round(fresh_seg_ms, 4),
+                                "states": "the same worlds freshly generated (device), one segment from step 0, "
+                                          "tables built inside the timed region; L2 flushed before each",
+                                "vs_cpu_fresh": round(fresh_value / cpu["fresh"]["value"], 1) if cpu else None},
+                "e2e_fresh": {"value": cells * S / (fresh_e2e_ms / 1e3), "unit": UNIT, "ms": round(fresh_e2e_ms, 2),
                               "sequential_ms": round(fresh_seq, 2),
                               "inputs": "the freshly generated worlds at step 0 (everything still falling), "
-                                        "same calls and pipelining"},
+                                        "same calls and pipelining",
+                              "vs_cpu_fresh": round(cells * S / (fresh_e2e_ms / 1e3) / cpu["fresh"]["value"], 1)
+                              if cpu else None},
                 "plain_per_world": {"value": plain_val, "unit": UNIT, "ms_per_segment": round(plain_ms, 2),
                                     "launches_per_segment": S * len(worlds),
+                                    "us_per_launch": round(plain_ms * 1e3 / (S * len(worlds)), 2),
+                                    "path": "fs3d_step_device_many: one launch of the drop-in kernel per world per "
+                                            "step from native code, the timed segments' world states",
                                     "speedup_batched_vs_plain": round(value / world / plain_val, 2)},
                 "processed": {"voxel_updates_per_s": value * proc_frac, "fraction_of_dense": round(proc_frac, 4),
                               "note": "value counts every cell of every world each step (dense-equivalent); "
                                       "this counts the cell-steps the kernels evaluated"},
                 "plain_512": p512, "served": served, "large_render": large, "mesh_render": mesh, "parity": parity,
-                "segment_ms": [round(x, 4) for x in seg_ms]}
+                "segment_ms": [round(x, 4) for x in seg_ms], "fresh_segment_ms": [round(x, 4) for x in fresh_ms]}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -764,6 +925,8 @@ def main():
     ap.add_argument("--worlds", type=int, default=2048)
     ap.add_argument("--master", type=int, default=1)
     ap.add_argument("--segment", type=int, default=64)
+    ap.add_argument("--timed-from", type=int, default=640,
+                    help="step at which the timed segments start (both arms step the states from there)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")

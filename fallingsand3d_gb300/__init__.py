@@ -38,12 +38,13 @@ ERR_IO = -9
 # every entry point of include/fs3d.h (checked by the tests)
 EXPORTS = (
     "fs3d_abi_version", "fs3d_status_string", "fs3d_last_error", "fs3d_kernel_launch_count",
-    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_simple", "fs3d_run_device",
+    "fs3d_default_config", "fs3d_step_device", "fs3d_step_device_many", "fs3d_step_device_simple", "fs3d_run_device",
     "fs3d_run_device_noalloc", "fs3d_run_device_check", "fs3d_hash_device", "fs3d_first_diff_device",
     "fs3d_world_create", "fs3d_world_step", "fs3d_world_sync", "fs3d_world_read", "fs3d_world_write",
     "fs3d_world_hash", "fs3d_world_info", "fs3d_world_device_ptr", "fs3d_world_stream",
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
     "fs3d_batch_retire_many", "fs3d_batch_admit_many_async", "fs3d_batch_retire_many_async", "fs3d_batch_wait_copies",
+    "fs3d_batch_read_many",
     "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
@@ -137,6 +138,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_default_config": (Config, []),
         "fs3d_step_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_step_device_simple": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
+        "fs3d_step_device_many": (S, [i32, C.POINTER(vp), vp, vp, u64, i32, vp]),
         "fs3d_run_device": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_run_device_noalloc": (S, [vp, i32, i32, i32, u64, u64, i32, vp]),
         "fs3d_run_device_check": (S, [vp, i64]),
@@ -164,6 +166,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_admit_many_async": (S, [vp, i32, C.POINTER(WorldSpec), C.POINTER(u64), C.POINTER(i32)]),
         "fs3d_batch_retire_many_async": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
         "fs3d_batch_wait_copies": (S, [vp, i64]),
+        "fs3d_batch_read_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
         "fs3d_batch_run_segment": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
@@ -324,6 +327,16 @@ def render_meshes_device(view: ObjectView, draws, W: int, H: int, rgba_ptr: int,
 def step_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
     """Drop-in step of a device grid (pointer) in place; async on `stream`."""
     check(lib().fs3d_step_device(grid_ptr, X, Y, Z, seed, t0, n_steps, stream))
+
+
+def step_device_many(grid_ptrs, dims, seeds, t0: int, n_steps: int, stream: int = 0) -> None:
+    """The drop-in kernel launched once per world per step from native code
+    (device grids at grid_ptrs, dims an n x 3 array of X, Y, Z)."""
+    n = len(grid_ptrs)
+    ptrs = np.asarray(grid_ptrs if n else [0], dtype=np.uint64)
+    d = np.ascontiguousarray(np.asarray(dims if n else [[1, 1, 1]], dtype=np.int32).reshape(-1, 3))
+    sd = np.asarray(seeds if n else [0], dtype=np.uint64)
+    check(lib().fs3d_step_device_many(n, ptrs.ctypes.data_as(C.POINTER(vp)), _ptr(d), _ptr(sd), t0, n_steps, stream))
 
 
 def run_device(grid_ptr: int, X: int, Y: int, Z: int, seed: int, t0: int, n_steps: int, stream: int = 0) -> None:
@@ -557,6 +570,15 @@ class Batch:
             outs = outs_arr.ctypes.data_as(C.POINTER(vp))
         fn = lib().fs3d_batch_retire_many if wait else lib().fs3d_batch_retire_many_async
         check(fn(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)), outs))
+
+    def read_many(self, tickets, out_ptrs) -> None:
+        """Reads live worlds back into out_ptrs (host or device buffers) without
+        retiring them; returns once the grids are there."""
+        n = len(tickets)
+        ts = np.asarray(tickets if n else [0], dtype=np.uint64)
+        outs = np.asarray([p or 0 for p in out_ptrs] if n else [0], dtype=np.uint64)
+        check(lib().fs3d_batch_read_many(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)),
+                                         outs.ctypes.data_as(C.POINTER(vp))))
 
     def wait_copies(self, timeout_ns: int = -1) -> None:
         """Waits for every admission upload and read-back enqueued so far."""

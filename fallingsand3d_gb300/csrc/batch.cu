@@ -1183,8 +1183,11 @@ std::shared_ptr<CUevent_st> record_read(cudaStream_t rb) {
 
 // Retires tickets[0..n): the read-backs (conversion + copy into grids_out[a]
 // where given) run on the read-back stream after each world's last segment;
-// with `wait` it returns once the outputs hold the grids.
-fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out, bool wait) {
+// with `wait` it returns once the outputs hold the grids.  With `keep` the
+// worlds stay in the batch (a snapshot of their current state): the next
+// segment waits for the read-back's conversion.
+fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out, bool wait,
+                             bool keep = false) {
     if (!b || n < 0 || (n > 0 && !tickets)) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_retire_many: bad args");
     std::vector<std::map<uint64_t, BWorld>::iterator> its;
     its.reserve((size_t)n);
@@ -1394,10 +1397,23 @@ fs3d_status retire_many_impl(fs3d_batch* b, int n, const uint64_t* tickets, uint
     } else if (table) {
         cudaFreeAsync(table, rb);
     }
+    for (PendingAdmit* pa : readers) pa->reader = read;
+    if (keep) {
+        // the worlds stay: later segments must not change their planes before
+        // the conversion has read them
+        if (s == FS3D_OK) {
+            const cudaError_t e = read ? cudaStreamWaitEvent(b->stream, read.get(), 0) : cudaStreamSynchronize(rb);
+            if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_read_many ordering");
+        }
+        if (wait && s == FS3D_OK) {
+            FS3D_CUDA(cudaStreamSynchronize(rb));
+            FS3D_CUDA(cudaStreamSynchronize(b->download));
+        }
+        return s;
+    }
     // the worlds' memory goes back once the conversion has read it
     fs3d_batch::DeferredFree d;
     d.after = read;
-    for (PendingAdmit* pa : readers) pa->reader = read;
     for (auto it : its) {
         BWorld& w = it->second;
         b->used -= w.bytes;
@@ -1446,6 +1462,11 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
 
 fs3d_status fs3d_batch_retire_many_async(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
     return retire_many_impl(b, n, tickets, grids_out, false);
+}
+
+fs3d_status fs3d_batch_read_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out) {
+    if (!grids_out) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_read_many: NULL outputs");
+    return retire_many_impl(b, n, tickets, grids_out, true, true);
 }
 
 fs3d_status fs3d_batch_wait_copies(fs3d_batch* b, int64_t timeout_ns) {

@@ -436,6 +436,25 @@ fs3d_status fs3d_step_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t se
     return launch_step_bytes(grid_dev, X, Y, Z, seed, t0, n_steps, (cudaStream_t)stream);
 }
 
+fs3d_status fs3d_step_device_many(int n, uint8_t* const* grids_dev, const int* dims, const uint64_t* seeds,
+                                  uint64_t t0, int n_steps, void* stream) {
+    if (n < 0 || n_steps < 0 || (n > 0 && (!grids_dev || !dims || !seeds)))
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_step_device_many: bad args");
+    for (int w = 0; w < n; ++w)
+        if (!grids_dev[w] || !dims_valid(dims[3 * w], dims[3 * w + 1], dims[3 * w + 2]))
+            return set_error(FS3D_ERR_INVALID_ARG, "fs3d_step_device_many: null grid or bad dims");
+    // step-major, one launch per world per step: every world takes step t
+    // before any takes step t + 1, as separate callers stepping their own
+    // worlds would
+    for (int a = 0; a < n_steps; ++a)
+        for (int w = 0; w < n; ++w) {
+            const fs3d_status s = launch_step_bytes(grids_dev[w], dims[3 * w], dims[3 * w + 1], dims[3 * w + 2],
+                                                    seeds[w], t0 + (uint64_t)a, 1, (cudaStream_t)stream);
+            if (s != FS3D_OK) return s;
+        }
+    return FS3D_OK;
+}
+
 fs3d_status fs3d_step_device_simple(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
                                     int n_steps, void* stream) {
     if (!grid_dev || !dims_valid(X, Y, Z) || n_steps < 0)

@@ -103,6 +103,13 @@ fs3d_config fs3d_default_config(void);
  * legacy default stream).  No device memory is allocated. */
 fs3d_status fs3d_step_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
                              int n_steps, void* stream);
+/* fs3d_step_device for n separate worlds, called from native code: for each
+ * of n_steps steps, one launch of the drop-in kernel per world (worlds i with
+ * dims[3i..3i+2] = X, Y, Z and seed seeds[i], all at step t0 + step).  The
+ * plain per-world baseline the batched pool is measured against.  No
+ * counterpart in the upstream project. */
+fs3d_status fs3d_step_device_many(int n, uint8_t* const* grids_dev, const int* dims, const uint64_t* seeds,
+                                  uint64_t t0, int n_steps, void* stream);
 /* Same contract as fs3d_step_device, through the bit-plane kernels: the grid is
  * converted into 2-bit planes held in device scratch taken from the
  * stream-ordered pool (about X*Y*Z/4 bytes, freed on `stream` when done), the
@@ -214,6 +221,11 @@ fs3d_status fs3d_batch_retire_many(fs3d_batch* b, int n, const uint64_t* tickets
  * each world's last segment (downloads overlap later segments); grids_out
  * holds the grids once fs3d_batch_wait_copies returns. */
 fs3d_status fs3d_batch_retire_many_async(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
+/* Reads n live worlds back without retiring them (a snapshot of their state
+ * after the segments enqueued so far; the grids are in grids_out when the call
+ * returns; a NULL entry skips that world).  The worlds keep running: the next
+ * segment waits for the read-back.  No counterpart in the upstream project. */
+fs3d_status fs3d_batch_read_many(fs3d_batch* b, int n, const uint64_t* tickets, uint8_t* const* grids_out);
 /* Waits (timeout_ns < 0: without limit) until every admission and read-back
  * enqueued so far has run. */
 fs3d_status fs3d_batch_wait_copies(fs3d_batch* b, int64_t timeout_ns);

@@ -604,3 +604,23 @@ def test_back_to_back_async_retires_into_scattered_pinned_outputs(fs3d, orc, cud
     for worlds, o in zip(groups, outs):
         for (dims, seed), t in zip(worlds, o):
             assert (t.numpy() == oracle_final(orc, fs3d, dims, seed, S)).all(), dims
+
+
+def test_read_many_snapshots_live_worlds(fs3d, orc, cuda):
+    """read_many returns the worlds' state after the segments enqueued so far
+    and leaves them running: the next segment continues from there."""
+    S = 32
+    worlds = small_batch(fs3d, 61, 9, max_dim=96)
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        ts = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, 3 * S) for dims, seed in worlds]
+        b.run_segment()
+        b.run_segment()
+        snap = [cuda.zeros((Y, Z, X), dtype=cuda.uint8).pin_memory() for (X, Y, Z), _ in worlds]
+        b.read_many(ts, [t.data_ptr() for t in snap])
+        b.run_segment()  # must not touch the planes before the read-back has them
+        assert b.stats()["live_worlds"] == len(worlds)
+        outs = [np.zeros((Y, Z, X), dtype=np.uint8) for (X, Y, Z), _ in worlds]
+        b.retire_many(ts, [o.ctypes.data for o in outs])
+    for (dims, seed), sn, o in zip(worlds, snap, outs):
+        assert (sn.numpy() == oracle_final(orc, fs3d, dims, seed, 2 * S)).all(), dims
+        assert (o == oracle_final(orc, fs3d, dims, seed, 3 * S)).all(), dims

@@ -149,3 +149,19 @@ def test_run_device_matches_oracle(fs3d, orc, cuda, dims):
     cuda.cuda.synchronize()
     out = d.cpu().numpy()
     assert (out == ref).all(), describe_diff(out, ref, 32)
+
+
+def test_step_device_many_native_launch_loop(fs3d, orc, cuda):
+    """One launch per world per step from native code: each world equals the
+    oracle."""
+    dims = [(24, 40, 33), (64, 64, 64), (128, 30, 17), (48, 16, 96)]
+    grids = [mixed_grid(X, Y, Z, 100 + i) for i, (X, Y, Z) in enumerate(dims)]
+    devs = [to_device(cuda, g) for g in grids]
+    seeds = [7 + i for i in range(len(dims))]
+    fs3d.step_device_many([d.data_ptr() for d in devs], dims, seeds, 4, 15, stream_ptr(cuda))
+    cuda.cuda.synchronize()
+    for g, d, s in zip(grids, devs, seeds):
+        ref = g.copy()
+        orc.run(ref, s, 4, 15, nthreads=0)
+        got = d.cpu().numpy()
+        assert (got == ref).all(), describe_diff(got, ref, 18)
