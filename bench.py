@@ -200,17 +200,20 @@ def run_parallel(fn, items, threads):
         return list(ex.map(fn, items))
 
 
-def oracle_rate(orc, states, budget_s: float, threads: int, steps_each: int = 4):
-    """Times the oracle step on `states` ([grid, seed, step] each, stepped in
-    place from its own step counter) for about budget_s: a queue of worlds,
-    largest first; a thread takes a world, steps it steps_each steps and puts
-    it back, so no world is held by two threads and no thread waits for a
-    round to end.  Returns voxel-updates/s and a description."""
+def oracle_rate(orc, states, budget_s: float, threads: int, steps_each: int = 4, window: int = 64):
+    """Times the oracle step on `states` ([grid, seed, step] each) for about
+    budget_s: a queue of worlds, largest first; a thread takes a world, steps
+    a working copy steps_each steps from where it stands and puts it back, so
+    no world is held by two threads and no thread waits for a round to end.
+    Every `window` steps a world starts over from its given state, so the
+    timed work is the given states' next `window` steps (one segment), as the
+    GPU times it.  Returns voxel-updates/s and a description."""
     import queue
     import threading
     q = queue.Queue()
     for i in sorted(range(len(states)), key=lambda i: -states[i][0].size):
         q.put(i)
+    work = [[np.ascontiguousarray(g).copy(), 0] for g, _, _ in states]
     deadline = time.perf_counter() + budget_s
     done = []
 
@@ -218,11 +221,15 @@ def oracle_rate(orc, states, budget_s: float, threads: int, steps_each: int = 4)
         n = 0
         while time.perf_counter() < deadline:
             i = q.get()
-            g, seed, t = states[i]
-            Y, Z, X = g.shape
-            orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, t, steps_each, None, 1)
-            states[i][2] = t + steps_each
-            n += g.size * steps_each
+            g0, seed, t0 = states[i]
+            cur, k = work[i]
+            if k >= window:
+                np.copyto(cur, g0)
+                k = 0
+            Y, Z, X = cur.shape
+            orc.L.orc_run(cur.ctypes.data, X, Y, Z, seed, t0 + k, steps_each, None, 1)
+            work[i][1] = k + steps_each
+            n += cur.size * steps_each
             q.put(i)
         done.append(n)
 
@@ -233,8 +240,8 @@ def oracle_rate(orc, states, budget_s: float, threads: int, steps_each: int = 4)
     for t in ts:
         t.join()
     dt = time.perf_counter() - t0
-    return sum(done) / dt, {"worlds": len(states), "steps_per_take": steps_each, "voxel_updates": int(sum(done)),
-                            "seconds": round(dt, 3)}
+    return sum(done) / dt, {"worlds": len(states), "steps_per_take": steps_each, "window": window,
+                            "voxel_updates": int(sum(done)), "seconds": round(dt, 3)}
 
 
 ORACLE_FLAGS = "gcc -O3 -fopenmp -ffp-contract=off (oracle/Makefile), one world per thread, work queue"
@@ -316,16 +323,16 @@ def run_reference(args):
     run_parallel(advance, sorted(settled, key=lambda st: -st[0].size), threads)
     advance_s = time.perf_counter() - t0
     for _ in range(args.warmup):
-        oracle_rate(orc, settled, 0.5, threads)
+        oracle_rate(orc, settled, 0.5, threads, window=args.segment)
     vals = []
     for _ in range(args.steps):
-        v, info = oracle_rate(orc, settled, args.cpu_budget / max(args.steps, 1), threads)
+        v, info = oracle_rate(orc, settled, args.cpu_budget / max(args.steps, 1), threads, window=args.segment)
         vals.append(v)
     v = float(np.mean(vals))
-    vf, info_f = oracle_rate(orc, fresh, args.cpu_budget / 2, threads)
+    vf, info_f = oracle_rate(orc, fresh, args.cpu_budget / 2, threads, window=args.segment)
     sample_txt = (f"{len(sample)} of the {args.worlds} worlds (every 16th), advanced untimed to step "
-                  f"{args.timed_from} ({advance_s:.1f} s), then stepped from there in 4-step takes for "
-                  f"{args.cpu_budget:g} s over {args.steps} timed steps; {ORACLE_FLAGS}")
+                  f"{args.timed_from} ({advance_s:.1f} s), then their next {args.segment} steps, over and over, "
+                  f"in 4-step takes for {args.cpu_budget:g} s over {args.steps} timed steps; {ORACLE_FLAGS}")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
@@ -333,7 +340,8 @@ def run_reference(args):
                                    f"step {args.timed_from} on, as the GPU arm's timed segments",
                        "master_seed": args.master, "timed_from_step": args.timed_from},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_txt},
-            "value_fresh": {"value": vf, "unit": UNIT, "states": "the same worlds freshly generated, from step 0",
+            "value_fresh": {"value": vf, "unit": UNIT,
+                            "states": f"the same worlds freshly generated, their first {args.segment} steps",
                             "seconds": info_f["seconds"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -351,7 +359,8 @@ def run_fs3d(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    master = args.master + rank  # weak scaling: each rank steps its own 2048-world batch
+    from fallingsand3d_gb300 import sharding
+    master = sharding.weak_master(args.master, rank)  # weak scaling: each rank steps its own 2048-world batch
     worlds = batch_worlds(fs3d, master, args.worlds)
     cells = int(sum(X * Y * Z for (X, Y, Z), _ in worlds))
     shapes = [(Y, Z, X) for (X, Y, Z), _ in worlds]
@@ -491,34 +500,43 @@ def run_fs3d(args):
                 eb.retire_many(ts, out_ptrs2[it % nb])
                 seq.append((time.perf_counter() - t0) * 1e3)
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            host = {"admit_many_async": 0.0, "retire_many_async": 0.0, "run_segment": 0.0}
+            pc = time.perf_counter
+            t0 = pc()
             prev = [None] * nb
             for it in range(args.e2e_steps):
                 k = it % nb
+                a = pc()
                 ts = ebs[k].admit_many(None, seeds, S, start_steps=starts, ptrs=in_ptrs, dims=dims_xyz, wait=False)
+                b_ = pc()
                 if prev[k] is not None:
                     ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
+                c = pc()
                 ebs[k].run_segment()
+                host["admit_many_async"] += b_ - a
+                host["retire_many_async"] += c - b_
+                host["run_segment"] += pc() - c
                 prev[k] = ts
             for k in range(nb):
                 if prev[k] is not None:
                     ebs[k].retire_many(prev[k], out_ptrs2[k], wait=False)
             for eb in ebs:
                 eb.wait_copies()
-            ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+            ms = (pc() - t0) * 1e3 / args.e2e_steps
         finally:
             for eb in ebs:
                 eb.close()
-        return ms, float(np.mean(seq[2:]))
+        host_ms = {k: round(v * 1e3 / args.e2e_steps, 3) for k, v in host.items()}
+        return ms, float(np.mean(seq[2:])), host_ms
 
     # every output of a round trip is its input stepped S steps (each e2e
     # step admits the same inputs, so the arena holds that result): all
     # worlds are checked against the oracle
-    fresh_e2e_ms, fresh_seq = e2e_run(host, 0)
+    fresh_e2e_ms, fresh_seq, fresh_host_ms = e2e_run(host, 0)
     if checks is not None:
         for i in range(len(worlds)):
             checks.add_run("fresh e2e round trip", host[i].numpy(), worlds[i][1], 0, S, outs[i].numpy().copy())
-    e2e_ms, seq_ms = e2e_run(steady, T0)
+    e2e_ms, seq_ms, e2e_host_ms = e2e_run(steady, T0)
     if checks is not None:
         for i in range(len(worlds)):
             checks.add_run("e2e round trip", steady[i].numpy(), worlds[i][1], T0, S, outs[i].numpy().copy())
@@ -578,7 +596,7 @@ def run_fs3d(args):
             dram_gbs = warm["dram_bytes_per_launch"] / warm["duration_ns"]
             p512.update({"dram_gbs": round(dram_gbs, 1), "dram_frac": round(dram_gbs / hbm, 3),
                          "dram_source": "ncu, 3 warm launches at steps ~990 (profiles/k_step_rows64_pillars512_warm.md)"})
-        # same world through the plane layout (the tiled per-step kernel)
+        # same world through the plane layout (the per-step kernel that skips settled row-pairs)
         with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
             w.step(8)
             ws = torch.cuda.ExternalStream(w.stream())
@@ -614,15 +632,16 @@ def run_fs3d(args):
         # past the headline rates, until the loop no longer keeps up: the
         # served rate falls below the offered one and the latency grows
         sweep = {}
-        for lam in (32000.0, 128000.0, 512000.0):
-            sweep[str(int(lam))] = serve_one(lam, args.serve_seconds / 2.5)
+        for lam in (16000.0, 32000.0, 64000.0):
+            sweep[str(int(lam))] = serve_one(lam, args.serve_seconds / 5)
         served["saturation"] = sweep
         # a budget that binds: 64 MiB of pool for 8000 req/s (the 150 GiB pool
         # holds about 300 000 of the largest requests, so at these request
         # sizes it never binds)
         served["budget_64MiB_8000"] = serve_one(8000.0, args.serve_seconds / 2.5, hbm_budget=64 << 20)
-        served["config"] = (f"{args.serve_seconds:g} s of arrivals per headline rate ({args.serve_seconds / 2.5:g} s "
-                            "for the saturation sweep and the tight budget); dims iid from {16..128}^3, n_steps "
+        served["config"] = (f"{args.serve_seconds:g} s of arrivals per headline rate ({args.serve_seconds / 5:g} s "
+                            f"for the saturation sweep, {args.serve_seconds / 2.5:g} s for the tight budget); dims iid "
+                            "from {16..128}^3, n_steps "
                             "log-uniform in [10, 1000], 150 GiB budget unless stated, 64-step segments; latency = "
                             "arrival to hash visible on the host")
 
@@ -669,13 +688,14 @@ def run_fs3d(args):
         else:
             settled = [[steady[i].numpy().copy(), worlds[i][1], T0] for i in idx]
             settled_txt = f"the states the timed segments left (step {T0})"
-        v, info = oracle_rate(orc, settled, args.cpu_budget, threads)
+        v, info = oracle_rate(orc, settled, args.cpu_budget, threads, window=S)
         fresh_states = [[host[i].numpy().copy(), worlds[i][1], 0] for i in idx]
-        vf, info_f = oracle_rate(orc, fresh_states, args.cpu_budget / 2, threads)
+        vf, info_f = oracle_rate(orc, fresh_states, args.cpu_budget / 2, threads, window=S)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{len(idx)} of the {args.worlds} worlds (every 16th), {settled_txt}, stepped in "
-                         f"4-step takes for {info['seconds']} s; {ORACLE_FLAGS}",
-               "fresh": {"value": vf, "unit": UNIT, "states": "the same worlds freshly generated, from step 0",
+               "sample": f"{len(idx)} of the {args.worlds} worlds (every 16th), {settled_txt}, their next {S} "
+                         f"steps over and over in 4-step takes for {info['seconds']} s; {ORACLE_FLAGS}",
+               "fresh": {"value": vf, "unit": UNIT,
+                         "states": f"the same worlds freshly generated, their first {S} steps over and over",
                          "seconds": info_f["seconds"]}}
     parity = None
     if checks is not None:
@@ -710,13 +730,14 @@ def run_fs3d(args):
                         "batches": max(1, min(2, args.e2e_batches)),
                         "sequential_ms": round(seq_ms, 2),
                         "sequential_path": "fs3d_batch_admit_many + fs3d_batch_run_segment + fs3d_batch_retire_many, "
-                                           "each step waited for"},
+                                           "each step waited for",
+                        "host_ms_per_step": e2e_host_ms},
                 "value_fresh": {"value": fresh_value, "unit": UNIT, "ms_per_segment": round(fresh_seg_ms, 4),
                                 "states": "the same worlds freshly generated (device), one segment from step 0, "
                                           "tables built inside the timed region; L2 flushed before each",
                                 "vs_cpu_fresh": round(fresh_value / cpu["fresh"]["value"], 1) if cpu else None},
                 "e2e_fresh": {"value": cells * S / (fresh_e2e_ms / 1e3), "unit": UNIT, "ms": round(fresh_e2e_ms, 2),
-                              "sequential_ms": round(fresh_seq, 2),
+                              "sequential_ms": round(fresh_seq, 2), "host_ms_per_step": fresh_host_ms,
                               "inputs": "the freshly generated worlds at step 0 (everything still falling), "
                                         "same calls and pipelining",
                               "vs_cpu_fresh": round(cells * S / (fresh_e2e_ms / 1e3) / cpu["fresh"]["value"], 1)
@@ -868,15 +889,46 @@ def run_only(args):
                 eb.run_segment()
                 eb.retire_many(t, outp)
             prev = None
+            pc = time.perf_counter
+            host = [0.0, 0.0, 0.0]
+            torch.cuda.synchronize()
+            t0 = pc()
             for _ in range(args.e2e_steps):
+                a = pc()
                 t = eb.admit_many(None, seeds, S, start_steps=starts, ptrs=inp, dims=dims, wait=False)
+                b_ = pc()
                 if prev is not None:
                     eb.retire_many(prev, outp, wait=False)
+                c = pc()
                 eb.run_segment()
+                host[0] += b_ - a
+                host[1] += c - b_
+                host[2] += pc() - c
                 prev = t
             eb.retire_many(prev, outp, wait=False)
             eb.wait_copies()
-        print(json.dumps({"only": args.only, "ok": True}))
+            ms = (pc() - t0) * 1e3 / args.e2e_steps
+        n = args.e2e_steps
+        print(json.dumps({"only": args.only, "ok": True, "ms_per_step": round(ms, 3),
+                          "host_ms_per_step": {"admit_many_async": round(host[0] * 1e3 / n, 3),
+                                               "retire_many_async": round(host[1] * 1e3 / n, 3),
+                                               "run_segment": round(host[2] * 1e3 / n, 3)}}))
+        return 0
+    if args.only == "dunes":
+        # the 1024^3 dune world stepped alone (no frames): per-step times over the run
+        g = fs3d.gen_dunes(1, 1024, 1024, 1024)
+        with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
+            ws = torch.cuda.ExternalStream(w.stream())
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.large_steps + 1)]
+            ev[0].record(ws)
+            for s in range(args.large_steps):
+                w.step(1)
+                ev[s + 1].record(ws)
+            ev[-1].synchronize()
+            us = [ev[s].elapsed_time(ev[s + 1]) * 1e3 for s in range(args.large_steps)]
+        marks = {str(a): round(float(np.mean(us[a:a + 10])), 1) for a in range(0, args.large_steps, 50)}
+        print(json.dumps({"only": args.only, "ok": True, "mean_step_us": round(float(np.mean(us)), 2),
+                          "step_us_by_step": marks}))
         return 0
     if args.only == "large":
         out = run_large(fs3d, torch, torch.device("cuda", 0), args)
@@ -935,7 +987,7 @@ def main():
     ap.add_argument("--skip-large", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--large-steps", type=int, default=500)
-    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "plain512p", "large", "mesh", "e2e", "fresh"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "plain512", "plain512p", "large", "dunes", "mesh", "e2e", "fresh"],
                     help="run one workload alone (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -21,7 +21,6 @@
 #include <cooperative_groups.h>
 #include <stdint.h>
 
-#include <atomic>
 #include <mutex>
 
 #include "fs3d_common.h"
@@ -326,6 +325,82 @@ __global__ void __launch_bounds__(256) k_plane_step(const PlaneWorld* __restrict
         const int rp = item.rp0 + (lane >> w.lg);
         const int nrp = nblocks(w.Y, o) * nblocks(w.Z, o);
         plane_rowpair(w, o, stepkey(w.seed, t), rp, rp < nrp, gl, G, item.world == 0 ? counts : nullptr);
+    }
+}
+
+// One step of one large world (too large for the resident kernels), skipping
+// settled row-pairs exactly.  Per row (y, z) one byte holds the low 8 bits of
+// the last step that changed the row.  A block row-pair of phase o at step t
+// is evaluated when one of its four rows changed at step t-1 or t-2 (age
+// (t - flag) & 255 of 1 or 2; an older change that aliases to those ages only
+// adds work).  Otherwise its cells are those it had when last evaluated (at
+// t-2, same phase), which changed nothing, and whether a block can change
+// depends on its own cells alone, so it would change nothing again.  Each
+// row belongs to one row-pair per step, so the row-pair reads and writes its
+// rows' bytes with no other reader in the step.  A fresh world starts with
+// every byte at t0 - 1 (every row changed just before).  Warps take
+// (32 >> lg) row-pairs each in order; a warp whose row-pairs are all settled
+// loads nothing.
+__device__ __forceinline__ bool rows_changed_recently(const uint8_t* __restrict__ rf, int Y, int Z, int y0, int z0,
+                                                      uint32_t tb) {
+    bool d = false;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int y = y0 + (a >> 1), z = z0 + (a & 1);
+        if (y >= 0 && y < Y && z >= 0 && z < Z) d |= ((tb - (uint32_t)rf[(int64_t)y * Z + z]) & 0xFFu) - 1u < 2u;
+    }
+    return d;
+}
+
+__global__ void __launch_bounds__(256) k_plane_step_skip(const PlaneWorld w, uint8_t* __restrict__ rflags,
+                                                        int* counts) {
+    const uint64_t t = w.t;
+    const int o = (int)(t & 1u);
+    const int lane = threadIdx.x & 31;
+    const int G = 1 << w.lg, per = 32 >> w.lg, gl = lane & (G - 1);
+    const int NBZ = nblocks(w.Z, o), nrp = nblocks(w.Y, o) * NBZ, n_items = (nrp + per - 1) / per;
+    const uint32_t sk = stepkey(w.seed, t), tb = (uint32_t)t & 0xFFu;
+    const uint32_t gmask = G == 32 ? 0xFFFFFFFFu : ((1u << G) - 1u) << (lane & ~(G - 1));
+    const bool half_at_end = (w.X & 63) == 0;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += warps) {
+        const int rp = it * per + (lane >> w.lg);
+        const bool valid = rp < nrp;
+        const int j = valid ? rp / NBZ : 0, k = valid ? rp - j * NBZ : 0;
+        const int y0 = 2 * j - o, z0 = 2 * k - o;
+        bool dirty = false;
+        if (valid && gl == 0) dirty = rows_changed_recently(rflags, w.Y, w.Z, y0, z0, tb);
+        dirty = __shfl_sync(0xFFFFFFFFu, dirty, lane & ~(G - 1));
+        if (!__any_sync(0xFFFFFFFFu, dirty)) continue;
+        const bool has = dirty && gl < w.nw;
+        uint4 q[4], q0[4];
+        uint4* ptr[4];
+        bool in[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+            in[a] = has && y >= 0 && y < w.Y && z >= 0 && z < w.Z;
+            ptr[a] = in[a] ? w.rows + ((int64_t)y * w.Z + z) * w.nw + gl : w.rows;
+            q[a] = in[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+            q0[a] = q[a];
+        }
+        rowpair_core(q, has, o, rowkey(sk, (uint32_t)j, (uint32_t)k), gl, G, w.nw, half_at_end);
+        bool any = false;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const bool chg =
+                in[a] && (q[a].x != q0[a].x || q[a].y != q0[a].y || q[a].z != q0[a].z || q[a].w != q0[a].w);
+            if (chg) {
+                *ptr[a] = q[a];
+                any = true;
+            }
+            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, chg);
+            if (gl == 0 && (bal & gmask)) {
+                const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+                rflags[(int64_t)y * w.Z + z] = (uint8_t)tb;
+            }
+        }
+        if (counts && any) count_bricks(counts, w, y0, z0, gl, q, q0, in);
     }
 }
 
@@ -830,17 +905,10 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
     return FS3D_OK;
 }
 
-namespace {
-std::atomic<uint32_t> g_inject_tx_extra_host{0};  // the same value, for kernels that take it as an argument
-}  // namespace
-
 fs3d_status set_inject_tx_extra(uint32_t bytes) {
     FS3D_CUDA(cudaMemcpyToSymbol(g_inject_tx_extra, &bytes, sizeof(bytes)));
-    g_inject_tx_extra_host.store(bytes);
     return FS3D_OK;
 }
-
-uint32_t inject_tx_extra() { return g_inject_tx_extra_host.load(); }
 
 int smem_world_limit() {
     init_classes();
@@ -1058,6 +1126,28 @@ __global__ void k_advance_worlds(PlaneWorld* __restrict__ worlds, const int* __r
 fs3d_status launch_advance_worlds(PlaneWorld* worlds, const int* meta, cudaStream_t st) {
     k_advance_worlds<<<8, 256, 0, st>>>(worlds, meta);
     FS3D_CHECK_LAUNCH("advance worlds launch");
+    return FS3D_OK;
+}
+
+fs3d_status init_row_flags(uint8_t* rflags, int Y, int Z, uint64_t t0, cudaStream_t st) {
+    FS3D_CUDA(cudaMemsetAsync(rflags, (int)((t0 - 1u) & 0xFFu), (size_t)Y * (size_t)Z, st));
+    return FS3D_OK;
+}
+
+fs3d_status launch_plane_step_skip(const PlaneWorld& w, uint8_t* rflags, int* counts, cudaStream_t st) {
+    static const int per_sm = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_plane_step_skip, 256, 0) != cudaSuccess || v < 1) v = 1;
+        cudaGetLastError();
+        return v;
+    }();
+    const int per = 32 >> w.lg;
+    const int64_t nrp = (int64_t)nblocks(w.Y, 1) * nblocks(w.Z, 1);
+    const int64_t need = ((nrp + per - 1) / per + 7) / 8;  // eight warps per CTA
+    const int64_t cap = (int64_t)sm_count_public() * per_sm;
+    const int grid = (int)(need < 1 ? 1 : (need < cap ? need : cap));
+    k_plane_step_skip<<<grid, 256, 0, st>>>(w, rflags, counts);
+    FS3D_CHECK_LAUNCH("plane step (settled skip) launch");
     return FS3D_OK;
 }
 

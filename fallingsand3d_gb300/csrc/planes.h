@@ -60,7 +60,6 @@ int smem_world_limit();
 constexpr int kErrInts = 4;  // size of the error record a resident launch is given
 // test hook: resident kernels announce `bytes` more than each bulk copy delivers
 fs3d_status set_inject_tx_extra(uint32_t bytes);
-uint32_t inject_tx_extra();  // its current value (host side)
 // test hook: the next n stream-ordered allocations of batch admissions fail as out of memory
 void set_inject_alloc_failures(int n);
 // One launch steps every world of class `cls` (order[meta[1+K+cls] ...],
@@ -137,24 +136,21 @@ fs3d_status planes_generate_batch_world(uint64_t world_seed, int X, int Y, int Z
 fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, int Y, int Z, uint8_t* g,
                             cudaStream_t st, const int* skip_if_set = nullptr);
 
-// ---- per-step kernel of one large world: TMA tensor tiles and an exact skip
-// of settled tiles (tiled.cu).  Rows of 2..32 plane words (65..2048 cells).
-bool tiled_supported(int X, int Y, int Z);
-// bytes of the row change flags (four rotating buffers of Y x ceil(Z/32) words)
-size_t tiled_flag_bytes(int Y, int Z);
-// the tensor map (128 bytes, 64-byte aligned) of a world's planes at `rows`
-fs3d_status tiled_encode(const uint4* rows, int X, int Y, int Z, void* tmap_out);
-// flags for a world about to take step t0 with no history: every row changed at t0-1 and t0-2
-fs3d_status tiled_init_flags(uint32_t* flags, int Y, int Z, uint64_t t0, cudaStream_t st);
-// one step (w.t) of the world; err: a kErrInts error record (a set record: the launch steps nothing)
-fs3d_status launch_plane_step_tiled(const void* tmap, const PlaneWorld& w, uint32_t* flags, int* counts, int* err,
-                                    cudaStream_t st);
+// ---- per-step kernel of one large world with an exact skip of settled
+// row-pairs: one byte per row (y, z) holds the low 8 bits of the last step
+// that changed it (Y*Z bytes).  init_row_flags: a world about to take step t0
+// with no history (every row changed at t0 - 1).
+fs3d_status init_row_flags(uint8_t* rflags, int Y, int Z, uint64_t t0, cudaStream_t st);
+// one step (w.t) of the world; counts as for launch_plane_step
+fs3d_status launch_plane_step_skip(const PlaneWorld& w, uint8_t* rflags, int* counts, cudaStream_t st);
 fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,
                               unsigned long long* out_dev, cudaStream_t st);
-// brick_counts: nullable per-brick counts of non-empty cells of world 0, kept
-// exact as it steps (one-world launches of a world that renders)
+// One step of many worlds at once (the batch's worlds too large to be
+// resident).  brick_counts: nullable per-brick counts of non-empty cells of
+// world 0, kept exact as it steps.
 fs3d_status launch_plane_step(const PlaneWorld* worlds, const PlaneItem* items, const int* n_items_dev, int grid,
                               int s_seg, cudaStream_t st, int* brick_counts = nullptr);
+
 // After a segment: every world of the table (meta[kMetaWorlds] of them) moves
 // on by its segment steps, and its layer flags count as kept, so the next
 // segment of an unchanged batch reuses the table as it stands.

@@ -60,8 +60,7 @@ fs3d_status run_error_word(int** out) {
 struct RunScratch {
     uint4* rows = nullptr;
     PlaneWorld* desc = nullptr;
-    int* ints = nullptr;  // meta (1 + 2*classes), order[0], counter, error flag
-    PlaneItem* items = nullptr;
+    int* ints = nullptr;  // meta (1 + 2*classes), order[0], counter
 };
 
 constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kInts = kCounter + 1;
@@ -76,25 +75,20 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     if (n_steps == 0) return FS3D_OK;
     if (X > kPlaneMaxX) return launch_step_bytes(grid_dev, X, Y, Z, seed, t0, n_steps, st);
     const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
-    // worlds too large for shared memory: the tiled per-step kernel (rows of
-    // 2..32 words), else the per-step kernel with its work items
-    const bool tiled = cls < 0 && tiled_supported(X, Y, Z);
-    const int n_items = cls >= 0 || tiled ? 0 : plane_items_for(Y, Z, nw);
+    // worlds too large for shared memory: the per-step kernel that skips
+    // settled row-pairs (per-row flags in the scratch)
     int* err = nullptr;
-    if (cls >= 0 || tiled) {
+    {
         const fs3d_status se = run_error_word(&err);
         if (se != FS3D_OK) return se;
     }
     RunScratch sc;
-    uint32_t* flags = nullptr;
+    uint8_t* rflags = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&sc.rows, plane_bytes(X, Y, Z), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.desc, sizeof(PlaneWorld), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.ints, sizeof(int) * kInts, st);
-    if (e == cudaSuccess && n_items) e = cudaMallocAsync((void**)&sc.items, sizeof(PlaneItem) * n_items, st);
-    if (e == cudaSuccess && tiled) e = cudaMallocAsync((void**)&flags, tiled_flag_bytes(Y, Z), st);
+    if (e == cudaSuccess && cls < 0) e = cudaMallocAsync((void**)&rflags, (size_t)Y * Z, st);
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_run_device scratch");
-    alignas(64) unsigned char tmap[128];
-    if (s == FS3D_OK && tiled) s = tiled_encode(sc.rows, X, Y, Z, tmap);
     PlaneWorld d{};
     d.rows = sc.rows;
     d.seed = seed;
@@ -106,30 +100,21 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     d.steps = n_steps;
     d.lg = lg;
     int ints[kInts] = {};
-    ints[0] = n_items;
     if (cls >= 0) ints[1 + cls] = 1;
-    std::vector<PlaneItem> items((size_t)n_items);
-    for (int a = 0; a < n_items; ++a) items[(size_t)a] = PlaneItem{0, a * (32 >> lg)};
     // pageable sources: staged before each call returns
     if (s == FS3D_OK) e = cudaMemcpyAsync(sc.desc, &d, sizeof(d), cudaMemcpyHostToDevice, st);
     if (s == FS3D_OK && e == cudaSuccess) e = cudaMemcpyAsync(sc.ints, ints, sizeof(ints), cudaMemcpyHostToDevice, st);
-    if (s == FS3D_OK && e == cudaSuccess && n_items)
-        e = cudaMemcpyAsync(sc.items, items.data(), sizeof(PlaneItem) * n_items, cudaMemcpyHostToDevice, st);
     if (s == FS3D_OK && e != cudaSuccess) s = cuda_fail(e, "fs3d_run_device tables");
     if (s == FS3D_OK) s = planes_from_bytes(grid_dev, X, Y, Z, sc.rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
             s = launch_plane_segment_resident(cls, sc.desc, sc.ints + kOrder, sc.ints, sc.ints + kCounter, err, st);
-        } else if (tiled) {
-            s = tiled_init_flags(flags, Y, Z, t0, st);
+        } else {
+            s = init_row_flags(rflags, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = t0 + (uint64_t)a;
-                s = launch_plane_step_tiled(tmap, d, flags, nullptr, err, st);
+                s = launch_plane_step_skip(d, rflags, nullptr, st);
             }
-        } else {
-            const int grid = plane_step_grid(n_items);
-            for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
-                s = launch_plane_step(sc.desc, sc.items, sc.ints, grid, a, st);
         }
     }
     // a recorded failure (this run's or an earlier one's) leaves the grid as it was
@@ -137,8 +122,7 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     cudaFreeAsync(sc.rows, st);
     cudaFreeAsync(sc.desc, st);
     cudaFreeAsync(sc.ints, st);
-    if (sc.items) cudaFreeAsync(sc.items, st);
-    if (flags) cudaFreeAsync(flags, st);
+    if (rflags) cudaFreeAsync(rflags, st);
     return s;
 }
 

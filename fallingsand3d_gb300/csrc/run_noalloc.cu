@@ -16,7 +16,8 @@
 //    cells, e.g. 512^3), and rows wider than 2048 cells are refused; larger
 //    worlds are rejected with FS3D_ERR_INVALID_ARG and a message;
 //  * every GPU that loads this library holds the array (64 MiB of planes +
-//    3 MiB of tables and flags) until the process exits;
+//    4 MiB of row flags and a few hundred bytes of tables) until the process
+//    exits;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it for the
 //    device's current context (a new context after cudaDeviceReset looks it
@@ -37,17 +38,17 @@ namespace fs3d {
 namespace {
 
 constexpr size_t kNoAllocPlaneBytes = (size_t)64 << 20;
-constexpr size_t kNoAllocMaxItems = 1u << 17;  // per-step work items (1 MiB)
 constexpr int kMaxDevices = 64;
 
-// scratch layout: [planes][one-world descriptor][ints][sticky error word][work items][row change flags]
+// scratch layout: [planes][one-world descriptor][ints][sticky error record][row flags]
 constexpr size_t kDescOff = kNoAllocPlaneBytes;
 constexpr size_t kIntsOff = kDescOff + 256;
 constexpr int kOrder = kMetaInts, kCounter = kOrder + 1, kInts = kCounter + 1;
 constexpr size_t kErrOff = kIntsOff + 256;  // set by a timed-out copy, cleared by fs3d_run_device_check only
-constexpr size_t kItemsOff = kErrOff + 256;
-constexpr size_t kFlagsOff = kItemsOff + kNoAllocMaxItems * sizeof(PlaneItem);
-constexpr size_t kNoAllocFlagBytes = (size_t)2 << 20;  // row change flags of the tiled per-step kernel
+constexpr size_t kFlagsOff = kErrOff + 256;
+// one byte per row of the per-step kernel: a world of at most 64 MiB of
+// planes has at most 4 Mi rows (one 16-byte word each at the least)
+constexpr size_t kNoAllocFlagBytes = kNoAllocPlaneBytes / sizeof(uint4);
 constexpr size_t kScratchBytes = kFlagsOff + kNoAllocFlagBytes;
 static_assert(kInts * sizeof(int) <= 256, "ints region");
 
@@ -62,20 +63,16 @@ ScratchAddr g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_mu;
 
 // Writes the one-world tables into the scratch and clears the work counter
-// (the array keeps whatever the previous call left; the sticky error word is
-// left alone).
-__global__ void k_noalloc_tables(PlaneWorld d, int cls, int n_items, int per, unsigned char* base) {
+// (the array keeps whatever the previous call left; the sticky error record
+// is left alone).
+__global__ void k_noalloc_tables(PlaneWorld d, int cls, unsigned char* base) {
     PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
     int* ints = reinterpret_cast<int*>(base + kIntsOff);
-    PlaneItem* items = reinterpret_cast<PlaneItem*>(base + kItemsOff);
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         *desc = d;
         for (int a = 0; a < kInts; ++a) ints[a] = 0;
-        ints[0] = n_items;
         if (cls >= 0) ints[1 + cls] = 1;
     }
-    for (int a = tid; a < n_items; a += gridDim.x * blockDim.x) items[a] = PlaneItem{0, a * per};
 }
 
 }  // namespace
@@ -123,10 +120,6 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
                          "fs3d_run_device_noalloc: world too large for the static scratch (planes of at most "
                          "64 MiB, about 268 M cells, and rows of at most 2048 cells)");
     const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
-    const bool tiled = cls < 0 && tiled_supported(X, Y, Z) && tiled_flag_bytes(Y, Z) <= kNoAllocFlagBytes;
-    const int n_items = cls >= 0 || tiled ? 0 : plane_items_for(Y, Z, nw);
-    if ((size_t)n_items > kNoAllocMaxItems)
-        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_run_device_noalloc: too many row-pairs for the static scratch");
     if (n_steps == 0) return FS3D_OK;
     unsigned char* base = nullptr;
     fs3d_status s = noalloc_scratch_base(&base);
@@ -143,29 +136,22 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
     d.nw = nw;
     d.steps = n_steps;
     d.lg = lg;
-    k_noalloc_tables<<<n_items > 0 ? (n_items + 255) / 256 : 1, 256, 0, st>>>(d, cls, n_items, 32 >> lg, base);
+    k_noalloc_tables<<<1, 32, 0, st>>>(d, cls, base);
     FS3D_CHECK_LAUNCH("noalloc tables launch");
     PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
     int* ints = reinterpret_cast<int*>(base + kIntsOff);
-    PlaneItem* items = reinterpret_cast<PlaneItem*>(base + kItemsOff);
     int* err = reinterpret_cast<int*>(base + kErrOff);
     s = planes_from_bytes(grid_dev, X, Y, Z, rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
             s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, err, st);
-        } else if (tiled) {
-            // the tensor map is a host-side description: encoding it allocates nothing
-            alignas(64) unsigned char tmap[128];
-            uint32_t* flags = reinterpret_cast<uint32_t*>(base + kFlagsOff);
-            s = tiled_encode(rows, X, Y, Z, tmap);
-            if (s == FS3D_OK) s = tiled_init_flags(flags, Y, Z, t0, st);
+        } else {
+            uint8_t* rflags = base + kFlagsOff;
+            s = init_row_flags(rflags, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = t0 + (uint64_t)a;
-                s = launch_plane_step_tiled(tmap, d, flags, nullptr, err, st);
+                s = launch_plane_step_skip(d, rflags, nullptr, st);
             }
-        } else {
-            const int grid = plane_step_grid(n_items);
-            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) s = launch_plane_step(desc, items, ints, grid, a, st);
         }
     }
     // static cells never change: their values are read back from the grid

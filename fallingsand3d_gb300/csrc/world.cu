@@ -24,23 +24,17 @@ struct fs3d_world {
     uint8_t* bytes = nullptr;    // BYTES: the state
     uint4* rows = nullptr;       // PLANES: the state
     uint8_t* statics = nullptr;  // PLANES: initial bytes when some cell holds a material >= 4
-    PlaneWorld* desc = nullptr;  // PLANES: one-world step tables
-    PlaneItem* items = nullptr;
-    int* n_items_dev = nullptr;
-    int n_items = 0;
-    int* aux = nullptr;  // resident tables, see kAux*
+    PlaneWorld* desc = nullptr;  // PLANES: one-world descriptor of the resident kernels
+    int* aux = nullptr;          // resident tables, see kAux*
     int cls = -1;        // resident class (-1: stepped by the per-step kernel)
     unsigned long long* hash_dev = nullptr;
     uint32_t* brickmap = nullptr;  // render: per-frame occupancy of 8x8x8 bricks
     int* brick_counts = nullptr;   // PLANES render: non-empty cells per brick, kept by the per-step kernel
     bool counts_valid = false;     // brick_counts match the planes
-    // PLANES worlds stepped by the tiled per-step kernel: its tensor map and row change flags
-    bool tiled = false;
-    alignas(64) unsigned char tmap[128] = {};
-    uint32_t* tflags = nullptr;
-    bool flags_ok = false;  // tflags describe the state at step flags_t
+    // PLANES worlds stepped by the per-step kernel: per-row last-changed step (Y*Z bytes)
+    uint8_t* rflags = nullptr;
+    bool flags_ok = false;  // rflags describe the state at step flags_t
     uint64_t flags_t = 0;
-    bool broken = false;    // a per-step launch failed part-way: the state must be rewritten
     int64_t cells() const { return (int64_t)X * Y * Z; }
 };
 
@@ -86,13 +80,11 @@ void destroy(fs3d_world* w) {
     cudaFree(w->rows);
     cudaFree(w->statics);
     cudaFree(w->desc);
-    cudaFree(w->items);
-    cudaFree(w->n_items_dev);
     cudaFree(w->aux);
     cudaFree(w->hash_dev);
     cudaFree(w->brickmap);
     cudaFree(w->brick_counts);
-    cudaFree(w->tflags);
+    cudaFree(w->rflags);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
 }
@@ -158,33 +150,17 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
     } else {
         e = cudaMalloc((void**)&w->rows, plane_bytes(X, Y, Z));
         if (e != cudaSuccess) return fail(e, "cudaMalloc(planes)");
-        const int nw = plane_nw(X);
-        w->n_items = plane_items_for(Y, Z, nw);
-        std::vector<PlaneItem> items((size_t)w->n_items);
-        const int per = 32 >> plane_lg(nw);
-        for (int a = 0; a < w->n_items; ++a) items[(size_t)a] = PlaneItem{0, a * per};
         e = cudaMalloc((void**)&w->desc, sizeof(PlaneWorld));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&w->items, sizeof(PlaneItem) * items.size());
-        if (e == cudaSuccess) e = cudaMalloc((void**)&w->n_items_dev, sizeof(int));
-        // resident tables: meta (one world in its class), order {0}, work counter, error flag
+        // resident tables: meta (one world in its class), order {0}, work counter, error record
         int aux[kAuxInts] = {};
         w->cls = resident_class(X, Y, Z);
         if (w->cls >= 0) aux[1 + w->cls] = 1;
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->aux, sizeof(aux));
         if (e == cudaSuccess) e = cudaMemcpy(w->aux, aux, sizeof(aux), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess)
-            e = cudaMemcpy(w->items, items.data(), sizeof(PlaneItem) * items.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(w->n_items_dev, &w->n_items, sizeof(int), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return fail(e, "cudaMalloc/copy(step tables)");
-        if (w->cls < 0 && tiled_supported(X, Y, Z)) {
-            e = cudaMalloc((void**)&w->tflags, tiled_flag_bytes(Y, Z));
+        if (w->cls < 0) {
+            e = cudaMalloc((void**)&w->rflags, (size_t)Y * Z);
             if (e != cudaSuccess) return fail(e, "cudaMalloc(row change flags)");
-            s = tiled_encode(w->rows, X, Y, Z, w->tmap);
-            if (s != FS3D_OK) {
-                destroy(w);
-                return s;
-            }
-            w->tiled = true;
         }
     }
     s = upload(w, grid_host);
@@ -198,7 +174,6 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
 
 fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
     if (!w || n_steps < 0) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_step: bad args");
-    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_step: the world must be rewritten (fs3d_world_write)");
     if (n_steps == 0) return FS3D_OK;
     fs3d_status s;
     if (w->layout == FS3D_LAYOUT_BYTES) {
@@ -216,17 +191,19 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
         d.steps = n_steps;
         d.lg = plane_lg(nw);
         s = FS3D_OK;
-        if (w->tiled) {
-            // one launch per step; the row change flags carry over from the
-            // previous call when nothing else touched the world since
+        if (w->cls < 0) {
+            // one launch per step, settled row-pairs skipped; the row flags
+            // carry over from the previous call when nothing else touched the
+            // world since.  Once a frame has counted the bricks, the kernel
+            // keeps the counts exact, so later frames read no pass over the planes
             if (!w->flags_ok || w->flags_t != w->step) {
-                s = tiled_init_flags(w->tflags, w->Y, w->Z, w->step, w->stream);
+                s = init_row_flags(w->rflags, w->Y, w->Z, w->step, w->stream);
                 w->flags_ok = s == FS3D_OK;
             }
             int* counts = w->counts_valid ? w->brick_counts : nullptr;
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = w->step + (uint64_t)a;
-                s = launch_plane_step_tiled(w->tmap, d, w->tflags, counts, w->aux + kAuxErr, w->stream);
+                s = launch_plane_step_skip(d, w->rflags, counts, w->stream);
             }
             if (s == FS3D_OK) {
                 w->flags_t = w->step + (uint64_t)n_steps;
@@ -236,21 +213,13 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
             }
             return s;
         }
-        // pageable source: staged before the call returns
+        // the world fits in shared memory (one CTA or a cluster): all n steps
+        // in one launch; the descriptor's pageable source is staged before the
+        // call returns
         FS3D_CUDA(cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream));
-        if (w->cls >= 0) {
-            // the world fits in shared memory (one CTA or a cluster): all n steps in one launch
-            s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
-                                              w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
-            w->counts_valid = false;  // the next frame recounts
-        } else {
-            // once a frame has counted the bricks, the per-step kernel keeps
-            // the counts exact, so later frames read no pass over the planes
-            const int grid = plane_step_grid(w->n_items);
-            for (int a = 0; a < n_steps && s == FS3D_OK; ++a)
-                s = launch_plane_step(w->desc, w->items, w->n_items_dev, grid, a, w->stream,
-                                      w->counts_valid ? w->brick_counts : nullptr);
-        }
+        s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
+                                          w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
+        w->counts_valid = false;  // the next frame recounts
     }
     if (s == FS3D_OK) w->step += (uint64_t)n_steps;
     return s;
@@ -268,15 +237,6 @@ fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
             memcpy(&t_fail, err + 2, sizeof(t_fail));
             FS3D_CUDA(cudaMemset(w->aux + kAuxErr, 0, sizeof(err)));
             w->counts_valid = false;
-            w->flags_ok = false;
-            if (w->tiled) {
-                // the per-step kernel stores each tile as it goes: the failed
-                // step left some tiles stepped and others not
-                w->broken = true;
-                return set_error(FS3D_ERR_TIMEOUT,
-                                 "a tile copy of the per-step kernel did not complete in time; the world holds a "
-                                 "partly stepped state and must be rewritten (fs3d_world_write)");
-            }
             // the failed launch and every launch after it stepped nothing: the
             // state is the one the failed launch started from
             w->step = t_fail;
@@ -290,7 +250,6 @@ fs3d_status fs3d_world_sync(fs3d_world* w, int64_t timeout_ns) {
 
 fs3d_status fs3d_world_read(fs3d_world* w, uint8_t* out) {
     if (!w || !out) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_read: bad args");
-    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_read: the world must be rewritten (fs3d_world_write)");
     const size_t n = (size_t)w->cells();
     if (w->layout == FS3D_LAYOUT_BYTES) {
         FS3D_CUDA(cudaMemcpyAsync(out, w->bytes, n, cudaMemcpyDeviceToHost, w->stream));
@@ -312,14 +271,11 @@ fs3d_status fs3d_world_write(fs3d_world* w, const uint8_t* g) {
     if (!w || !g) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_write: bad args");
     w->counts_valid = false;
     w->flags_ok = false;
-    const fs3d_status s = upload(w, g);
-    if (s == FS3D_OK) w->broken = false;
-    return s;
+    return upload(w, g);
 }
 
 fs3d_status fs3d_world_hash(fs3d_world* w, uint64_t* out) {
     if (!w || !out) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_world_hash: bad args");
-    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_world_hash: the world must be rewritten (fs3d_world_write)");
     fs3d_status s = (w->layout == FS3D_LAYOUT_BYTES)
                         ? hash_bytes_async(w->bytes, w->cells(), w->hash_dev, w->stream)
                         : planes_hash_async(w->rows, w->statics, w->X, w->Y, w->Z, w->hash_dev, w->stream);
@@ -414,7 +370,6 @@ fs3d_status fs3d_render(fs3d_world* w, const fs3d_camera* cam, int W, int H, int
                         int out_on_device) {
     if (!w || !cam || !rgba || W <= 0 || H <= 0 || (mode != FS3D_RENDER_DDA && mode != FS3D_RENDER_SDF_SPHERE))
         return set_error(FS3D_ERR_INVALID_ARG, "fs3d_render: bad args");
-    if (w->broken) return set_error(FS3D_ERR_STATE, "fs3d_render: the world must be rewritten (fs3d_world_write)");
     float* dst = rgba;
     const size_t bytes = (size_t)W * H * 4 * sizeof(float);
     if (mode == FS3D_RENDER_DDA && !w->brickmap)

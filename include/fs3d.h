@@ -120,7 +120,7 @@ fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t see
 /* fs3d_run_device for callers that cannot allocate device memory (an engine
  * whose own allocator owns all GPU memory, a real-time frame loop that must
  * not stall on an allocation): same arguments and results, but the scratch
- * lives in one static device array (64 MiB of planes plus 3 MiB of tables)
+ * lives in one static device array (64 MiB of planes plus 4 MiB of row flags)
  * that every GPU loading this library holds until exit, so the call allocates
  * nothing.  Worlds whose planes exceed 64 MiB (about 268 M cells) or whose
  * rows exceed 2048 cells are rejected with FS3D_ERR_INVALID_ARG.  The first

@@ -2,11 +2,10 @@
 oracle runs the same steps on the host cores).
 
 * 512^3 pillars, 1000 steps: the drop-in byte kernel's whole-grid hash every
-  10 steps and the final grid; the same world in the plane layout (tiled
-  per-step kernel) by hash after the 1000 steps.
-* 1024^3 dunes, 500 steps: the plane-layout world (tiled kernel, exact skip of
-  settled tiles) by hash after every one of the first 50 steps, and the whole
-  final grid after step 500.
+  10 steps and the final grid; the same world in the plane layout (per-step
+  kernel with the exact skip of settled row-pairs) by hash after the 1000 steps.
+* 1024^3 dunes, 500 steps: the plane-layout world (the same kernel) by hash
+  after every one of the first 50 steps, and the whole final grid after step 500.
 
 On a mismatch the first differing voxel is reported.  Integer work: bit-exact."""
 import numpy as np
@@ -41,7 +40,7 @@ def test_pillars_512_1000_steps(fs3d, orc, cuda):
             fs3d.step_device(again.data_ptr(), X, Y, Z, seed, 0, every * (c + 1), st)
             pytest.fail("byte kernel: " + describe_diff(again.cpu().numpy(), ref, every * (c + 1) - 1))
     assert (final == ref).all(), describe_diff(final, ref, n - 1)
-    assert planes_hash == orc.hash(ref), "plane layout (tiled kernel) differs after 1000 steps"
+    assert planes_hash == orc.hash(ref), "plane layout (per-step kernel) differs after 1000 steps"
 
 
 def test_dunes_1024_500_steps(fs3d, orc):

@@ -1,9 +1,9 @@
-"""GPU parity of the tiled per-step kernel (one large world: TMA tensor tiles
-and the exact skip of settled tiles) against the CPU oracle, whole-grid hash
+"""GPU parity of the per-step kernel of one large world (exact skip of settled
+row-pairs by per-row change bytes) against the CPU oracle, whole-grid hash
 after every step, first differing voxel on failure.  The worlds are too large
 for the shared-memory resident kernels, so the world object steps them with
-the tiled kernel; rows of 2 to 32 plane words, odd sizes in y and z, static
-materials.  Integer work: bit-exact."""
+the per-step kernel; rows of 1 to 32 plane words, odd sizes in y and z,
+static materials.  Integer work: bit-exact."""
 import numpy as np
 import oracle_lib
 import pytest
@@ -21,9 +21,9 @@ def mixed_grid(X, Y, Z, seed):
     return g
 
 
-# (X, Y, Z): plane words per row 16, 32 (17 used), 3, 2, 8, 16 (partial last word), 32
+# (X, Y, Z): plane words per row 16, 17 (groups of 32 lanes), 3, 2, 8, 16 (partial last word), 32, 1
 DIMS = [(1024, 64, 256), (1088, 63, 200), (130, 300, 260), (100, 600, 333), (512, 257, 97), (1000, 33, 300),
-        (2048, 64, 96)]
+        (2048, 64, 96), (64, 700, 700)]
 
 
 def check_every_step(fs3d, orc, g, seed, t0, n, layout=1):
@@ -41,22 +41,22 @@ def check_every_step(fs3d, orc, g, seed, t0, n, layout=1):
 
 
 @pytest.mark.parametrize("dims", DIMS)
-def test_tiled_world_every_step(fs3d, orc, dims):
+def test_large_world_every_step(fs3d, orc, dims):
     X, Y, Z = dims
     seed = X * 131 + Y * 7 + Z
     g = mixed_grid(X, Y, Z, seed)
     check_every_step(fs3d, orc, g, seed, 3, 40)
 
 
-def test_tiled_settled_dunes_every_step(fs3d, orc):
+def test_settled_dunes_every_step(fs3d, orc):
     """256^3 dunes (rows of 4 words): the sand settles and the rain lands, so
-    ever more tiles are skipped; every step still equals the oracle."""
+    ever more row-pairs are skipped; every step still equals the oracle."""
     g = orc.gen_c5(4, 256, 256, 256)
     assert (g == fs3d.gen_dunes(4, 256, 256, 256)).all()
     check_every_step(fs3d, orc, g, 4, 0, 300)
 
 
-def test_tiled_steps_in_several_calls_and_after_write(fs3d, orc):
+def test_steps_in_several_calls_and_after_write(fs3d, orc):
     """The row change flags carry over between step calls (the same results as
     one call), and a rewrite of the world's contents starts them afresh."""
     X, Y, Z = 512, 200, 160
@@ -79,8 +79,8 @@ def test_tiled_steps_in_several_calls_and_after_write(fs3d, orc):
 
 @pytest.mark.parametrize("entry", ["fs3d_run_device", "fs3d_run_device_noalloc"])
 def test_drop_in_runs_of_large_worlds(fs3d, orc, cuda, entry):
-    """The drop-in runs take the tiled kernel for worlds too large for shared
-    memory: two runs in a row equal the oracle."""
+    """The drop-in runs take the per-step kernel for worlds too large for
+    shared memory: two runs in a row equal the oracle."""
     X, Y, Z = 1024, 96, 200
     seed = 77
     g = mixed_grid(X, Y, Z, seed)
@@ -96,8 +96,8 @@ def test_drop_in_runs_of_large_worlds(fs3d, orc, cuda, entry):
     assert (got == ref).all(), describe_diff(got, ref, 33)
 
 
-def test_tiled_render_counts_stay_exact(fs3d, orc):
-    """A rendered world keeps its per-brick counts through the tiled kernel:
+def test_render_counts_stay_exact(fs3d, orc):
+    """A rendered world keeps its per-brick counts through the per-step kernel:
     frames after stepping equal the CPU DDA of the oracle's grid."""
     X, Y, Z = 512, 160, 192
     g = mixed_grid(X, Y, Z, 9)
@@ -110,29 +110,3 @@ def test_tiled_render_counts_stay_exact(fs3d, orc):
             img = w.render(cam, 160, 90)
         exp = orc.render_dda(ref, oracle_lib.camera_from(cam), 160, 90)
         assert float(np.abs(img - exp).max()) <= 1e-5
-
-
-def test_tiled_copy_timeout_marks_the_world(fs3d, orc):
-    """With every tile copy's wait made to run out (test hook), the step
-    reports FS3D_ERR_TIMEOUT; the world then refuses use until rewritten, and
-    after a rewrite it steps exactly again."""
-    X, Y, Z = 1024, 64, 160
-    g = mixed_grid(X, Y, Z, 12)
-    with fs3d.World(g, 12, 0, fs3d.LAYOUT_PLANES) as w:
-        fs3d.inject(fs3d.INJECT_COPY_STALL, 1)
-        try:
-            w.step(3)
-            with pytest.raises(fs3d.Fs3dError) as e:
-                w.sync()
-            assert e.value.status == fs3d.ERR_TIMEOUT
-        finally:
-            fs3d.inject(fs3d.INJECT_NONE, 0)
-        with pytest.raises(fs3d.Fs3dError) as e:
-            w.step(1)
-        assert e.value.status == fs3d.ERR_STATE
-        w.write(g)
-        w.step(10)
-        ref = g.copy()
-        orc.run(ref, 12, 3, 10, nthreads=0)  # the counter kept the three reported steps
-        got = w.read()
-        assert (got == ref).all(), describe_diff(got, ref, 12)
