@@ -45,7 +45,7 @@ EXPORTS = (
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
     "fs3d_batch_retire_many", "fs3d_batch_admit_many_async", "fs3d_batch_retire_many_async", "fs3d_batch_wait_copies",
     "fs3d_batch_read_many",
-    "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_retire",
+    "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_poll_many", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
     "fs3d_render_object", "fs3d_render_meshes", "fs3d_gen_parity", "fs3d_gen_pillars",
@@ -170,6 +170,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_run_segment": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
+        "fs3d_batch_poll_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(i32), C.POINTER(u64)]),
         "fs3d_batch_retire": (S, [vp, u64, vp]),
         "fs3d_batch_autotune": (S, [vp, i32, C.POINTER(TuneReport)]),
         "fs3d_batch_counters": (S, [vp, C.POINTER(u64), C.POINTER(u64)]),
@@ -602,6 +603,18 @@ class Batch:
         done, h = i32(), u64()
         check(lib().fs3d_batch_poll(self.handle, ticket, C.byref(done), C.byref(h) if with_hash else None))
         return bool(done.value), (int(h.value) if done.value and with_hash else None)
+
+    def poll_many(self, tickets, with_hash: bool = True):
+        """(done, hashes) arrays for many worlds; hashes of the finished ones
+        computed together."""
+        n = len(tickets)
+        ts = np.asarray(tickets if n else [0], dtype=np.uint64)
+        done = np.zeros(max(n, 1), dtype=np.int32)
+        hs = np.zeros(max(n, 1), dtype=np.uint64)
+        check(lib().fs3d_batch_poll_many(self.handle, n, ts.ctypes.data_as(C.POINTER(u64)),
+                                         done.ctypes.data_as(C.POINTER(i32)),
+                                         hs.ctypes.data_as(C.POINTER(u64)) if with_hash else None))
+        return done[:n].astype(bool), hs[:n]
 
     def retire(self, ticket: int, shape=None) -> Optional[np.ndarray]:
         if shape is None:

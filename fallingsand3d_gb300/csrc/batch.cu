@@ -901,6 +901,69 @@ fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t*
     return FS3D_OK;
 }
 
+fs3d_status fs3d_batch_poll_many(fs3d_batch* b, int n, const uint64_t* tickets, int* done, uint64_t* hashes) {
+    if (!b || n < 0 || (n > 0 && (!tickets || !done)))
+        return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_poll_many: bad args");
+    std::vector<BWorld*> need;
+    std::vector<int> need_at;
+    for (int i = 0; i < n; ++i) {
+        auto it = b->worlds.find(tickets[i]);
+        if (it == b->worlds.end()) return set_error(FS3D_ERR_NOT_FOUND, "fs3d_batch_poll_many: unknown ticket");
+        BWorld& w = it->second;
+        done[i] = 0;
+        if (!w.done) continue;
+        if (w.admit_id && hashes) {
+            const fs3d_status f = finalize_admits(b, w.admit_id, true);
+            if (f != FS3D_OK) return f;
+        }
+        if (w.finished) {
+            const cudaError_t q = cudaEventQuery(w.finished.get());
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess) return cuda_fail(q, "fs3d_batch_poll_many");
+        }
+        done[i] = 1;
+        if (!hashes) continue;
+        if (w.hash_valid) {
+            hashes[i] = w.hash;
+        } else {
+            need.push_back(&w);
+            need_at.push_back(i);
+        }
+    }
+    if (need.empty()) return FS3D_OK;
+    // the hashes of every world still without one: one launch, one wait
+    const int k = (int)need.size();
+    std::vector<HashJob> jobs((size_t)k);
+    for (int j = 0; j < k; ++j) {
+        const BWorld& w = *need[(size_t)j];
+        if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
+        jobs[(size_t)j] = HashJob{w.rows, w.statics, w.X, w.Y, w.Z, w.nw};
+    }
+    const size_t jobs_bytes = (sizeof(HashJob) * (size_t)k + 15) / 16 * 16;
+    void* table = nullptr;
+    FS3D_CUDA(stream_alloc(&table, jobs_bytes + sizeof(unsigned long long) * (size_t)k, b->side));
+    unsigned long long* out_dev = reinterpret_cast<unsigned long long*>(static_cast<char*>(table) + jobs_bytes);
+    std::vector<unsigned long long> out((size_t)k);
+    cudaError_t e = cudaMemcpyAsync(table, jobs.data(), sizeof(HashJob) * (size_t)k, cudaMemcpyHostToDevice, b->side);
+    fs3d_status s = e == cudaSuccess ? planes_hash_many(static_cast<const HashJob*>(table), k, out_dev, b->side)
+                                     : cuda_fail(e, "fs3d_batch_poll_many jobs");
+    if (s == FS3D_OK) {
+        e = cudaMemcpyAsync(out.data(), out_dev, sizeof(unsigned long long) * (size_t)k, cudaMemcpyDeviceToHost,
+                            b->side);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
+        if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_poll_many hashes");
+    }
+    cudaFreeAsync(table, b->side);
+    if (s != FS3D_OK) return s;
+    for (int j = 0; j < k; ++j) {
+        BWorld& w = *need[(size_t)j];
+        w.hash = out[(size_t)j];
+        w.hash_valid = true;
+        hashes[need_at[(size_t)j]] = w.hash;
+    }
+    return FS3D_OK;
+}
+
 }  // extern "C"
 
 namespace {

@@ -99,6 +99,34 @@ __global__ void k_hash_planes(const uint4* __restrict__ rows, const uint8_t* __r
     if ((threadIdx.x & 31) == 0 && h) atomicAdd(out, (unsigned long long)h);
 }
 
+// Whole-grid hashes of many worlds in one launch: CTA j hashes world j
+// (jobs[j]) and writes its sum to out[j].
+__global__ void __launch_bounds__(256) k_hash_planes_many(const HashJob* __restrict__ jobs,
+                                                         unsigned long long* __restrict__ out) {
+    const HashJob jb = jobs[blockIdx.x];
+    const int64_t n = (int64_t)jb.Y * jb.Z * jb.nw;
+    uint64_t h = 0;
+    for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+        const int w = (int)(u % jb.nw);
+        const int64_t r = u / jb.nw;
+        const uint4 q = jb.rows[u];
+        for (int x = 64 * w; x < 64 * w + 64 && x < jb.X; ++x) {
+            const int64_t idx = r * jb.X + x;
+            h += fmix64((uint64_t)idx * 256u + cell_value(q, (x >> 1) & 31, x & 1, jb.statics, idx));
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) h += __shfl_xor_sync(0xffffffffu, h, off);
+    __shared__ unsigned long long part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = h;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += part[i];
+        out[blockIdx.x] = t;
+    }
+}
+
 // Many worlds per launch (admission and retirement of a batch): job j covers
 // units [unit_off[j], unit_off[j+1]) of (row, word) pairs; its bytes sit at
 // byte_off in one staging buffer.
@@ -1104,6 +1132,13 @@ fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, 
     FS3D_CUDA(cudaMemsetAsync(out_dev, 0, sizeof(unsigned long long), st));
     k_hash_planes<<<conv_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, statics, X, Y, Z, nw, out_dev);
     FS3D_CHECK_LAUNCH("hash planes launch");
+    return FS3D_OK;
+}
+
+fs3d_status planes_hash_many(const HashJob* jobs, int njobs, unsigned long long* out_dev, cudaStream_t st) {
+    if (njobs <= 0) return FS3D_OK;
+    k_hash_planes_many<<<njobs, 256, 0, st>>>(jobs, out_dev);
+    FS3D_CHECK_LAUNCH("hash many worlds launch");
     return FS3D_OK;
 }
 

@@ -145,6 +145,13 @@ fs3d_status init_row_flags(uint8_t* rflags, int Y, int Z, uint64_t t0, cudaStrea
 fs3d_status launch_plane_step_skip(const PlaneWorld& w, uint8_t* rflags, int* counts, cudaStream_t st);
 fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,
                               unsigned long long* out_dev, cudaStream_t st);
+// whole-grid hashes of njobs worlds in one launch: out_dev[j] for jobs[j]
+struct HashJob {
+    const uint4* rows;
+    const uint8_t* statics;  // nullable
+    int32_t X, Y, Z, nw;
+};
+fs3d_status planes_hash_many(const HashJob* jobs, int njobs, unsigned long long* out_dev, cudaStream_t st);
 // One step of many worlds at once (the batch's worlds too large to be
 // resident).  brick_counts: nullable per-brick counts of non-empty cells of
 // world 0, kept exact as it steps.

@@ -101,6 +101,9 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
     int64_t peak_live = 0;
     double vu = 0.0;
     bool segment_in_flight = false;
+    std::vector<uint64_t> tk, fin;  // live tickets, finished tickets
+    std::vector<int> dn;
+    std::vector<uint64_t> hs;
     while (completed < n && s == FS3D_OK) {
         const double now = now_s();
         while (next < n && reqs[next].arrival_s <= now) queue.push_back(next++);
@@ -130,25 +133,28 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
             s = fs3d_batch_sync(b, seg_timeout_ns);
             segment_in_flight = false;
             if (s != FS3D_OK) break;
-            for (auto it = live.begin(); it != live.end();) {
-                int done = 0;
-                uint64_t h = 0;
-                s = fs3d_batch_poll(b, it->first, &done, p->with_hash ? &h : nullptr);
-                if (s != FS3D_OK) break;
-                if (!done) {
-                    ++it;
-                    continue;
-                }
-                fs3d_serve_request& q = reqs[it->second];
-                q.hash = h;
-                q.finished_s = now_s();
+            // every live world polled at once: the finished ones are hashed
+            // together (one launch, one wait) and retired together
+            tk.clear();
+            for (const auto& kv : live) tk.push_back(kv.first);
+            dn.assign(tk.size(), 0);
+            hs.assign(tk.size(), 0);
+            s = fs3d_batch_poll_many(b, (int)tk.size(), tk.data(), dn.data(), p->with_hash ? hs.data() : nullptr);
+            if (s != FS3D_OK) break;
+            const double fin_s = now_s();
+            fin.clear();
+            for (size_t i = 0; i < tk.size(); ++i) {
+                if (!dn[i]) continue;
+                fs3d_serve_request& q = reqs[live[tk[i]]];
+                q.hash = hs[i];
+                q.finished_s = fin_s;
                 lat.push_back((q.finished_s - q.arrival_s) * 1e3);
                 vu += (double)q.X * q.Y * q.Z * q.n_steps;
                 ++completed;
-                s = fs3d_batch_retire(b, it->first, nullptr);
-                it = live.erase(it);
-                if (s != FS3D_OK) break;
+                live.erase(tk[i]);
+                fin.push_back(tk[i]);
             }
+            if (!fin.empty()) s = fs3d_batch_retire_many(b, (int)fin.size(), fin.data(), nullptr);
             continue;
         }
         if (!live.empty()) {

@@ -213,6 +213,11 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream 
 fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
 /* done = 1 once the world has taken all its steps; hash valid when done */
 fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash);
+/* fs3d_batch_poll for n worlds at once: done[i] as there; with `hashes`
+ * (nullable), hashes[i] for every world that is done, those not hashed yet
+ * computed together in one launch and one wait.  No counterpart in the
+ * upstream project. */
+fs3d_status fs3d_batch_poll_many(fs3d_batch* b, int n, const uint64_t* tickets, int* done, uint64_t* hashes);
 /* frees the world's pool space; grid_out (nullable) receives the final grid */
 fs3d_status fs3d_batch_retire(fs3d_batch* b, uint64_t ticket, uint8_t* grid_out);
 /* retire n worlds with one host wait; grids_out (nullable) holds n host pointers (nullable each) */

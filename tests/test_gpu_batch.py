@@ -624,3 +624,28 @@ def test_read_many_snapshots_live_worlds(fs3d, orc, cuda):
     for (dims, seed), sn, o in zip(worlds, snap, outs):
         assert (sn.numpy() == oracle_final(orc, fs3d, dims, seed, 2 * S)).all(), dims
         assert (o == oracle_final(orc, fs3d, dims, seed, 3 * S)).all(), dims
+
+
+def test_poll_many_matches_single_polls_and_oracle(fs3d, orc):
+    """poll_many reports the same done flags as one poll per world, and the
+    hashes of the finished worlds (computed in one launch) equal the oracle's."""
+    S = 32
+    worlds = small_batch(fs3d, 71, 12, max_dim=96)
+    steps = [10, 32, 40, 64, 70, 96, 5, 33, 64, 65, 20, 90]
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        ts = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for (dims, seed), n in zip(worlds, steps)]
+        b.run_segment()
+        b.run_segment()
+        b.sync()
+        done, hs = b.poll_many(ts)
+        for t, d, h, (dims, seed), n in zip(ts, done, hs, worlds, steps):
+            assert bool(d) == (n <= 2 * S)
+            if d:
+                assert int(h) == orc.hash(oracle_final(orc, fs3d, dims, seed, n)), (dims, n)
+                assert b.poll(t) == (1, int(h))
+        b.retire_many([t for t, d in zip(ts, done) if d])
+        b.run_segment()
+        b.sync()
+        rest = [t for t, d in zip(ts, done) if not d]
+        done2, hs2 = b.poll_many(rest)
+        assert done2.all()
