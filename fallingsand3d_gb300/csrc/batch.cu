@@ -85,13 +85,22 @@ struct PinnedArray {
     // two page-locked host images, written in turn (one may still be being
     // uploaded while the next segment's tables are built), and the device copy
     T* hb[2] = {nullptr, nullptr};
-    T* h = nullptr;  // the image in use
+    T* dvb[2] = {nullptr, nullptr};  // the images' device views (null: not addressable by the device)
+    T* h = nullptr;                  // the image in use
+    T* hv = nullptr;                 // its device view
     int cur = 0;
     T* d = nullptr;
     size_t cap = 0;
     void select(int i) {
         cur = i;
         h = hb[i];
+        hv = dvb[i];
+    }
+    // copies the first n entries of the image in use to the device: a kernel
+    // reading the page-locked image (no copy engine) when it can
+    cudaError_t upload(size_t n, cudaStream_t st) const {
+        return hv ? copy_small_async(d, hv, sizeof(T) * n, st)
+                  : cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, st);
     }
     fs3d_status reserve(size_t n) {
         if (n <= cap) return FS3D_OK;
@@ -111,7 +120,10 @@ struct PinnedArray {
         cudaFree(d);
         hb[0] = nh0;
         hb[1] = nh1;
+        dvb[0] = reinterpret_cast<T*>(device_view(nh0));
+        dvb[1] = reinterpret_cast<T*>(device_view(nh1));
         h = hb[cur];
+        hv = dvb[cur];
         d = nd;
         cap = c;
         return FS3D_OK;
@@ -120,7 +132,8 @@ struct PinnedArray {
         cudaFreeHost(hb[0]);
         cudaFreeHost(hb[1]);
         cudaFree(d);
-        hb[0] = hb[1] = h = d = nullptr;
+        hb[0] = hb[1] = h = hv = d = nullptr;
+        dvb[0] = dvb[1] = nullptr;
         cap = 0;
     }
 };
@@ -157,6 +170,7 @@ struct fs3d_batch {
     // event recorded after its upload has completed
     struct HostChunk {
         char* p = nullptr;
+        uint8_t* dv = nullptr;  // device view of p (null: not addressable by the device)
         size_t cap = 0;
         cudaEvent_t uploaded = nullptr;
     };
@@ -373,6 +387,7 @@ int take_chunk(fs3d_batch* b, size_t n) {
     fs3d_batch::HostChunk c;
     c.cap = std::max<size_t>(n, (size_t)1 << 16);
     if (cudaMallocHost((void**)&c.p, c.cap) != cudaSuccess) return -1;
+    c.dv = device_view(c.p);
     if (cudaEventCreateWithFlags(&c.uploaded, cudaEventDisableTiming) != cudaSuccess) {
         cudaFreeHost(c.p);
         return -1;
@@ -381,8 +396,12 @@ int take_chunk(fs3d_batch* b, size_t n) {
     return (int)b->host_chunks.size() - 1;
 }
 
+// (a kernel reads the page-locked chunk: a copy-engine transfer here would
+// queue behind the hundreds of MB other streams move over the host link, and
+// hold up the conversion or segment that needs the table)
 cudaError_t upload_chunk(fs3d_batch* b, int i, void* dst, size_t n, cudaStream_t st) {
-    cudaError_t e = cudaMemcpyAsync(dst, b->host_chunks[(size_t)i].p, n, cudaMemcpyHostToDevice, st);
+    const fs3d_batch::HostChunk& c = b->host_chunks[(size_t)i];
+    cudaError_t e = c.dv ? copy_small_async(dst, c.dv, n, st) : cudaMemcpyAsync(dst, c.p, n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaEventRecord(b->host_chunks[(size_t)i].uploaded, st);
     return e;
 }
@@ -787,11 +806,12 @@ fs3d_status build_tables(fs3d_batch* b) {
             cudaEventDestroy(kv.second.ready);
             kv.second.ready = nullptr;
         }
-    FS3D_CUDA(cudaMemcpyAsync(b->tw.d, b->tw.h, sizeof(PlaneWorld) * nw_, cudaMemcpyHostToDevice, b->stream));
-    if (ii) FS3D_CUDA(cudaMemcpyAsync(b->ti.d, b->ti.h, sizeof(PlaneItem) * ii, cudaMemcpyHostToDevice, b->stream));
-    if (si) FS3D_CUDA(cudaMemcpyAsync(b->to.d, b->to.h, sizeof(int) * si, cudaMemcpyHostToDevice, b->stream));
-    FS3D_CUDA(cudaMemcpyAsync(b->tn.d, b->tn.h, sizeof(int) * kMetaInts, cudaMemcpyHostToDevice,
-                              b->stream));
+    // the tables go up through small kernels reading the page-locked images,
+    // not the copy engines, which may be busy with hundreds of MB of grids
+    FS3D_CUDA(b->tw.upload(nw_, b->stream));
+    if (ii) FS3D_CUDA(b->ti.upload(ii, b->stream));
+    if (si) FS3D_CUDA(b->to.upload(si, b->stream));
+    FS3D_CUDA(b->tn.upload(kMetaInts, b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free[b->tab_cur], b->stream));
     if (b->cfg.use_graphs &&
         (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d)) {
@@ -1183,8 +1203,13 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         admitted = shared_event();
         e = admitted ? cudaEventRecord(admitted.get(), b->side) : cudaErrorMemoryAllocation;
         pa.converted = admitted;
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(pa.flags, flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
+        if (e == cudaSuccess) {
+            // the flags come down through a small kernel writing the page-locked
+            // buffer (a copy-engine transfer would queue behind the read-backs)
+            int* fv = reinterpret_cast<int*>(device_view(pa.flags));
+            e = fv ? copy_small_async(fv, flags_dev, sizeof(int) * (size_t)k, b->side)
+                   : cudaMemcpyAsync(pa.flags, flags_dev, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost, b->side);
+        }
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pa.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(pa.done, b->side);
         if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_admit_many conversion");

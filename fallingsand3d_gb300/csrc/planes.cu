@@ -1058,6 +1058,29 @@ __global__ void k_copy_many(const CopyJob* __restrict__ jobs, const int64_t* __r
     }
 }
 
+// A small copy done by the SMs (16-byte pieces, then the last bytes one by
+// one): either side may be page-locked host memory the device can address.
+__global__ void k_copy_small(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, size_t bytes) {
+    const size_t n16 = bytes / 16;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (size_t i = n16 * 16; i < bytes; ++i) dst[i] = src[i];
+}
+
+cudaError_t copy_small_async(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes == 0) return cudaSuccess;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) != 0)
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st);
+    const size_t n16 = bytes / 16;
+    const int64_t need = (int64_t)((n16 + 255) / 256), cap = (int64_t)sm_count_public() * 2;
+    const int grid = (int)(need < 1 ? 1 : (need < cap ? need : cap));
+    k_copy_small<<<grid, 256, 0, st>>>(static_cast<const uint8_t*>(src), static_cast<uint8_t*>(dst), bytes);
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) note_launch();
+    return e;
+}
+
 fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, int64_t total_chunks,
                       cudaStream_t st) {
     if (njobs <= 0 || total_chunks <= 0) return FS3D_OK;

@@ -116,6 +116,11 @@ struct CopyJob {
     int64_t bytes;
 };
 fs3d_status copy_many(const CopyJob* jobs, const int64_t* chunk_off, int njobs, int64_t total_chunks, cudaStream_t st);
+// A small copy (tables, flags) done by a kernel instead of a copy engine, so
+// it does not queue behind large transfers on the copy engines.  Both
+// pointers must be device-addressable (device memory, or the device view of
+// page-locked host memory); pointers not 16-byte aligned take cudaMemcpyAsync.
+cudaError_t copy_small_async(void* dst, const void* src, size_t bytes, cudaStream_t st);
 // A device-addressable alias of p (itself for device or managed memory, the
 // mapped address for page-locked host memory), or nullptr for pageable memory.
 uint8_t* device_view(const void* p);
