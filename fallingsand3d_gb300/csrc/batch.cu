@@ -959,25 +959,45 @@ fs3d_status fs3d_batch_poll_many(fs3d_batch* b, int n, const uint64_t* tickets, 
         if (w.ready) FS3D_CUDA(cudaStreamWaitEvent(b->side, w.ready, 0));
         jobs[(size_t)j] = HashJob{w.rows, w.statics, w.X, w.Y, w.Z, w.nw};
     }
+    // the kernel reads its jobs from, and writes the hashes into, one
+    // page-locked chunk: no allocation and no copy-engine transfer on the way
     const size_t jobs_bytes = (sizeof(HashJob) * (size_t)k + 15) / 16 * 16;
-    void* table = nullptr;
-    FS3D_CUDA(stream_alloc(&table, jobs_bytes + sizeof(unsigned long long) * (size_t)k, b->side));
-    unsigned long long* out_dev = reinterpret_cast<unsigned long long*>(static_cast<char*>(table) + jobs_bytes);
-    std::vector<unsigned long long> out((size_t)k);
-    cudaError_t e = cudaMemcpyAsync(table, jobs.data(), sizeof(HashJob) * (size_t)k, cudaMemcpyHostToDevice, b->side);
-    fs3d_status s = e == cudaSuccess ? planes_hash_many(static_cast<const HashJob*>(table), k, out_dev, b->side)
-                                     : cuda_fail(e, "fs3d_batch_poll_many jobs");
+    const size_t bytes = jobs_bytes + sizeof(unsigned long long) * (size_t)k;
+    const int ci = take_chunk(b, bytes);
+    if (ci < 0) return set_error(FS3D_ERR_CUDA, "fs3d_batch_poll_many: page-locked chunk");
+    fs3d_batch::HostChunk& c = b->host_chunks[(size_t)ci];
+    memcpy(c.p, jobs.data(), sizeof(HashJob) * (size_t)k);
+    const unsigned long long* out_host = reinterpret_cast<const unsigned long long*>(c.p + jobs_bytes);
+    fs3d_status s;
+    if (c.dv) {
+        s = planes_hash_many(reinterpret_cast<const HashJob*>(c.dv), k,
+                             reinterpret_cast<unsigned long long*>(c.dv + jobs_bytes), b->side);
+    } else {
+        // a chunk the device cannot address: through device memory
+        void* table = nullptr;
+        FS3D_CUDA(stream_alloc(&table, bytes, b->side));
+        cudaError_t e = cudaMemcpyAsync(table, c.p, jobs_bytes, cudaMemcpyHostToDevice, b->side);
+        s = e == cudaSuccess ? planes_hash_many(static_cast<const HashJob*>(table), k,
+                                                reinterpret_cast<unsigned long long*>(static_cast<char*>(table) +
+                                                                                      jobs_bytes),
+                                                b->side)
+                             : cuda_fail(e, "fs3d_batch_poll_many jobs");
+        if (s == FS3D_OK) {
+            e = cudaMemcpyAsync(c.p + jobs_bytes, static_cast<char*>(table) + jobs_bytes, bytes - jobs_bytes,
+                                cudaMemcpyDeviceToHost, b->side);
+            if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_poll_many hashes");
+        }
+        cudaFreeAsync(table, b->side);
+    }
     if (s == FS3D_OK) {
-        e = cudaMemcpyAsync(out.data(), out_dev, sizeof(unsigned long long) * (size_t)k, cudaMemcpyDeviceToHost,
-                            b->side);
+        cudaError_t e = cudaEventRecord(c.uploaded, b->side);  // the chunk is in use until here
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->side);
         if (e != cudaSuccess) s = cuda_fail(e, "fs3d_batch_poll_many hashes");
     }
-    cudaFreeAsync(table, b->side);
     if (s != FS3D_OK) return s;
     for (int j = 0; j < k; ++j) {
         BWorld& w = *need[(size_t)j];
-        w.hash = out[(size_t)j];
+        w.hash = out_host[j];
         w.hash_valid = true;
         hashes[need_at[(size_t)j]] = w.hash;
     }
