@@ -45,7 +45,7 @@ EXPORTS = (
     "fs3d_world_destroy", "fs3d_world_save", "fs3d_world_load", "fs3d_batch_create", "fs3d_batch_admit", "fs3d_batch_admit_generated", "fs3d_batch_admit_many",
     "fs3d_batch_retire_many", "fs3d_batch_admit_many_async", "fs3d_batch_retire_many_async", "fs3d_batch_wait_copies",
     "fs3d_batch_read_many",
-    "fs3d_batch_run_segment", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_poll_many", "fs3d_batch_retire",
+    "fs3d_batch_run_segment", "fs3d_batch_prepare", "fs3d_batch_sync", "fs3d_batch_poll", "fs3d_batch_poll_many", "fs3d_batch_retire",
     "fs3d_batch_stats", "fs3d_batch_counters", "fs3d_batch_autotune", "fs3d_batch_stream", "fs3d_batch_destroy", "fs3d_serve_plan", "fs3d_serve_run", "fs3d_render", "fs3d_render_sdf",
     "fs3d_camera_fs_raymarch", "fs3d_camera_world_view", "fs3d_object_view_scene", "fs3d_mesh_cube",
     "fs3d_render_object", "fs3d_render_meshes", "fs3d_gen_parity", "fs3d_gen_pillars",
@@ -168,6 +168,7 @@ def _bind(lib: C.CDLL) -> None:
         "fs3d_batch_wait_copies": (S, [vp, i64]),
         "fs3d_batch_read_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(vp)]),
         "fs3d_batch_run_segment": (S, [vp]),
+        "fs3d_batch_prepare": (S, [vp]),
         "fs3d_batch_sync": (S, [vp, i64]),
         "fs3d_batch_poll": (S, [vp, u64, C.POINTER(i32), C.POINTER(u64)]),
         "fs3d_batch_poll_many": (S, [vp, i32, C.POINTER(u64), C.POINTER(i32), C.POINTER(u64)]),
@@ -595,6 +596,10 @@ class Batch:
 
     def run_segment(self) -> None:
         check(lib().fs3d_batch_run_segment(self.handle))
+
+    def prepare(self) -> None:
+        """Builds the next segment's tables now (fs3d_batch_prepare)."""
+        check(lib().fs3d_batch_prepare(self.handle))
 
     def sync(self, timeout_ns: int = -1) -> None:
         check(lib().fs3d_batch_sync(self.handle, timeout_ns))

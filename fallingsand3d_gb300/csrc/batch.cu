@@ -36,6 +36,8 @@ namespace {
 
 struct BWorld {
     int X = 0, Y = 0, Z = 0, nw = 0;
+    // the classes that hold the world (they depend on its dims only), looked up once
+    mutable int cls_smem = -2, cls_gm = -2;
     uint64_t seed = 0, t = 0;
     int64_t remaining = 0;
     uint4* rows = nullptr;
@@ -215,6 +217,7 @@ struct fs3d_batch {
     // retired, changes class, or takes fewer steps than a full segment:
     // `reuse_left` more segments may launch without rebuilding them.
     bool tables_stale = true;
+    bool prepared = false;  // fs3d_batch_prepare built the next segment's tables
     uint64_t reuse_left = 0;
     std::vector<BWorld*> running;  // the worlds of the tables, in table order
     size_t table_items = 0;        // per-step kernel items in the tables
@@ -240,12 +243,14 @@ constexpr uint64_t kYoungSteps = 128;
 int segment_class(const fs3d_batch* b, const BWorld& w) {
     const int mode = b->cfg.use_smem;
     auto smem = [&]() {
-        int c = resident_class(w.X, w.Y, w.Z);
+        if (w.cls_smem == -2) w.cls_smem = resident_class(w.X, w.Y, w.Z);
+        int c = w.cls_smem;
         if (mode == 1 && c >= 0 && c < kSingleCtaClasses) c = std::min(c + b->promote, kSingleCtaClasses - 1);
         return c;
     };
     auto gm = [&]() {
-        const int c = resident_class_gm(w.X, w.Y, w.Z);
+        if (w.cls_gm == -2) w.cls_gm = resident_class_gm(w.X, w.Y, w.Z);
+        const int c = w.cls_gm;
         return c < 0 ? -1 : kResidentClasses + std::min(c + b->promote, kGmDense - 1);
     };
     if (mode == 1) return smem();
@@ -831,12 +836,26 @@ fs3d_status build_tables(fs3d_batch* b) {
 
 extern "C" {
 
+fs3d_status fs3d_batch_prepare(fs3d_batch* b) {
+    if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_prepare: NULL batch");
+    if (b->prepared && !b->tables_stale) return FS3D_OK;
+    // an unchanged batch whose tables hold for another segment needs nothing
+    if (!b->tables_stale && b->reuse_left > 0 && !b->running.empty()) return FS3D_OK;
+    const fs3d_status s = build_tables(b);
+    b->prepared = s == FS3D_OK;
+    return s;
+}
+
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     if (!b) return set_error(FS3D_ERR_INVALID_ARG, "fs3d_batch_run_segment: NULL batch");
     const int S = b->cfg.steps_per_segment;
-    if (!b->tables_stale && b->reuse_left > 0 && !b->running.empty()) {
+    if (b->prepared && !b->tables_stale) {
+        b->prepared = false;  // the tables fs3d_batch_prepare built are this segment's
+        if (b->running.empty()) return FS3D_OK;
+    } else if (!b->tables_stale && b->reuse_left > 0 && !b->running.empty()) {
         --b->reuse_left;  // the tables on the device are this segment's
     } else {
+        b->prepared = false;
         const fs3d_status s = build_tables(b);
         if (s != FS3D_OK) return s;
         if (b->running.empty()) return FS3D_OK;

@@ -210,6 +210,12 @@ fs3d_status fs3d_batch_admit_many(fs3d_batch* b, int n, const fs3d_world_spec* s
 fs3d_status fs3d_batch_admit_many_async(fs3d_batch* b, int n, const fs3d_world_spec* specs, uint64_t* tickets,
                                         int* n_admitted);
 fs3d_status fs3d_batch_run_segment(fs3d_batch* b); /* async on the batch stream */
+/* Builds and uploads the next segment's tables now (host work and small
+ * uploads on the batch stream), so the next fs3d_batch_run_segment only
+ * launches it: a caller overlaps the build with a segment still running.
+ * An admission or retirement in between makes the next segment build them
+ * again.  No counterpart in the upstream project. */
+fs3d_status fs3d_batch_prepare(fs3d_batch* b);
 fs3d_status fs3d_batch_sync(fs3d_batch* b, int64_t timeout_ns);
 /* done = 1 once the world has taken all its steps; hash valid when done */
 fs3d_status fs3d_batch_poll(fs3d_batch* b, uint64_t ticket, int* done, uint64_t* hash);

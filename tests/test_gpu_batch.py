@@ -649,3 +649,30 @@ def test_poll_many_matches_single_polls_and_oracle(fs3d, orc):
         rest = [t for t, d in zip(ts, done) if not d]
         done2, hs2 = b.poll_many(rest)
         assert done2.all()
+
+
+def test_prepare_builds_tables_ahead_and_stays_exact(fs3d, orc):
+    """fs3d_batch_prepare builds the next segment's tables while a segment is
+    still running; an admission after it makes the segment build them again.
+    Every world equals the oracle."""
+    S = 16
+    worlds = small_batch(fs3d, 81, 10, max_dim=64)
+    steps = [S * 4, S * 3, S * 4, S * 2, 40, S * 4, 25, S * 4, S * 3, S * 4]
+    with fs3d.Batch(GiB, steps_per_segment=S) as b:
+        ts = [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for (dims, seed), n in zip(worlds[:8], steps[:8])]
+        b.prepare()
+        b.run_segment()
+        b.prepare()      # built while the first segment may still run
+        b.run_segment()
+        b.prepare()
+        # an admission after the prepare: the next segment rebuilds its tables
+        ts += [b.admit(fs3d.gen_batch_world(seed, *dims), seed, n) for (dims, seed), n in zip(worlds[8:], steps[8:])]
+        for _ in range(4):
+            b.run_segment()
+            b.prepare()
+        b.run_segment()
+        b.sync()
+        for t, (dims, seed), n in zip(ts, worlds, steps):
+            done, h = b.poll(t)
+            assert done
+            assert h == orc.hash(oracle_final(orc, fs3d, dims, seed, n)), (dims, n)
