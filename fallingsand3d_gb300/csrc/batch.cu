@@ -44,7 +44,7 @@ struct BWorld {
     std::shared_ptr<void> arena;  // set when rows live in a block shared by the worlds of one admit_many
     uint8_t* statics = nullptr;
     uint8_t* lflags = nullptr;  // layer flags after the planes (same allocation)
-    bool flags_valid = false;   // kept up to date by every segment that stepped the world
+    bool flags_valid = false;   // set from the cells at admission, then kept by every resident segment
     size_t bytes = 0;
     bool done = false;
     cudaEvent_t ready = nullptr;     // admission finished (side stream)
@@ -495,9 +495,13 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
     // ones first (the dense global-memory class, then the shared-memory
     // classes widest first), since they take the longest; settled worlds: the
     // global-memory classes smallest CTA first, whose chains are the longest.
+    // In a graph the branches' kernels are all pending at once and the launch
+    // order alone does not decide which grid is placed first: the dense class
+    // carries the greatest priority.
     auto gm = [&](int c) {
         return launch_plane_segment_gm(c, b->tw.d, b->to.d, b->tn.d, b->counter + kResidentClasses + c, b->err,
-                                       fork ? b->branch[kResidentClasses + c] : a, b->processed_dev);
+                                       fork ? b->branch[kResidentClasses + c] : a, b->processed_dev,
+                                       mode == 3 && c == kGmDense);
     };
     if (mode == 3) s = gm(kGmDense);
     if (mode == 1 || mode == 3)
@@ -668,6 +672,10 @@ fs3d_status admit(fs3d_batch* b, const uint8_t* g, int X, int Y, int Z, uint64_t
     } else {
         s = planes_generate_batch_world(seed, X, Y, Z, w.rows, b->side);
     }
+    // layer flags from the cells: the first two steps evaluate only the
+    // row-pairs that can change
+    if (s == FS3D_OK) s = layer_flags_from_cells(w.rows, w.lflags, X, Y, Z, start_step, b->side);
+    w.flags_valid = s == FS3D_OK;
     if (s == FS3D_OK) {
         e = cudaEventCreateWithFlags(&w.ready, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(w.ready, b->side);
@@ -1197,7 +1205,14 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         }
         a = e_run;
     }
-    for (int a = 0; a < k; ++a) jobs[(size_t)a].rows = rows[(size_t)a];
+    int max_Y = 0;
+    for (int a = 0; a < k; ++a) {
+        ConvJob& j = jobs[(size_t)a];
+        j.rows = rows[(size_t)a];
+        j.lflags = reinterpret_cast<uint8_t*>(j.rows) + plane_bytes(j.X, j.Y, j.Z);
+        j.t0b = (uint32_t)specs[a].start_step & 0xFFu;
+        max_Y = std::max(max_Y, j.Y);
+    }
     // the conversion (admission stream) follows the uploads
     if (e == cudaSuccess) {
         cudaEvent_t uploaded = nullptr;
@@ -1236,6 +1251,8 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
     if (s == FS3D_OK) s = copy_many(copies_dev, chunk_dev, (int)copies.size(), chunks, b->side);
     const int* bj_dev = reinterpret_cast<const int*>(static_cast<char*>(pa.table) + bj_off);
     if (s == FS3D_OK) s = planes_from_bytes_multi(jobs_dev, off_dev, bj_dev, k, units, staging, flags_dev, b->side);
+    // layer flags from the cells: the first two steps evaluate only the row-pairs that can change
+    if (s == FS3D_OK) s = layer_flags_from_cells_multi(jobs_dev, k, max_Y, b->side);
     // segments may start once the planes are written
     std::shared_ptr<CUevent_st> admitted;
     if (s == FS3D_OK) {
@@ -1279,6 +1296,7 @@ fs3d_status admit_many_impl(fs3d_batch* b, int n, const fs3d_world_spec* specs, 
         w.rows = rows[(size_t)a];
         w.arena = arena;
         w.lflags = reinterpret_cast<uint8_t*>(w.rows) + plane_bytes(p.X, p.Y, p.Z);
+        w.flags_valid = true;
         w.bytes = plane_bytes(p.X, p.Y, p.Z) + layer_flag_bytes(p.Y) + sizeof(PlaneWorld);
         w.admit_id = pa.id;
         w.admit_index = a;

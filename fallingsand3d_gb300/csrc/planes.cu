@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "fs3d_common.h"
@@ -436,6 +437,89 @@ __global__ void __launch_bounds__(256, 3) k_plane_step_skip(const PlaneWorld w, 
 }
 
 // ---------------------------------------------------------------------------
+// change flags of a world with no history, from its cells
+// ---------------------------------------------------------------------------
+// A world admitted (or loaded, or written) at step t0 has no record of its
+// last changes.  Marking every layer or row changed at t0 - 1 makes its first
+// two steps evaluate every row-pair.  Instead a layer or row is marked changed
+// at t0 - 1 only when a block row-pair of either phase that covers it can
+// change (rowpair_can_change), and at t0 - 3 (two steps before the window the
+// skip reads) otherwise.  Exact: at t0 and t0 + 1 a skipped pair has no block
+// that can change and no row of it changed since t0 (at t0 + 1 a change at t0
+// marks it); from t0 + 2 on the skip's usual argument holds, since a pair not
+// evaluated at t0 could not change then.
+
+// the four rows of block row-pair (j, k) of phase o for lane gl, solid outside the world
+__device__ __forceinline__ void load_rowpair(const uint4* __restrict__ rows, int Y, int Z, int nw, int y0, int z0,
+                                             int gl, bool has, uint4 (&q)[4]) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+        const bool in = has && y >= 0 && y < Y && z >= 0 && z < Z;
+        q[a] = in ? rows[((int64_t)y * Z + z) * nw + gl] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    }
+}
+
+__device__ __forceinline__ int lanes_lg(int nw) { return nw <= 1 ? 0 : 32 - __clz(nw - 1); }
+
+// One warp per layer y of each job (blockIdx.x: job, blockIdx.y * 8 + warp: y).
+// `one` stands for the job table when jobs is null.
+__global__ void __launch_bounds__(256) k_layer_flags_from_cells(const ConvJob* __restrict__ jobs, ConvJob one) {
+    const ConvJob jb = jobs ? jobs[blockIdx.x] : one;
+    const int y = (int)blockIdx.y * 8 + (int)(threadIdx.x >> 5);
+    if (!jb.lflags || y >= jb.Y) return;  // warp-uniform
+    const int lane = threadIdx.x & 31, lg = lanes_lg(jb.nw);
+    const int G = 1 << lg, per = 32 >> lg, gl = lane & (G - 1), gi = lane >> lg;
+    const bool half_at_end = (jb.X & 63) == 0;
+    bool any = false;
+    for (int o = 0; o < 2 && !any; ++o) {
+        const int y0 = 2 * ((y + o) >> 1) - o;  // the pair of phase o covering y: layers y0, y0 + 1
+        const int nbz = nblocks(jb.Z, o);
+        for (int k0 = 0; k0 < nbz && !any; k0 += per) {
+            const int k = k0 + gi;
+            const bool has = k < nbz && gl < jb.nw;
+            uint4 q[4];
+            load_rowpair(jb.rows, jb.Y, jb.Z, jb.nw, y0, 2 * k - o, gl, has, q);
+            any = __any_sync(0xFFFFFFFFu, rowpair_can_change(q, has, o, gl, G, jb.nw, half_at_end));
+        }
+    }
+    if (lane == 0) jb.lflags[y] = (uint8_t)(jb.t0b - (any ? 1u : 3u));
+}
+
+// Row flags, already set to t0 - 3: every block row-pair of both phases that
+// can change marks its rows changed at t0 - 1 (rows shared by two such pairs
+// get the same value from both).
+__global__ void __launch_bounds__(256) k_row_flags_from_cells(const uint4* __restrict__ rows,
+                                                              uint8_t* __restrict__ rflags, int X, int Y, int Z,
+                                                              int nw, uint32_t t0b) {
+    const int lane = threadIdx.x & 31, lg = lanes_lg(nw);
+    const int G = 1 << lg, per = 32 >> lg, gl = lane & (G - 1), gi = lane >> lg;
+    const uint32_t gmask = G == 32 ? 0xFFFFFFFFu : ((1u << G) - 1u) << (lane & ~(G - 1));
+    const bool half_at_end = (X & 63) == 0;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (int o = 0; o < 2; ++o) {
+        const int nbz = nblocks(Z, o), chunks = (nbz + per - 1) / per;
+        const int64_t items = (int64_t)nblocks(Y, o) * chunks;
+        for (int64_t it = first; it < items; it += warps) {
+            const int j = (int)(it / chunks), k = (int)(it - (int64_t)j * chunks) * per + gi;
+            const int y0 = 2 * j - o, z0 = 2 * k - o;
+            const bool has = k < nbz && gl < nw;
+            uint4 q[4];
+            load_rowpair(rows, Y, Z, nw, y0, z0, gl, has, q);
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, rowpair_can_change(q, has, o, gl, G, nw, half_at_end));
+            if (gl == 0 && k < nbz && (m & gmask)) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
+                    if (y >= 0 && y < Y && z >= 0 && z < Z) rflags[(int64_t)y * Z + z] = (uint8_t)(t0b - 1u);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // shared-memory resident segment: one CTA steps one whole world
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -576,29 +660,24 @@ __device__ __forceinline__ bool layer_dirty(const SlabView<CL>& v, const PlaneWo
 
 // Evaluates block row-pair (j, k) of a world held in shared memory when `run`
 // is set.  Every lane of the warp calls this together (the odd phase passes
-// carry bits between lanes).  Layers with a changed row get the step's flag;
-// the cells evaluated are added to *s_processed.
+// carry bits between lanes).  Layers with a changed row get the step's flag.
 template <bool CL>
 __device__ __forceinline__ void slab_rowpair(const SlabView<CL>& v, const PlaneWorld& w, int o, uint32_t sk,
                                              uint32_t tt /* step & 3 */, int j, int k, bool run, int gl,
-                                             int G, unsigned long long* s_processed) {
+                                             int G) {
     if (!__any_sync(0xFFFFFFFFu, run)) return;
     const int y0 = 2 * j - o, z0 = 2 * k - o;
     const uint32_t rk = rowkey(sk, (uint32_t)j, (uint32_t)k);
     const bool has = run && gl < w.nw;
     uint4 q[4], q0[4];
     uint4* ptr[4];
-    uint32_t rows_in = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int y = (a < 2) ? y0 + 1 : y0, z = z0 + (a & 1);
         ptr[a] = (has && y >= 0 && y < w.Y && z >= 0 && z < w.Z) ? v.at(y, z, gl) : nullptr;
         q[a] = ptr[a] ? *ptr[a] : make_uint4(0u, 0u, 0xFFFFFFFFu, 0xFFFFFFFFu);
         q0[a] = q[a];
-        rows_in += ptr[a] ? 1u : 0u;
     }
-    const uint32_t cells = __reduce_add_sync(0xFFFFFFFFu, has ? rows_in * (uint32_t)min(64, w.X - 64 * gl) : 0u);
-    if ((threadIdx.x & 31) == 0 && cells) atomicAdd(s_processed, (unsigned long long)cells);
     rowpair_core(q, has, o, rk, gl, G, w.nw, (w.X & 63) == 0);
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -763,16 +842,31 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
                 __syncthreads();
                 n_layers = *cnt;
             }
-            if (threadIdx.x == 0) s_count[(s + 1) & 1] = 0;  // the next step's counter (read before this step)
+            if (threadIdx.x == 0) {
+                s_count[(s + 1) & 1] = 0;  // the next step's counter (read before this step)
+                // cells evaluated: the rows of every dirty layer pair inside the world, X*Z cells each
+                int rows = 2 * n_layers;
+                if (n_layers) {
+                    if (2 * j_lo - o < 0 && layer_dirty(v, w, o, tb, j_lo)) --rows;
+                    if (2 * (j_hi - 1) - o + 1 >= w.Y && layer_dirty(v, w, o, tb, j_hi - 1)) --rows;
+                }
+                s_processed += (unsigned long long)rows * (unsigned long long)(w.X * w.Z);
+            }
             const int npairs = n_layers * NBZ;
+            // e / NBZ as a multiply-high: exact for e, NBZ < 2^16
+            const uint32_t nbz_magic = 0xFFFFFFFFu / (uint32_t)NBZ + 1u;
             for (int base = 0; base < npairs; base += per) {
                 const int e = base + (int)(threadIdx.x >> w.lg);
                 const bool valid = e < npairs;
-                const int jd = valid ? e / NBZ : 0, kk = valid ? e - jd * NBZ : 0;
+                const int jd =
+                    valid ? (NBZ == 1 ? e : (npairs <= 65536 ? (int)__umulhi((uint32_t)e, nbz_magic) : e / NBZ)) : 0;
+                const int kk = valid ? e - jd * NBZ : 0;
                 int jj = 0;
                 if (valid) {
                     if (!masked)
                         jj = (int)jlist[jd];
+                    else if (jd == 0 && dm0)
+                        jj = __ffs(dm0) - 1;
                     else if (jd < __popc(dm0))
                         jj = select_bit(dm0, jd);
                     else if (jd < __popc(dm0) + __popc(dm1))
@@ -780,7 +874,7 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
                     else
                         jj = 64 + select_bit(dm2, jd - __popc(dm0) - __popc(dm1));
                 }
-                slab_rowpair(v, w, o, sk, tb, j_lo + jj, kk, valid, gl, G, &s_processed);
+                slab_rowpair(v, w, o, sk, tb, j_lo + jj, kk, valid, gl, G);
             }
             group_sync();
         }
@@ -897,14 +991,30 @@ int resident_class_gm(int X, int Y, int Z) {
 template <int NT>
 static cudaError_t launch_gm(int cls, int grid, size_t smem, cudaStream_t st, const PlaneWorld* worlds,
                              const int* order, const int* meta, int* counter, int* err,
-                             unsigned long long* processed_cells) {
-    k_plane_segment_resident<NT, false, true>
-        <<<grid, NT, smem, st>>>(worlds, order, meta, kResidentClasses + cls, 1, counter, err, processed_cells);
-    return cudaGetLastError();
+                             unsigned long long* processed_cells, bool first) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3((unsigned)NT);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (first) {
+        // the greatest priority: its CTAs take the SMs before the other
+        // classes' grids, which are pending at the same moment in a segment graph
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        attr[0].id = cudaLaunchAttributePriority;
+        attr[0].val.priority = greatest;
+    }
+    lc.attrs = attr;
+    lc.numAttrs = first ? 1 : 0;
+    return cudaLaunchKernelEx(&lc, k_plane_segment_resident<NT, false, true>, worlds, order, meta,
+                              kResidentClasses + cls, 1, counter, err, processed_cells);
 }
 
 fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
-                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells) {
+                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells,
+                                    bool first) {
     if (cls < 0 || cls >= kGmClasses) return set_error(FS3D_ERR_INVALID_ARG, "global-memory class out of range");
     std::call_once(g_gm_once, [] {
         // the planes are read through L1: leave most of the unified memory to it
@@ -922,15 +1032,15 @@ fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int
     const size_t smem = slab_aux_bytes((uint32_t)kGmMaxY[cls]);
     cudaError_t e;
     if (nt == 32)
-        e = launch_gm<32>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+        e = launch_gm<32>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells, first);
     else if (nt == 64)
-        e = launch_gm<64>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+        e = launch_gm<64>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells, first);
     else if (nt == 128)
-        e = launch_gm<128>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+        e = launch_gm<128>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells, first);
     else if (nt == 256)
-        e = launch_gm<256>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+        e = launch_gm<256>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells, first);
     else
-        e = launch_gm<768>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells);
+        e = launch_gm<768>(cls, grid, smem, st, worlds, order, meta, counter, err, processed_cells, first);
     if (e != cudaSuccess) return cuda_fail(e, "global-memory segment launch");
     note_launch();
     return FS3D_OK;
@@ -1190,8 +1300,39 @@ fs3d_status launch_advance_worlds(PlaneWorld* worlds, const int* meta, cudaStrea
     return FS3D_OK;
 }
 
-fs3d_status init_row_flags(uint8_t* rflags, int Y, int Z, uint64_t t0, cudaStream_t st) {
-    FS3D_CUDA(cudaMemsetAsync(rflags, (int)((t0 - 1u) & 0xFFu), (size_t)Y * (size_t)Z, st));
+fs3d_status init_row_flags(const uint4* rows, uint8_t* rflags, int X, int Y, int Z, uint64_t t0, cudaStream_t st) {
+    FS3D_CUDA(cudaMemsetAsync(rflags, (int)((t0 - 3u) & 0xFFu), (size_t)Y * (size_t)Z, st));
+    const int nw = plane_nw(X), per = 32 >> plane_lg(nw);
+    const int64_t items = (int64_t)nblocks(Y, 0) * ((nblocks(Z, 0) + per - 1) / per);  // the larger phase's
+    const int64_t blocks = std::min<int64_t>((items + 7) / 8, (int64_t)sm_count_public() * 8);
+    k_row_flags_from_cells<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(rows, rflags, X, Y, Z, nw,
+                                                                                   (uint32_t)t0 & 0xFFu);
+    FS3D_CUDA(cudaGetLastError());
+    note_launch();
+    return FS3D_OK;
+}
+
+fs3d_status layer_flags_from_cells_multi(const ConvJob* jobs, int njobs, int max_Y, cudaStream_t st) {
+    if (njobs <= 0 || max_Y <= 0) return FS3D_OK;
+    k_layer_flags_from_cells<<<dim3((unsigned)njobs, (unsigned)((max_Y + 7) / 8)), 256, 0, st>>>(jobs, ConvJob{});
+    FS3D_CUDA(cudaGetLastError());
+    note_launch();
+    return FS3D_OK;
+}
+
+fs3d_status layer_flags_from_cells(const uint4* rows, uint8_t* lflags, int X, int Y, int Z, uint64_t t0,
+                                   cudaStream_t st) {
+    ConvJob one{};
+    one.rows = const_cast<uint4*>(rows);
+    one.X = X;
+    one.Y = Y;
+    one.Z = Z;
+    one.nw = plane_nw(X);
+    one.lflags = lflags;
+    one.t0b = (uint32_t)t0 & 0xFFu;
+    k_layer_flags_from_cells<<<dim3(1u, (unsigned)((Y + 7) / 8)), 256, 0, st>>>(nullptr, one);
+    FS3D_CUDA(cudaGetLastError());
+    note_launch();
     return FS3D_OK;
 }
 

@@ -74,8 +74,11 @@ fs3d_status launch_plane_segment_resident(int cls, const PlaneWorld* worlds, con
                                           int* counter, int* err, cudaStream_t st,
                                           unsigned long long* processed_cells = nullptr);
 
+// `first`: launched with the greatest priority, so that in a segment graph,
+// where every class's grid is pending at once, its CTAs are placed first.
 fs3d_status launch_plane_segment_gm(int cls, const PlaneWorld* worlds, const int* order, const int* meta,
-                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells);
+                                    int* counter, int* err, cudaStream_t st, unsigned long long* processed_cells,
+                                    bool first = false);
 
 // One world of a many-world conversion: its planes, its static bytes
 // (nullable) and the offset of its canonical bytes in a shared staging buffer.
@@ -88,6 +91,10 @@ struct ConvJob {
     // host yet: when *static_flag is set, its static bytes are at static_src
     const int* static_flag;
     const uint8_t* static_src;
+    // admission: the world's layer flags (set from its cells by
+    // layer_flags_from_cells_multi; null: none) and its first step's low 8 bits
+    uint8_t* lflags = nullptr;
+    uint32_t t0b = 0;
 };
 // bytes -> planes for njobs worlds in one launch; unit_off[j] = sum of Y*Z*nw
 // over jobs before j; block_job[i] = the job of unit kConvBlock*i (from
@@ -144,8 +151,18 @@ fs3d_status planes_to_bytes(const uint4* rows, const uint8_t* statics, int X, in
 // ---- per-step kernel of one large world with an exact skip of settled
 // row-pairs: one byte per row (y, z) holds the low 8 bits of the last step
 // that changed it (Y*Z bytes).  init_row_flags: a world about to take step t0
-// with no history (every row changed at t0 - 1).
-fs3d_status init_row_flags(uint8_t* rflags, int Y, int Z, uint64_t t0, cudaStream_t st);
+// with no history: a row is marked changed at t0 - 1 when a block row-pair of
+// either phase that covers it can change (the rule's activity mask on its
+// cells), else at t0 - 3.
+fs3d_status init_row_flags(const uint4* rows, uint8_t* rflags, int X, int Y, int Z, uint64_t t0, cudaStream_t st);
+
+// Layer flags of newly admitted worlds (jobs with lflags set), the same way
+// per layer: marked changed at t0 - 1 when a block row-pair of either phase
+// covering the layer can change, else at t0 - 3.  max_Y: the largest Y of the jobs.
+fs3d_status layer_flags_from_cells_multi(const ConvJob* jobs, int njobs, int max_Y, cudaStream_t st);
+// the same for one world
+fs3d_status layer_flags_from_cells(const uint4* rows, uint8_t* lflags, int X, int Y, int Z, uint64_t t0,
+                                   cudaStream_t st);
 // one step (w.t) of the world; counts as for launch_plane_step
 fs3d_status launch_plane_step_skip(const PlaneWorld& w, uint8_t* rflags, int* counts, cudaStream_t st);
 fs3d_status planes_hash_async(const uint4* rows, const uint8_t* statics, int X, int Y, int Z,

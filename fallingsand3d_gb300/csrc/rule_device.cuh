@@ -133,6 +133,17 @@ __device__ __forceinline__ void bs_select(uint32_t mov, uint32_t c1, uint32_t c2
 // The three other columns of q, in increasing order.
 __host__ __device__ constexpr int other_col(int q, int n) { return n < q ? n : n + 1; }
 
+// The rule's activity mask of 32 blocks (W = water, E = empty per slot): the
+// blocks with a particle that has an empty candidate (a top particle over an
+// empty bottom cell, or water beside an empty cell of its layer).  A block
+// outside the mask does not change, whatever the draws; a block in it does.
+__device__ __forceinline__ uint32_t activity_mask(const uint32_t (&A)[8], const uint32_t (&W)[8],
+                                                  const uint32_t (&E)[8]) {
+    const uint32_t etop = E[0] | E[1] | E[2] | E[3], ebot = E[4] | E[5] | E[6] | E[7];
+    return ((A[0] | A[1] | A[2] | A[3]) & ebot) | ((W[0] | W[1] | W[2] | W[3]) & etop) |
+           ((W[4] | W[5] | W[6] | W[7]) & ebot);
+}
+
 // Runs one step of the rule on 32 blocks.  A[s], B[s] in/out per slot s.
 // Returns the mask of blocks that changed.
 __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], uint32_t rk, uint32_t g) {
@@ -147,9 +158,7 @@ __device__ __forceinline__ uint32_t bs_rule(uint32_t (&A)[8], uint32_t (&B)[8], 
         W[s] = A[s] & B[s];
         E[s] = ~(A[s] | B[s]);
     }
-    const uint32_t etop = E[0] | E[1] | E[2] | E[3], ebot = E[4] | E[5] | E[6] | E[7];
-    const uint32_t active = ((A[0] | A[1] | A[2] | A[3]) & ebot) | ((W[0] | W[1] | W[2] | W[3]) & etop) |
-                            ((W[4] | W[5] | W[6] | W[7]) & ebot);
+    const uint32_t active = activity_mask(A, W, E);
     if (!active) return 0u;
 #pragma unroll
     for (int s = 0; s < 8; ++s) B[s] = ~A[s] & B[s];  // from here on B holds the solids, which never change
@@ -239,19 +248,11 @@ __device__ __forceinline__ void half_block_rule(uint32_t& P, uint32_t& W, uint32
     }
 }
 
-// One step of one block row-pair held as plane words.  The pair's four rows
-// (a = layer*2 + dz: top z0, top z1, bottom z0, bottom z1) cover x in
-// [64*gl, 64*gl+64): lane gl of a group of G consecutive lanes (G a power of
-// two; every lane of the warp must call this together, `has` false for lanes
-// without a word).  q[a] = {A even, A odd, B even, B odd}, updated in place;
-// rows outside the world are passed as solid.  In the odd phase the dx=0 word
-// is the odd word shifted up one bit with bit 31 of the left lane's odd word
-// carried in (x = -1 is solid), and the left lane receives its new bit 31
-// back; when the row width is a multiple of 64 (`half_at_end`) the last lane
-// also runs the half block at x = 64*nw - 1.
-__device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uint32_t rk, int gl, int G, int nw,
-                                             bool half_at_end) {
-    uint32_t A[8], B[8];
+// The bit-sliced slots (A, B per slot) of the 32 blocks of a block row-pair
+// that lane gl holds, in the layout rowpair_core describes.  Every lane of the
+// warp calls this together (the odd phase takes a bit from the left lane).
+__device__ __forceinline__ void rowpair_slots(const uint4 (&q)[4], int o, int gl, int G, uint32_t (&A)[8],
+                                              uint32_t (&B)[8]) {
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int s0 = (a >> 1) * 4 + (a & 1) * 2;
@@ -276,6 +277,22 @@ __device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uin
             B[s0 + 1] = q[a].z;
         }
     }
+}
+
+// One step of one block row-pair held as plane words.  The pair's four rows
+// (a = layer*2 + dz: top z0, top z1, bottom z0, bottom z1) cover x in
+// [64*gl, 64*gl+64): lane gl of a group of G consecutive lanes (G a power of
+// two; every lane of the warp must call this together, `has` false for lanes
+// without a word).  q[a] = {A even, A odd, B even, B odd}, updated in place;
+// rows outside the world are passed as solid.  In the odd phase the dx=0 word
+// is the odd word shifted up one bit with bit 31 of the left lane's odd word
+// carried in (x = -1 is solid), and the left lane receives its new bit 31
+// back; when the row width is a multiple of 64 (`half_at_end`) the last lane
+// also runs the half block at x = 64*nw - 1.
+__device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uint32_t rk, int gl, int G, int nw,
+                                             bool half_at_end) {
+    uint32_t A[8], B[8];
+    rowpair_slots(q, o, gl, G, A, B);
     if (has) bs_rule(A, B, rk, (uint32_t)gl);
     if (o == 0) {
 #pragma unroll
@@ -313,6 +330,33 @@ __device__ __forceinline__ void rowpair_core(uint4 (&q)[4], bool has, int o, uin
         }
         q[a] = make_uint4(A[s0 + 1], (A[s0] >> 1) | (na << 31), B[s0 + 1], (B[s0] >> 1) | (nb << 31));
     }
+}
+
+// Whether lane gl's blocks of a block row-pair (q as for rowpair_core, only
+// read) can change in phase o: the rule's activity mask, and for the half
+// block at the end of an odd-phase row (`half_at_end`, last lane) a particle
+// and an empty cell in it (a superset of its moves).  Every lane of the warp
+// calls this together; lanes with `has` false answer false.
+__device__ __forceinline__ bool rowpair_can_change(const uint4 (&q)[4], bool has, int o, int gl, int G, int nw,
+                                                   bool half_at_end) {
+    uint32_t A[8], B[8], W[8], E[8];
+    rowpair_slots(q, o, gl, G, A, B);
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        W[s] = A[s] & B[s];
+        E[s] = ~(A[s] | B[s]);
+    }
+    bool can = has && activity_mask(A, W, E) != 0u;
+    if (o == 1 && has && half_at_end && gl == nw - 1) {
+        uint32_t ta = 0, tb = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            ta |= (q[a].y >> 31) << a;
+            tb |= (q[a].w >> 31) << a;
+        }
+        if (ta != 0u && (~(ta | tb) & 0xFu) != 0u) can = true;
+    }
+    return can;
 }
 
 }  // namespace fs3d

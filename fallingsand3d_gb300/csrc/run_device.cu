@@ -110,7 +110,7 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
         if (cls >= 0) {
             s = launch_plane_segment_resident(cls, sc.desc, sc.ints + kOrder, sc.ints, sc.ints + kCounter, err, st);
         } else {
-            s = init_row_flags(rflags, Y, Z, t0, st);
+            s = init_row_flags(sc.rows, rflags, X, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = t0 + (uint64_t)a;
                 s = launch_plane_step_skip(d, rflags, nullptr, st);

@@ -147,7 +147,7 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
             s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, err, st);
         } else {
             uint8_t* rflags = base + kFlagsOff;
-            s = init_row_flags(rflags, Y, Z, t0, st);
+            s = init_row_flags(rows, rflags, X, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = t0 + (uint64_t)a;
                 s = launch_plane_step_skip(d, rflags, nullptr, st);

@@ -197,7 +197,7 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
             // world since.  Once a frame has counted the bricks, the kernel
             // keeps the counts exact, so later frames read no pass over the planes
             if (!w->flags_ok || w->flags_t != w->step) {
-                s = init_row_flags(w->rflags, w->Y, w->Z, w->step, w->stream);
+                s = init_row_flags(w->rows, w->rflags, w->X, w->Y, w->Z, w->step, w->stream);
                 w->flags_ok = s == FS3D_OK;
             }
             int* counts = w->counts_valid ? w->brick_counts : nullptr;

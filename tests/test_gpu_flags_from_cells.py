@@ -1,0 +1,115 @@
+"""Worlds that arrive with no change history (admitted, created, written or
+run at some step t0) get their change flags from their cells: a layer (batch)
+or row (per-step kernel) is marked changed at t0 - 1 only when a block
+row-pair of either phase that covers it can change, so the first two steps
+evaluate only those row-pairs instead of every one.  Exactness is checked
+against the CPU oracle on mostly settled worlds, at even and odd start steps
+and at start steps whose low 8 bits wrap (t0 - 3 mod 256); the batch also
+shows that the first segment evaluates fewer cell-steps than two dense steps.
+Integer work: bit-exact."""
+import numpy as np
+import pytest
+
+from gpu_util import describe_diff, stream_ptr, to_device
+
+pytestmark = pytest.mark.gpu
+
+GiB = 1 << 30
+STARTS = [130, 255, 256, 257, 1025]
+
+
+def settled(orc, X, Y, Z, seed, steps=150):
+    """Random sand, water, solids and statics, fallen for `steps` steps on the
+    CPU: the bottom is packed and only the surface still moves."""
+    rng = np.random.default_rng(seed)
+    g = rng.choice(np.array([0, 0, 0, 1, 2, 2, 3, 3, 7], np.uint8), size=(Y, Z, X))
+    g[: Y // 3] = np.where(g[: Y // 3] == 0, 2, g[: Y // 3])
+    orc.run(g, seed, 0, steps, nthreads=0)
+    return g
+
+
+@pytest.mark.parametrize("use_smem", [1, 2, 3])
+def test_batch_admission_flags_exact_and_sparse(fs3d, orc, use_smem):
+    dims, seeds = fs3d.gen_batch_dims(23, 10)
+    dims = [(int(X), int(Y), int(Z)) for X, Y, Z in dims]
+    dims[0] = (128, 40, 24)  # rows of two full words: the odd phase's half block at the row end
+    dims[1] = (64, 33, 31)
+    grids = [settled(orc, X, Y, Z, int(s)) for (X, Y, Z), s in zip(dims, seeds)]
+    starts = [STARTS[i % len(STARTS)] for i in range(len(dims))]
+    S, n = 2, 12
+    cells = sum(X * Y * Z for X, Y, Z in dims)
+    with fs3d.Batch(GiB, steps_per_segment=S, use_smem=use_smem) as b:
+        ts = b.admit_many(grids, [int(s) for s in seeds], n, start_steps=starts)
+        b.run_segment()
+        b.sync()
+        first = b.counters()["processed_cell_steps"]
+        # without flags from the cells these first two steps evaluate every cell twice
+        assert first < 2 * cells, (first, cells)
+        for _ in range(n // S - 1):
+            b.run_segment()
+        b.sync()
+        for t, (X, Y, Z), s, t0, g in zip(ts, dims, seeds, starts, grids):
+            ref = g.copy()
+            orc.run(ref, int(s), t0, n, nthreads=0)
+            got = b.retire(t, (Y, Z, X))
+            assert (got == ref).all(), ((X, Y, Z), t0, describe_diff(got, ref, t0 + n - 1))
+
+
+def test_batch_single_admissions(fs3d, orc):
+    dims = [(96, 48, 40), (130, 37, 20), (64, 64, 64)]
+    with fs3d.Batch(GiB, steps_per_segment=8) as b:
+        items = []
+        for i, (X, Y, Z) in enumerate(dims):
+            seed, t0 = 300 + i, STARTS[i + 1]
+            g = settled(orc, X, Y, Z, seed)
+            items.append((b.admit(g, seed, 24, start_step=t0), g, (X, Y, Z), seed, t0))
+        for _ in range(3):
+            b.run_segment()
+        b.sync()
+        for t, g, (X, Y, Z), seed, t0 in items:
+            ref = g.copy()
+            orc.run(ref, seed, t0, 24, nthreads=0)
+            got = b.retire(t, (Y, Z, X))
+            assert (got == ref).all(), describe_diff(got, ref, t0 + 23)
+
+
+@pytest.mark.parametrize("t0", [256, 257])
+def test_world_created_settled_every_step(fs3d, orc, t0):
+    """The per-step kernel of a large world (rows of 8 words): created from a
+    settled grid at t0, every step's hash equals the oracle's."""
+    X, Y, Z = 512, 72, 300
+    g = settled(orc, X, Y, Z, 31, steps=120)
+    n = 12
+    exp = orc.run(g.copy(), 31, t0, n, nthreads=0, hashes=True)
+    with fs3d.World(g, 31, t0, fs3d.LAYOUT_PLANES) as w:
+        for s in range(n):
+            w.step(1)
+            if w.hash() != int(exp[s]):
+                ref = g.copy()
+                orc.run(ref, 31, t0, s + 1, nthreads=0)
+                pytest.fail(describe_diff(w.read(), ref, t0 + s))
+        # a rewrite starts the flags afresh from the new cells
+        g2 = settled(orc, X, Y, Z, 32, steps=90)
+        w.write(g2)
+        w.step(5)
+        ref2 = g2.copy()
+        orc.run(ref2, 31, t0 + n, 5, nthreads=0)
+        got = w.read()
+        assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 4)
+
+
+@pytest.mark.parametrize("entry", ["fs3d_run_device", "fs3d_run_device_noalloc"])
+def test_drop_in_run_of_settled_world(fs3d, orc, cuda, entry):
+    X, Y, Z = 1024, 48, 160  # too large for shared memory: the per-step kernel
+    seed = 57
+    g = settled(orc, X, Y, Z, seed, steps=100)
+    d = to_device(cuda, g)
+    st = stream_ptr(cuda)
+    fn = getattr(fs3d.lib(), entry)
+    assert fn(d.data_ptr(), X, Y, Z, seed, 255, 9, st) == 0
+    assert fn(d.data_ptr(), X, Y, Z, seed, 264, 4, st) == 0
+    fs3d.run_device_check(st)
+    ref = g.copy()
+    orc.run(ref, seed, 255, 13, nthreads=0)
+    got = d.cpu().numpy()
+    assert (got == ref).all(), describe_diff(got, ref, 267)
