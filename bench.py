@@ -956,11 +956,15 @@ def run_only(args):
                 b.admit_generated(X, Y, Z, seed, args.segment * (args.warmup + args.steps + 8))
             for _ in range(args.warmup):
                 b.run_segment()
+            tune = {"segments": 0}
             if not args.no_autotune:
-                b.autotune(trial_segments=1)  # as the headline run does before its timed segments
+                tune = b.autotune(trial_segments=1)  # as the headline run does before its timed segments
             for _ in range(args.steps):
                 b.run_segment()
             b.sync()
+        # segments run in all (a profiler selects the last one's class launches by this count)
+        extra = {"segments": args.warmup + tune["segments"] + args.steps,
+                 "tune": {k: tune.get(k) for k in ("mode", "promote", "ctas_per_sm")}}
     elif args.only == "plain512p":
         # the same world in the plane layout (per-step plane kernel), 8 steps per warm-up/step
         g = fs3d.gen_pillars(1, 512, 512, 512)
@@ -973,7 +977,7 @@ def run_only(args):
         fs3d.step_device(d.data_ptr(), 512, 512, 512, 1, 0, 8 * (args.warmup + args.steps),
                          torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
-    print(json.dumps({"only": args.only, "ok": True}))
+    print(json.dumps({"only": args.only, "ok": True, **(extra if args.only == "batched" else {})}))
     return 0
 
 
