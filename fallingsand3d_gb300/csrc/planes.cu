@@ -1001,8 +1001,11 @@ static cudaError_t launch_gm(int cls, int grid, size_t smem, cudaStream_t st, co
     if (first) {
         // the greatest priority: its CTAs take the SMs before the other
         // classes' grids, which are pending at the same moment in a segment graph
-        int least = 0, greatest = 0;
-        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        static const int greatest = [] {
+            int least = 0, g = 0;
+            if (cudaDeviceGetStreamPriorityRange(&least, &g) != cudaSuccess) g = 0;
+            return g;
+        }();
         attr[0].id = cudaLaunchAttributePriority;
         attr[0].val.priority = greatest;
     }

@@ -113,3 +113,34 @@ def test_drop_in_run_of_settled_world(fs3d, orc, cuda, entry):
     orc.run(ref, seed, 255, 13, nthreads=0)
     got = d.cpu().numpy()
     assert (got == ref).all(), describe_diff(got, ref, 267)
+
+
+@pytest.mark.parametrize("dims", [(2048, 1, 700), (2048, 700, 1), (1000, 3, 333), (1, 900, 900), (4, 2, 4)])
+def test_thin_and_tiny_worlds(fs3d, orc, dims):
+    """Single-layer, single-row and one-cell-wide worlds: the pairs at the
+    world's edges (a layer or row of the pair outside it) are handled as solid
+    by the flags from the cells too.  Created at an odd step, stepped once per
+    call, every hash against the oracle."""
+    X, Y, Z = dims
+    seed = X + 3 * Y + 7 * Z
+    rng = np.random.default_rng(seed)
+    g = rng.choice(np.array([0, 0, 1, 2, 2, 3, 3, 7], np.uint8), size=(Y, Z, X))
+    orc.run(g, seed, 0, 6, nthreads=0)
+    t0, n = 513, 8
+    exp = orc.run(g.copy(), seed, t0, n, nthreads=0, hashes=True)
+    with fs3d.World(g, seed, t0, fs3d.LAYOUT_PLANES) as w:
+        for s in range(n):
+            w.step(1)
+            if w.hash() != int(exp[s]):
+                ref = g.copy()
+                orc.run(ref, seed, t0, s + 1, nthreads=0)
+                pytest.fail(describe_diff(w.read(), ref, t0 + s))
+    with fs3d.Batch(GiB, steps_per_segment=3, use_smem=3) as b:
+        t = b.admit(g, seed, n, start_step=t0)
+        for _ in range(3):
+            b.run_segment()
+        b.sync()
+        ref = g.copy()
+        orc.run(ref, seed, t0, n, nthreads=0)
+        got = b.retire(t, (Y, Z, X))
+        assert (got == ref).all(), describe_diff(got, ref, t0 + n - 1)
