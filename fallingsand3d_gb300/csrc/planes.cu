@@ -741,6 +741,11 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
     uint4* left = (CL && r > 0) ? cg::this_cluster().map_shared_rank(srows, r - 1) : nullptr;
     __shared__ unsigned long long s_processed;  // cell-steps evaluated (the rest were skipped as settled)
     __shared__ int s_count[2];                   // work-list length, by step parity
+    constexpr int kKeys = 32;                    // step keys computed together, one per thread
+    __shared__ uint32_t s_keys[kKeys];
+    // per phase o: the world's block rows along z, and the multiplier that
+    // divides by it (e / n = umulhi(e, m), exact for e, n < 2^16)
+    __shared__ uint32_t s_nbz[2], s_magic[2];
     if (threadIdx.x == 0) {
         s_processed = 0;
         s_count[0] = s_count[1] = 0;
@@ -769,6 +774,10 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
         v.fleft = left ? reinterpret_cast<uint8_t*>(left) + slab_flag_offset((uint32_t)(v.lo - v.left_lo) * row_bytes)
                        : nullptr;
         if (threadIdx.x == 0 && bytes) bulk_load(srows, gslab, bytes, bytes + tx_extra, &bar);
+        if (threadIdx.x < 2) {
+            s_nbz[threadIdx.x] = (uint32_t)nblocks(w.Z, (int)threadIdx.x);
+            s_magic[threadIdx.x] = 0xFFFFFFFFu / (uint32_t)nblocks(w.Z, (int)threadIdx.x) + 1u;
+        }
         // change buffers from the kept flags (the low 8 bits of the last step
         // that changed the layer), or every layer changed at t0 - 1 and t0 - 2
         {
@@ -802,14 +811,21 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
         const uint32_t fs = SlabView<CL>::flag_stride(v.hi - v.lo);
         uint16_t* jlist = reinterpret_cast<uint16_t*>(v.fmine + 4u * fs);
         for (int s = 0; s < w.steps; ++s) {
+            if ((s & (kKeys - 1)) == 0) {
+                // the next kKeys steps' keys, one thread each (the previous step's
+                // barrier is behind every reader of the last ones)
+                for (int i = threadIdx.x; i < kKeys; i += NT)
+                    if (s + i < w.steps) s_keys[i] = stepkey(w.seed, w.t + (uint64_t)(s + i));
+                __syncthreads();
+            }
             if (poisoned) {
                 group_sync();
                 continue;
             }
             const uint64_t t = w.t + (uint64_t)s;
             const int o = (int)(t & 1u);
-            const uint32_t sk = stepkey(w.seed, t);
-            const int NBZ = nblocks(w.Z, o);
+            const uint32_t sk = s_keys[s & (kKeys - 1)];
+            const int NBZ = (int)s_nbz[o];
             const int j_lo = v.lo / 2, j_hi = (r == CS - 1) ? nblocks(w.Y, o) : v.hi / 2;
             const int nj = j_hi - j_lo;
             const uint32_t tb = (uint32_t)t & 3u;
@@ -853,8 +869,7 @@ __global__ void __launch_bounds__(NT, CL ? 1 : (GM ? kGmThreadsPerSm / NT : resi
                 s_processed += (unsigned long long)rows * (unsigned long long)(w.X * w.Z);
             }
             const int npairs = n_layers * NBZ;
-            // e / NBZ as a multiply-high: exact for e, NBZ < 2^16
-            const uint32_t nbz_magic = 0xFFFFFFFFu / (uint32_t)NBZ + 1u;
+            const uint32_t nbz_magic = s_magic[o];
             for (int base = 0; base < npairs; base += per) {
                 const int e = base + (int)(threadIdx.x >> w.lg);
                 const bool valid = e < npairs;
@@ -931,8 +946,12 @@ void fill_classes() {
         {512, 1, 8, 0, resident_fn<512, true>()}};
     for (int c = 0; c < kResidentClasses; ++c) {
         ResidentCfg k = base[c];
-        int smem = per_sm / k.ctas_per_sm - reserved - kStatic;
-        if (smem > optin - kStatic) smem = optin - kStatic;
+        int stat = kStatic;
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, k.fn) == cudaSuccess && (int)fa.sharedSizeBytes > stat)
+            stat = ((int)fa.sharedSizeBytes + 127) & ~127;
+        int smem = per_sm / k.ctas_per_sm - reserved - stat;
+        if (smem > optin - stat) smem = optin - stat;
         smem = smem / 16 * 16;
         if (smem <= 0 || cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
             smem = 0;
