@@ -685,6 +685,20 @@ def run_fs3d(args):
                 "note": "algorithmic bytes count the evaluated cell-steps (settled layer pairs are skipped "
                         "exactly); the worlds stay in L2, so DRAM sees a few MB per segment; the kernels are "
                         "latency-bound: each world's steps are a serial chain (see profiles/)"}
+    # the issue-rate roof beside it: the warp instructions of one steady segment
+    # (ncu, profiles/) against 4 issue slots per SM per cycle at the sampled clock
+    clocks = clk.summary()
+    inst = profile_values("k_plane_segment_resident_batch2048", ("warp_instructions_per_launch",))
+    if inst is not None:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = clocks.get("sm_mhz") or 2070.0
+        issue_peak = sms * 4 * mhz * 1e6
+        roofline["issue"] = {"warp_instructions_per_launch": inst["warp_instructions_per_launch"],
+                             "achieved_per_s": round(inst["warp_instructions_per_launch"] / (ms / 1e3), 1),
+                             "peak_per_s": issue_peak,
+                             "frac": round(inst["warp_instructions_per_launch"] / (ms / 1e3) / issue_peak, 3),
+                             "source": "ncu smsp__inst_executed.sum of one steady segment's launches; peak = "
+                                       f"{sms} SMs x 4 issue slots x {mhz:.0f} MHz"}
 
     # ---- CPU leg (rank 0): the oracle timed (N=1) on the same world states
     # the GPU stepped, then the recorded GPU results checked against it
@@ -729,7 +743,7 @@ def run_fs3d(args):
                            "layout": "2-bit planes", "parallelism": f"replicas x{world}",
                            "launch_config": {k: tune.get(k) for k in ("mode", "promote", "ctas_per_sm", "trials")},
                            "timed_from_step": args.timed_from, "untimed_segments": untimed},
-                "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
+                "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(e2e_ms, 2), "steps": args.e2e_steps,
                         "inputs": f"the {len(worlds)} worlds as the timed segments left them (step {T0}), "
