@@ -202,6 +202,32 @@ __global__ void k_brickmap_bytes(const uint8_t* __restrict__ g, int X, int Y, in
     }
 }
 
+// Crossing an empty brick at once, with the cell-by-cell walk's exact result.
+// The walk steps, at every cell, the axis whose next boundary key (m, added up
+// by e one cell at a time) is smallest; on equal keys z goes before y before x.
+// Its steps are therefore the merge of the three axes' key sequences in that
+// order.  The walk leaves the brick (or the grid) at the first of the three
+// axes' crossing steps (axis a's key after k_a - 1 additions, k_a = the cells
+// to its brick face); every step that comes before it in the merge is taken,
+// and nothing in between can hit, since the brick is empty.  Each axis's key
+// is advanced by the same additions in the same order, so the state after the
+// crossing (cells, keys, last axis, t) is bit for bit the walk's.
+__device__ __forceinline__ bool key_before(float p, int pa, float q, int pb) {
+    return p < q || (p == q && pa > pb);  // axis index as the tie priority: z (2) > y (1) > x (0)
+}
+
+// cells axis a takes to leave its brick (or the grid): k, and whether that leaves the grid
+__device__ __forceinline__ int cells_to_leave(int v, int s, int n, bool& out) {
+    if (s > 0) {
+        const int kb = 8 - (v & 7), kg = n - v;
+        out = kg <= kb;
+        return out ? kg : kb;
+    }
+    const int k = (v & 7) + 1;
+    out = v - k < 0;
+    return k;
+}
+
 template <class G>
 __global__ void __launch_bounds__(256) k_render_dda(G grid, BrickMap bm, CamDev cam, int W, int H,
                                                    float4* __restrict__ out) {
@@ -277,7 +303,58 @@ __global__ void __launch_bounds__(256) k_render_dda(G grid, BrickMap bm, CamDev 
                 cur_brick = b;
                 cur_occ = bm.occupied(v0, v1, v2);
             }
-            if (cur_occ) {
+            if (!cur_occ) {
+                // the whole brick is empty: take every step up to and including the one that leaves it
+                bool out0 = false, out1 = false, out2 = false;
+                const int k0 = s0 ? cells_to_leave(v0, s0, NX, out0) : 0;
+                const int k1 = s1 ? cells_to_leave(v1, s1, NY, out1) : 0;
+                const int k2 = s2 ? cells_to_leave(v2, s2, NZ, out2) : 0;
+                float x0 = m0, x1 = m1, x2 = m2;  // each axis's key at its leaving step
+                for (int j = 1; j < k0; ++j) x0 = __fadd_rn(x0, e0);
+                for (int j = 1; j < k1; ++j) x1 = __fadd_rn(x1, e1);
+                for (int j = 1; j < k2; ++j) x2 = __fadd_rn(x2, e2);
+                int ax = -1;
+                float ke = INFINITY;
+                if (s0) { ax = 0; ke = x0; }
+                if (s1 && (ax < 0 || key_before(x1, 1, ke, ax))) { ax = 1; ke = x1; }
+                if (s2 && (ax < 0 || key_before(x2, 2, ke, ax))) { ax = 2; ke = x2; }
+                // the other axes take their steps that come before it
+                if (ax != 0 && s0) {
+                    for (int j = 0; j < k0 && key_before(m0, 0, ke, ax); ++j) {
+                        m0 = __fadd_rn(m0, e0);
+                        v0 += s0;
+                    }
+                }
+                if (ax != 1 && s1) {
+                    for (int j = 0; j < k1 && key_before(m1, 1, ke, ax); ++j) {
+                        m1 = __fadd_rn(m1, e1);
+                        v1 += s1;
+                    }
+                }
+                if (ax != 2 && s2) {
+                    for (int j = 0; j < k2 && key_before(m2, 2, ke, ax); ++j) {
+                        m2 = __fadd_rn(m2, e2);
+                        v2 += s2;
+                    }
+                }
+                tcur = ke;
+                last = ax;
+                if (ax == 0) {
+                    if (out0) break;
+                    v0 += s0 * k0;
+                    m0 = __fadd_rn(x0, e0);
+                } else if (ax == 1) {
+                    if (out1) break;
+                    v1 += s1 * k1;
+                    m1 = __fadd_rn(x1, e1);
+                } else {
+                    if (out2) break;
+                    v2 += s2 * k2;
+                    m2 = __fadd_rn(x2, e2);
+                }
+                continue;
+            }
+            {
                 const uint32_t m = grid.at(v0, v1, v2);
                 if (m != 0u) {
                     float n[3] = {0.0f, 0.0f, 0.0f};

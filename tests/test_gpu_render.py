@@ -57,6 +57,39 @@ def test_dda_dunes_and_inside_camera(fs3d, orc):
             check_img(w.render(cam, W, H), orc.render_dda(g, oracle_lib.camera_from(cam), W, H))
 
 
+def axis_camera(fs3d, origin, forward, right, up, W, H):
+    c = fs3d.camera_world_view(8, 8, 8, W, H)
+    for a in range(3):
+        c.origin[a], c.forward[a], c.right[a], c.up[a] = origin[a], forward[a], right[a], up[a]
+    return c
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+def test_dda_empty_brick_crossings(fs3d, orc, layout):
+    """Rays cross empty 8^3 bricks in one go on the GPU and cell by cell on the
+    CPU: a sparse world whose sides are not multiples of 8, seen from outside
+    and from inside, along the axes (rays with zero direction components, and
+    the ties between axes that a ray at 45 degrees meets), and obliquely."""
+    X, Y, Z = 37, 29, 45
+    rng = np.random.default_rng(5)
+    g = np.where(rng.random((Y, Z, X)) < 0.004, rng.integers(1, 4, (Y, Z, X)), 0).astype(np.uint8)
+    g[0, : Z // 2] = 1
+    g[Y - 1, Z - 3:, X - 5:] = 3
+    W, H = 96, 64
+    cams = [fs3d.camera_world_view(X, Y, Z, W, H),
+            axis_camera(fs3d, (18.5, 14.5, -20.0), (0, 0, 1), (1, 0, 0), (0, 1, 0), W, H),
+            axis_camera(fs3d, (18.0, 14.0, 22.0), (0, 0, 1), (1, 0, 0), (0, 1, 0), W, H),
+            axis_camera(fs3d, (-10.0, 20.0, -10.0), (0.70710677, 0, 0.70710677), (0.70710677, 0, -0.70710677),
+                        (0, 1, 0), W, H),
+            axis_camera(fs3d, (36.5, 28.5, 44.5), (-0.57735026, -0.57735026, -0.57735026),
+                        (0.70710677, -0.70710677, 0), (-0.40824830, -0.40824830, 0.81649661), W, H),
+            axis_camera(fs3d, (4.0, 40.0, 4.0), (0, -1, 0), (1, 0, 0), (0, 0, 1), W, H)]
+    with fs3d.World(g, 1, 0, layout) as w:
+        for cam in cams:
+            exp = orc.render_dda(g, oracle_lib.camera_from(cam), W, H)
+            check_img(w.render(cam, W, H), exp)
+
+
 def test_world_render_to_device(fs3d, orc, cuda):
     g = orc.gen_c1(2)
     W, H = 128, 72
