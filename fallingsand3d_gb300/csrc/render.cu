@@ -114,10 +114,13 @@ struct PlaneGrid {
 struct BrickMap {
     const uint32_t* bits;
     int BX, BY, BZ;
+    const uint32_t* sbits;  // one bit per 64^3 super-brick (8^3 bricks): set when any of its bricks is
+    int SBX, SBY, SBZ;
     __device__ __forceinline__ bool occupied(int x, int y, int z) const {
         const int b = (x >> 3) + BX * ((z >> 3) + BZ * (y >> 3));
         return (__ldg(bits + (b >> 5)) >> (b & 31)) & 1u;
     }
+    __device__ __forceinline__ bool super_occupied(int sb) const { return (__ldg(sbits + (sb >> 5)) >> (sb & 31)) & 1u; }
 };
 
 __device__ __forceinline__ void mark_brick(uint32_t* bits, int BX, int BZ, int bx, int by, int bz) {
@@ -202,30 +205,48 @@ __global__ void k_brickmap_bytes(const uint8_t* __restrict__ g, int X, int Y, in
     }
 }
 
-// Crossing an empty brick at once, with the cell-by-cell walk's exact result.
-// The walk steps, at every cell, the axis whose next boundary key (m, added up
-// by e one cell at a time) is smallest; on equal keys z goes before y before x.
-// Its steps are therefore the merge of the three axes' key sequences in that
-// order.  The walk leaves the brick (or the grid) at the first of the three
-// axes' crossing steps (axis a's key after k_a - 1 additions, k_a = the cells
-// to its brick face); every step that comes before it in the merge is taken,
-// and nothing in between can hit, since the brick is empty.  Each axis's key
-// is advanced by the same additions in the same order, so the state after the
-// crossing (cells, keys, last axis, t) is bit for bit the walk's.
+// Crossing an empty region (an 8^3 brick or a 64^3 super-brick) at once, with
+// the cell-by-cell walk's exact result.  The walk steps, at every cell, the
+// axis whose next boundary key is smallest; on equal keys z goes before y
+// before x.  Axis a's key after n steps is fma(n, e_a, b_a), a non-decreasing
+// function of n, so the walk's steps are the merge of the three axes' key
+// sequences in that order.  It leaves the region at the first of the three
+// axes' leaving steps (axis a's key at step n_a + k_a - 1, k_a the cells to
+// the region's face); every step that comes before it in the merge is taken
+// (for each other axis a prefix of its keys, found from an estimate and
+// checked key by key), and nothing in between can hit, since the region is
+// empty.  The state after the crossing (cells, steps, keys, last axis, t) is
+// therefore bit for bit the walk's.
 __device__ __forceinline__ bool key_before(float p, int pa, float q, int pb) {
     return p < q || (p == q && pa > pb);  // axis index as the tie priority: z (2) > y (1) > x (0)
 }
 
-// cells axis a takes to leave its brick (or the grid): k, and whether that leaves the grid
-__device__ __forceinline__ int cells_to_leave(int v, int s, int n, bool& out) {
+// cells axis a takes to leave its region of R cells (or the grid): k, and whether that leaves the grid
+__device__ __forceinline__ int cells_to_leave(int v, int s, int n, int R, bool& out) {
     if (s > 0) {
-        const int kb = 8 - (v & 7), kg = n - v;
+        const int kb = R - (v & (R - 1)), kg = n - v;
         out = kg <= kb;
         return out ? kg : kb;
     }
-    const int k = (v & 7) + 1;
+    const int k = (v & (R - 1)) + 1;
     out = v - k < 0;
     return k;
+}
+
+// Takes the steps of one axis (steps n.., at most k - 1 of them: its k-th
+// leaves the region) whose keys come before the leaving step's key ke of axis ax.
+__device__ __forceinline__ void advance_before(int& v, int s, int& n, float b, float e, float& m, int k, int pa,
+                                               float ke, int ax) {
+    const int lo = n, hi = n + k - 2;  // candidate steps
+    if (hi < lo) return;
+    // estimate the last step before ke, then correct it key by key
+    const float q = __fdiv_rn(__fsub_rn(ke, b), e);
+    int j = q < (float)lo ? lo - 1 : (q > (float)hi ? hi : (int)q);
+    while (j < hi && key_before(__fmaf_rn((float)(j + 1), e, b), pa, ke, ax)) ++j;
+    while (j >= lo && !key_before(__fmaf_rn((float)j, e, b), pa, ke, ax)) --j;
+    v += s * (j + 1 - n);
+    n = j + 1;
+    m = __fmaf_rn((float)n, e, b);
 }
 
 template <class G>
@@ -272,125 +293,126 @@ __global__ void __launch_bounds__(256) k_render_dda(G grid, BrickMap bm, CamDev 
         if (t1 < tmax) tmax = t1;
     }
     if (!miss && tmin <= tmax) {
-        // per-axis state as scalars (no local-memory arrays)
-        int v0, v1, v2, s0, s1, s2;
-        float m0, m1, m2, e0, e1, e2;  // next boundary t, t per cell
-        auto setup = [&](int a, int& v, int& st, float& tm, float& td) {
+        // per-axis state as scalars (no local-memory arrays): cell v, step s, steps
+        // taken n, first boundary t b, t per cell e; the next boundary key is
+        // m = fma(n, e, b), one rounding, as in the CPU walk
+        int v0, v1, v2, s0, s1, s2, n0 = 0, n1 = 0, n2 = 0;
+        float b0, b1, b2, e0, e1, e2;
+        auto setup = [&](int a, int& v, int& st, float& bt, float& td) {
             const float p = __fadd_rn(cam.o[a], __fmul_rn(d[a], tmin));
             int c = (int)floorf(p);
             c = c < 0 ? 0 : (c > N[a] - 1 ? N[a] - 1 : c);
             v = c;
             st = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
             if (d[a] == 0.0f) {
-                tm = INFINITY;
+                bt = INFINITY;
                 td = INFINITY;
             } else {
-                tm = __fmul_rn(__fsub_rn((float)(c + (st > 0 ? 1 : 0)), cam.o[a]), inv[a]);
+                bt = __fmul_rn(__fsub_rn((float)(c + (st > 0 ? 1 : 0)), cam.o[a]), inv[a]);
                 td = fabsf(inv[a]);
             }
         };
-        setup(0, v0, s0, m0, e0);
-        setup(1, v1, s1, m1, e1);
-        setup(2, v2, s2, m2, e2);
+        setup(0, v0, s0, b0, e0);
+        setup(1, v1, s1, b1, e1);
+        setup(2, v2, s2, b2, e2);
+        float m0 = b0, m1 = b1, m2 = b2;
         int last = entry_axis;
         float tcur = tmin;
         const int max_iter = NX + NY + NZ + 3;
-        int cur_brick = -1;
-        bool cur_occ = true;
+        int cur_brick = -1, cur_super = -1;
+        bool brick_occ = true, super_occ = true;
         for (int it = 0; it < max_iter; ++it) {
-            const int b = (v0 >> 3) + bm.BX * ((v2 >> 3) + bm.BZ * (v1 >> 3));
-            if (b != cur_brick) {
-                cur_brick = b;
-                cur_occ = bm.occupied(v0, v1, v2);
+            const int sb = (v0 >> 6) + bm.SBX * ((v2 >> 6) + bm.SBZ * (v1 >> 6));
+            if (sb != cur_super) {
+                cur_super = sb;
+                super_occ = bm.super_occupied(sb);
             }
-            if (!cur_occ) {
-                // the whole brick is empty: take every step up to and including the one that leaves it
+            int R = 0;  // an empty region around the cell: a 64^3 super-brick or an 8^3 brick
+            if (!super_occ) {
+                R = 64;
+            } else {
+                const int b = (v0 >> 3) + bm.BX * ((v2 >> 3) + bm.BZ * (v1 >> 3));
+                if (b != cur_brick) {
+                    cur_brick = b;
+                    brick_occ = bm.occupied(v0, v1, v2);
+                }
+                if (!brick_occ) R = 8;
+            }
+            if (R) {
+                // cross the empty region: take every step up to and including the first
+                // that leaves it, with the walk's exact keys (see key_before)
                 bool out0 = false, out1 = false, out2 = false;
-                const int k0 = s0 ? cells_to_leave(v0, s0, NX, out0) : 0;
-                const int k1 = s1 ? cells_to_leave(v1, s1, NY, out1) : 0;
-                const int k2 = s2 ? cells_to_leave(v2, s2, NZ, out2) : 0;
-                float x0 = m0, x1 = m1, x2 = m2;  // each axis's key at its leaving step
-                for (int j = 1; j < k0; ++j) x0 = __fadd_rn(x0, e0);
-                for (int j = 1; j < k1; ++j) x1 = __fadd_rn(x1, e1);
-                for (int j = 1; j < k2; ++j) x2 = __fadd_rn(x2, e2);
+                const int k0 = s0 ? cells_to_leave(v0, s0, NX, R, out0) : 0;
+                const int k1 = s1 ? cells_to_leave(v1, s1, NY, R, out1) : 0;
+                const int k2 = s2 ? cells_to_leave(v2, s2, NZ, R, out2) : 0;
+                // each axis's key at its leaving step
+                const float x0 = s0 ? __fmaf_rn((float)(n0 + k0 - 1), e0, b0) : INFINITY;
+                const float x1 = s1 ? __fmaf_rn((float)(n1 + k1 - 1), e1, b1) : INFINITY;
+                const float x2 = s2 ? __fmaf_rn((float)(n2 + k2 - 1), e2, b2) : INFINITY;
                 int ax = -1;
                 float ke = INFINITY;
                 if (s0) { ax = 0; ke = x0; }
                 if (s1 && (ax < 0 || key_before(x1, 1, ke, ax))) { ax = 1; ke = x1; }
                 if (s2 && (ax < 0 || key_before(x2, 2, ke, ax))) { ax = 2; ke = x2; }
-                // the other axes take their steps that come before it
-                if (ax != 0 && s0) {
-                    for (int j = 0; j < k0 && key_before(m0, 0, ke, ax); ++j) {
-                        m0 = __fadd_rn(m0, e0);
-                        v0 += s0;
-                    }
-                }
-                if (ax != 1 && s1) {
-                    for (int j = 0; j < k1 && key_before(m1, 1, ke, ax); ++j) {
-                        m1 = __fadd_rn(m1, e1);
-                        v1 += s1;
-                    }
-                }
-                if (ax != 2 && s2) {
-                    for (int j = 0; j < k2 && key_before(m2, 2, ke, ax); ++j) {
-                        m2 = __fadd_rn(m2, e2);
-                        v2 += s2;
-                    }
-                }
+                // the other axes take their steps that come before it (a prefix of their keys)
+                if (ax != 0 && s0) advance_before(v0, s0, n0, b0, e0, m0, k0, 0, ke, ax);
+                if (ax != 1 && s1) advance_before(v1, s1, n1, b1, e1, m1, k1, 1, ke, ax);
+                if (ax != 2 && s2) advance_before(v2, s2, n2, b2, e2, m2, k2, 2, ke, ax);
                 tcur = ke;
                 last = ax;
                 if (ax == 0) {
                     if (out0) break;
                     v0 += s0 * k0;
-                    m0 = __fadd_rn(x0, e0);
+                    n0 += k0;
+                    m0 = __fmaf_rn((float)n0, e0, b0);
                 } else if (ax == 1) {
                     if (out1) break;
                     v1 += s1 * k1;
-                    m1 = __fadd_rn(x1, e1);
+                    n1 += k1;
+                    m1 = __fmaf_rn((float)n1, e1, b1);
                 } else {
                     if (out2) break;
                     v2 += s2 * k2;
-                    m2 = __fadd_rn(x2, e2);
+                    n2 += k2;
+                    m2 = __fmaf_rn((float)n2, e2, b2);
                 }
                 continue;
             }
-            {
-                const uint32_t m = grid.at(v0, v1, v2);
-                if (m != 0u) {
-                    float n[3] = {0.0f, 0.0f, 0.0f};
-                    if (last == 0) n[0] = s0 > 0 ? -1.0f : 1.0f;
-                    if (last == 1) n[1] = s1 > 0 ? -1.0f : 1.0f;
-                    if (last == 2) n[2] = s2 > 0 ? -1.0f : 1.0f;
-                    float l[3];
+            const uint32_t m = grid.at(v0, v1, v2);
+            if (m != 0u) {
+                float n[3] = {0.0f, 0.0f, 0.0f};
+                if (last == 0) n[0] = s0 > 0 ? -1.0f : 1.0f;
+                if (last == 1) n[1] = s1 > 0 ? -1.0f : 1.0f;
+                if (last == 2) n[2] = s2 > 0 ? -1.0f : 1.0f;
+                float l[3];
 #pragma unroll
-                    for (int a = 0; a < 3; ++a)
-                        l[a] = __fsub_rn(__fadd_rn(cam.o[a], __fmul_rn(d[a], tcur)), cam.light[a]);
-                    normalize3(l);
-                    const float diff = fmaxf(0.05f, dot3(n, l));
-                    const int ci = m < 4u ? (int)m : 4;
-                    res = make_float4(__fmul_rn(c_palette[ci][0], diff), __fmul_rn(c_palette[ci][1], diff),
-                                      __fmul_rn(c_palette[ci][2], diff), 1.0f);
-                    break;
-                }
+                for (int a = 0; a < 3; ++a)
+                    l[a] = __fsub_rn(__fadd_rn(cam.o[a], __fmul_rn(d[a], tcur)), cam.light[a]);
+                normalize3(l);
+                const float diff = fmaxf(0.05f, dot3(n, l));
+                const int ci = m < 4u ? (int)m : 4;
+                res = make_float4(__fmul_rn(c_palette[ci][0], diff), __fmul_rn(c_palette[ci][1], diff),
+                                  __fmul_rn(c_palette[ci][2], diff), 1.0f);
+                break;
             }
-            // next cell: the axis whose boundary comes first (ties: x, then y, then z)
+            // next cell: the axis whose boundary key comes first (equal keys: z, then y, then x)
             if (m0 < m1 ? m0 < m2 : false) {
                 tcur = m0;
                 v0 += s0;
                 if (v0 < 0 || v0 >= NX) break;
-                m0 = __fadd_rn(m0, e0);
+                m0 = __fmaf_rn((float)++n0, e0, b0);
                 last = 0;
             } else if (!(m0 < m1) && m1 < m2) {
                 tcur = m1;
                 v1 += s1;
                 if (v1 < 0 || v1 >= NY) break;
-                m1 = __fadd_rn(m1, e1);
+                m1 = __fmaf_rn((float)++n1, e1, b1);
                 last = 1;
             } else {
                 tcur = m2;
                 v2 += s2;
                 if (v2 < 0 || v2 >= NZ) break;
-                m2 = __fadd_rn(m2, e2);
+                m2 = __fmaf_rn((float)++n2, e2, b2);
                 last = 2;
             }
         }
@@ -424,16 +446,55 @@ static int map_grid(int64_t n) {
     return (int)(need < 1 ? 1 : (need < cap ? need : cap));
 }
 
-// bm_bits: ceil(bricks / 32) words of device scratch the caller provides
+// One bit per 64^3 super-brick: set when any of its (up to 8^3) bricks is.
+// One thread per super-brick.
+__global__ void k_superbits(const uint32_t* __restrict__ bits, int BX, int BY, int BZ, uint32_t* sbits, int SBX,
+                            int SBY, int SBZ) {
+    const int64_t n = (int64_t)SBX * SBY * SBZ;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int sx = (int)(i % SBX), sz = (int)((i / SBX) % SBZ), sy = (int)(i / ((int64_t)SBX * SBZ));
+        bool any = false;
+        for (int by = 8 * sy; by < min(8 * sy + 8, BY) && !any; ++by)
+            for (int bz = 8 * sz; bz < min(8 * sz + 8, BZ) && !any; ++bz)
+                for (int bx = 8 * sx; bx < min(8 * sx + 8, BX) && !any; ++bx) {
+                    const int64_t b = bx + (int64_t)BX * (bz + (int64_t)BZ * by);
+                    any = (bits[b >> 5] >> (b & 31)) & 1u;
+                }
+        if (any) atomicOr(sbits + (i >> 5), 1u << (i & 31));
+    }
+}
+
+static int64_t brick_words(int X, int Y, int Z) {
+    return (((int64_t)(X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8) + 31) / 32;
+}
+
+// The brick map of a frame: the bricks' bits (filled by the caller's map
+// kernel), then the super-bricks' bits after them, derived here.
+static fs3d_status superbits_and_map(uint32_t* bm_bits, int X, int Y, int Z, cudaStream_t st, BrickMap* bm) {
+    const int BX = (X + 7) / 8, BY = (Y + 7) / 8, BZ = (Z + 7) / 8;
+    const int SBX = (X + 63) / 64, SBY = (Y + 63) / 64, SBZ = (Z + 63) / 64;
+    uint32_t* sbits = bm_bits + brick_words(X, Y, Z);
+    const int64_t ns = (int64_t)SBX * SBY * SBZ;
+    FS3D_CUDA(cudaMemsetAsync(sbits, 0, (size_t)((ns + 31) / 32) * 4, st));
+    k_superbits<<<map_grid(ns), 256, 0, st>>>(bm_bits, BX, BY, BZ, sbits, SBX, SBY, SBZ);
+    FS3D_CHECK_LAUNCH("super-brick map launch");
+    *bm = BrickMap{bm_bits, BX, BY, BZ, sbits, SBX, SBY, SBZ};
+    return FS3D_OK;
+}
+
+// bm_bits: brickmap_bytes(X, Y, Z) of device scratch the caller provides
 fs3d_status launch_render_dda_bytes(const uint8_t* g, int X, int Y, int Z, uint32_t* bm_bits, const fs3d_camera* cam,
                                     int W, int H, float* rgba_dev, cudaStream_t st) {
-    const int BX = (X + 7) / 8, BY = (Y + 7) / 8, BZ = (Z + 7) / 8;
-    FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
+    const int BX = (X + 7) / 8, BZ = (Z + 7) / 8;
+    FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (size_t)brick_words(X, Y, Z) * 4, st));
     k_brickmap_bytes<<<map_grid((int64_t)Y * Z * BX), 256, 0, st>>>(g, X, Y, Z, bm_bits, BX, BZ);
     FS3D_CHECK_LAUNCH("brick map (bytes) launch");
+    BrickMap bm;
+    const fs3d_status s = superbits_and_map(bm_bits, X, Y, Z, st, &bm);
+    if (s != FS3D_OK) return s;
     const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
-    k_render_dda<BytesGrid><<<grd, blk, 0, st>>>(BytesGrid{g, X, Y, Z}, BrickMap{bm_bits, BX, BY, BZ}, to_dev(cam), W,
-                                                 H, reinterpret_cast<float4*>(rgba_dev));
+    k_render_dda<BytesGrid><<<grd, blk, 0, st>>>(BytesGrid{g, X, Y, Z}, bm, to_dev(cam), W, H,
+                                                 reinterpret_cast<float4*>(rgba_dev));
     FS3D_CHECK_LAUNCH("render dda launch");
     return FS3D_OK;
 }
@@ -452,14 +513,16 @@ fs3d_status launch_render_dda_planes(const uint4* rows, const uint8_t* statics, 
         k_counts_to_bits<<<map_grid((nb + 31) / 32 + 32), 256, 0, st>>>(brick_counts, nb, bm_bits);
         FS3D_CHECK_LAUNCH("brick map from counts launch");
     } else {
-        FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (((size_t)BX * BY * BZ + 31) / 32) * 4, st));
+        FS3D_CUDA(cudaMemsetAsync(bm_bits, 0, (size_t)brick_words(X, Y, Z) * 4, st));
         k_brickmap_planes<<<map_grid((int64_t)Y * Z * nw), 256, 0, st>>>(rows, X, Y, Z, nw, bm_bits, BX, BZ);
         FS3D_CHECK_LAUNCH("brick map (planes) launch");
     }
+    BrickMap bm;
+    const fs3d_status s = superbits_and_map(bm_bits, X, Y, Z, st, &bm);
+    if (s != FS3D_OK) return s;
     const dim3 blk(16, 16), grd((W + 15) / 16, (H + 15) / 16);
-    k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(
-        PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw}, BrickMap{bm_bits, BX, BY, BZ},
-        to_dev(cam), W, H, reinterpret_cast<float4*>(rgba_dev));
+    k_render_dda<PlaneGrid><<<grd, blk, 0, st>>>(PlaneGrid{reinterpret_cast<const uint32_t*>(rows), statics, X, Y, Z, nw},
+                                                 bm, to_dev(cam), W, H, reinterpret_cast<float4*>(rgba_dev));
     FS3D_CHECK_LAUNCH("render dda (planes) launch");
     return FS3D_OK;
 }
@@ -469,7 +532,8 @@ size_t brick_count_bytes(int X, int Y, int Z) {
 }
 
 size_t brickmap_bytes(int X, int Y, int Z) {
-    return ((((size_t)(X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8) + 31) / 32) * 4;
+    const size_t super_words = (((size_t)(X + 63) / 64) * ((Y + 63) / 64) * ((Z + 63) / 64) + 31) / 32;
+    return ((size_t)brick_words(X, Y, Z) + super_words) * 4;
 }
 
 }  // namespace fs3d

@@ -591,6 +591,14 @@ static const float k_palette[5][3] = {
 };
 
 /* Amanatides & Woo (1987) grid traversal of the uint8 world. */
+/* Voxel DDA: per pixel a ray from the camera, clipped to the grid's box
+ * (slab test per axis in x, y, z order), walks cell by cell (Amanatides &
+ * Woo): at each cell the axis whose next boundary comes first is stepped
+ * (on equal keys z, then y, then x).  Axis a's key after n steps is
+ * fmaf(n, |1/d_a|, b_a), b_a its first boundary's t: one rounding per key,
+ * so a walker may jump over cells and land on the same keys.  The first
+ * non-empty cell is shaded by its material colour times max(0.05, n.l),
+ * n the normal of the face the ray entered through, l towards the light. */
 void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* cam, int W,
                     int H, float* rgba) {
     const int N[3] = {X, Y, Z};
@@ -630,8 +638,8 @@ void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* 
                 if (t1 < tmax) tmax = t1;
             }
             if (!miss && tmin <= tmax) {
-                int v[3], step[3];
-                float tmx[3], tdl[3];
+                int v[3], step[3], nst[3] = {0, 0, 0};
+                float tmx[3], tdl[3], tb0[3];
                 for (int a = 0; a < 3; ++a) {
                     const float p = o[a] + d[a] * tmin;
                     int c = (int)floorf(p);
@@ -640,12 +648,13 @@ void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* 
                     v[a] = c;
                     step[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
                     if (d[a] == 0.0f) {
-                        tmx[a] = INFINITY;
+                        tb0[a] = INFINITY;
                         tdl[a] = INFINITY;
                     } else {
-                        tmx[a] = ((float)(c + (step[a] > 0 ? 1 : 0)) - o[a]) * inv[a];
+                        tb0[a] = ((float)(c + (step[a] > 0 ? 1 : 0)) - o[a]) * inv[a];
                         tdl[a] = fabsf(inv[a]);
                     }
+                    tmx[a] = tb0[a];
                 }
                 int last = entry_axis;
                 float tcur = tmin;
@@ -675,7 +684,8 @@ void orc_render_dda(const uint8_t* grid, int X, int Y, int Z, const orc_camera* 
                     tcur = tmx[a];
                     v[a] += step[a];
                     if (v[a] < 0 || v[a] >= N[a]) break;
-                    tmx[a] += tdl[a];
+                    nst[a] += 1;
+                    tmx[a] = fmaf((float)nst[a], tdl[a], tb0[a]);
                     last = a;
                 }
             }
