@@ -447,20 +447,26 @@ static int map_grid(int64_t n) {
 }
 
 // One bit per 64^3 super-brick: set when any of its (up to 8^3) bricks is.
-// One thread per super-brick.
+// One warp per super-brick; each lane reads the 8-brick x runs of two of its
+// 64 (y, z) brick rows (a run is 8 consecutive bits, in one or two words).
 __global__ void k_superbits(const uint32_t* __restrict__ bits, int BX, int BY, int BZ, uint32_t* sbits, int SBX,
                             int SBY, int SBZ) {
     const int64_t n = (int64_t)SBX * SBY * SBZ;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
         const int sx = (int)(i % SBX), sz = (int)((i / SBX) % SBZ), sy = (int)(i / ((int64_t)SBX * SBZ));
+        const int bx0 = 8 * sx, nx = min(8, BX - bx0);
         bool any = false;
-        for (int by = 8 * sy; by < min(8 * sy + 8, BY) && !any; ++by)
-            for (int bz = 8 * sz; bz < min(8 * sz + 8, BZ) && !any; ++bz)
-                for (int bx = 8 * sx; bx < min(8 * sx + 8, BX) && !any; ++bx) {
-                    const int64_t b = bx + (int64_t)BX * (bz + (int64_t)BZ * by);
-                    any = (bits[b >> 5] >> (b & 31)) & 1u;
-                }
-        if (any) atomicOr(sbits + (i >> 5), 1u << (i & 31));
+        for (int p = lane; p < 64; p += 32) {
+            const int by = 8 * sy + (p >> 3), bz = 8 * sz + (p & 7);
+            if (by >= BY || bz >= BZ) continue;
+            const int64_t b0 = bx0 + (int64_t)BX * (bz + (int64_t)BZ * by);
+            const uint64_t w = (uint64_t)__ldg(bits + (b0 >> 5)) |
+                               ((b0 & 31) + nx > 32 ? (uint64_t)__ldg(bits + (b0 >> 5) + 1) << 32 : 0ull);
+            any |= ((w >> (b0 & 31)) & ((1ull << nx) - 1ull)) != 0ull;
+        }
+        if (__any_sync(0xFFFFFFFFu, any) && lane == 0) atomicOr(sbits + (i >> 5), 1u << (i & 31));
     }
 }
 
@@ -476,7 +482,7 @@ static fs3d_status superbits_and_map(uint32_t* bm_bits, int X, int Y, int Z, cud
     uint32_t* sbits = bm_bits + brick_words(X, Y, Z);
     const int64_t ns = (int64_t)SBX * SBY * SBZ;
     FS3D_CUDA(cudaMemsetAsync(sbits, 0, (size_t)((ns + 31) / 32) * 4, st));
-    k_superbits<<<map_grid(ns), 256, 0, st>>>(bm_bits, BX, BY, BZ, sbits, SBX, SBY, SBZ);
+    k_superbits<<<map_grid(ns * 32), 256, 0, st>>>(bm_bits, BX, BY, BZ, sbits, SBX, SBY, SBZ);
     FS3D_CHECK_LAUNCH("super-brick map launch");
     *bm = BrickMap{bm_bits, BX, BY, BZ, sbits, SBX, SBY, SBZ};
     return FS3D_OK;
