@@ -590,7 +590,6 @@ static const float k_palette[5][3] = {
     {0.65f, 0.35f, 0.30f}, /* any static material >= 4 */
 };
 
-/* Amanatides & Woo (1987) grid traversal of the uint8 world. */
 /* Voxel DDA: per pixel a ray from the camera, clipped to the grid's box
  * (slab test per axis in x, y, z order), walks cell by cell (Amanatides &
  * Woo): at each cell the axis whose next boundary comes first is stepped
