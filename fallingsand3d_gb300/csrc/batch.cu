@@ -259,9 +259,13 @@ int segment_class(const fs3d_batch* b, const BWorld& w) {
         if (w.t < kYoungSteps) {
             // a young world that needs a cluster runs instead from L2 with a
             // whole SM (768 threads): dense steps keep its warps busy, and no
-            // cluster barrier or y-slab imbalance holds it up
+            // cluster barrier or y-slab imbalance holds it up.  The smallest
+            // worlds run in 256-thread CTAs: their dense steps take half the
+            // passes there (2048 fresh worlds: 2.79 ms per first segment
+            // against 3.02 ms in 128-thread CTAs; moving the 256-thread worlds
+            // up to 768 threads too measured 3.09 ms)
             const int c = smem();
-            if (c >= 0 && c < kSingleCtaClasses) return c;
+            if (c >= 0 && c < kSingleCtaClasses) return c == 0 ? 1 : c;
             if (w.Y <= 4096) return kResidentClasses + kGmDense;
             return c >= 0 ? c : gm();
         }
