@@ -87,7 +87,8 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     cudaError_t e = cudaMallocAsync((void**)&sc.rows, plane_bytes(X, Y, Z), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.desc, sizeof(PlaneWorld), st);
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&sc.ints, sizeof(int) * kInts, st);
-    if (e == cudaSuccess && cls < 0) e = cudaMallocAsync((void**)&rflags, (size_t)Y * Z, st);
+    // per-row flags for the per-step kernel, per-layer flags for a resident launch
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&rflags, cls < 0 ? (size_t)Y * Z : layer_flag_bytes(Y), st);
     fs3d_status s = e == cudaSuccess ? FS3D_OK : cuda_fail(e, "fs3d_run_device scratch");
     PlaneWorld d{};
     d.rows = sc.rows;
@@ -99,6 +100,7 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     d.nw = nw;
     d.steps = n_steps;
     d.lg = lg;
+    if (cls >= 0) d.lflags = rflags;  // set from the cells below: no dense first steps
     int ints[kInts] = {};
     if (cls >= 0) ints[1 + cls] = 1;
     // pageable sources: staged before each call returns
@@ -108,7 +110,9 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     if (s == FS3D_OK) s = planes_from_bytes(grid_dev, X, Y, Z, sc.rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
-            s = launch_plane_segment_resident(cls, sc.desc, sc.ints + kOrder, sc.ints, sc.ints + kCounter, err, st);
+            s = layer_flags_from_cells(sc.rows, rflags, X, Y, Z, t0, st);
+            if (s == FS3D_OK)
+                s = launch_plane_segment_resident(cls, sc.desc, sc.ints + kOrder, sc.ints, sc.ints + kCounter, err, st);
         } else {
             s = init_row_flags(sc.rows, rflags, X, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {

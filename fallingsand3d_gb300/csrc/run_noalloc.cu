@@ -136,6 +136,8 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
     d.nw = nw;
     d.steps = n_steps;
     d.lg = lg;
+    uint8_t* flags = base + kFlagsOff;  // per-row flags (per-step kernel) or per-layer flags (resident launch)
+    if (cls >= 0) d.lflags = flags;     // set from the cells below: no dense first steps
     k_noalloc_tables<<<1, 32, 0, st>>>(d, cls, base);
     FS3D_CHECK_LAUNCH("noalloc tables launch");
     PlaneWorld* desc = reinterpret_cast<PlaneWorld*>(base + kDescOff);
@@ -144,9 +146,10 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
     s = planes_from_bytes(grid_dev, X, Y, Z, rows, st);
     if (s == FS3D_OK) {
         if (cls >= 0) {
-            s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, err, st);
+            s = layer_flags_from_cells(rows, flags, X, Y, Z, t0, st);
+            if (s == FS3D_OK) s = launch_plane_segment_resident(cls, desc, ints + kOrder, ints, ints + kCounter, err, st);
         } else {
-            uint8_t* rflags = base + kFlagsOff;
+            uint8_t* rflags = flags;
             s = init_row_flags(rows, rflags, X, Y, Z, t0, st);
             for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
                 d.t = t0 + (uint64_t)a;

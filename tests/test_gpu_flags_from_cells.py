@@ -98,9 +98,12 @@ def test_world_created_settled_every_step(fs3d, orc, t0):
         assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 4)
 
 
+@pytest.mark.parametrize("dims", [(1024, 48, 160), (64, 48, 40), (130, 70, 90)])
 @pytest.mark.parametrize("entry", ["fs3d_run_device", "fs3d_run_device_noalloc"])
-def test_drop_in_run_of_settled_world(fs3d, orc, cuda, entry):
-    X, Y, Z = 1024, 48, 160  # too large for shared memory: the per-step kernel
+def test_drop_in_run_of_settled_world(fs3d, orc, cuda, entry, dims):
+    """The per-step kernel (1024 x 48 x 160: too large for shared memory, row
+    flags) and the resident launch (one CTA, and a cluster: layer flags)."""
+    X, Y, Z = dims
     seed = 57
     g = settled(orc, X, Y, Z, seed, steps=100)
     d = to_device(cuda, g)
