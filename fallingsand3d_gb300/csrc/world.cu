@@ -32,6 +32,8 @@ struct fs3d_world {
     int* brick_counts = nullptr;   // PLANES render: non-empty cells per brick, kept by the per-step kernel
     bool counts_valid = false;     // brick_counts match the planes
     // PLANES worlds stepped by the per-step kernel: per-row last-changed step (Y*Z bytes)
+    // change flags kept from one call to the next: per row (Y*Z bytes) for the
+    // per-step kernel, per layer (Y bytes, padded) for a resident launch
     uint8_t* rflags = nullptr;
     bool flags_ok = false;  // rflags describe the state at step flags_t
     uint64_t flags_t = 0;
@@ -158,10 +160,8 @@ fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uin
         if (e == cudaSuccess) e = cudaMalloc((void**)&w->aux, sizeof(aux));
         if (e == cudaSuccess) e = cudaMemcpy(w->aux, aux, sizeof(aux), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return fail(e, "cudaMalloc/copy(step tables)");
-        if (w->cls < 0) {
-            e = cudaMalloc((void**)&w->rflags, (size_t)Y * Z);
-            if (e != cudaSuccess) return fail(e, "cudaMalloc(row change flags)");
-        }
+        e = cudaMalloc((void**)&w->rflags, w->cls < 0 ? (size_t)Y * Z : layer_flag_bytes(Y));
+        if (e != cudaSuccess) return fail(e, "cudaMalloc(change flags)");
     }
     s = upload(w, grid_host);
     if (s != FS3D_OK) {
@@ -214,11 +214,25 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
             return s;
         }
         // the world fits in shared memory (one CTA or a cluster): all n steps
-        // in one launch; the descriptor's pageable source is staged before the
-        // call returns
-        FS3D_CUDA(cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream));
-        s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
-                                          w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
+        // in one launch, the layer flags kept from the previous call (or set
+        // from the cells); the descriptor's pageable source is staged before
+        // the call returns
+        if (!w->flags_ok || w->flags_t != w->step) {
+            s = layer_flags_from_cells(w->rows, w->rflags, w->X, w->Y, w->Z, w->step, w->stream);
+            w->flags_ok = s == FS3D_OK;
+        }
+        d.lflags = w->rflags;
+        if (s == FS3D_OK) {
+            const cudaError_t ce = cudaMemcpyAsync(w->desc, &d, sizeof(d), cudaMemcpyHostToDevice, w->stream);
+            s = ce == cudaSuccess ? FS3D_OK : cuda_fail(ce, "fs3d_world_step descriptor");
+        }
+        if (s == FS3D_OK)
+            s = launch_plane_segment_resident(w->cls, w->desc, w->aux + kAuxOrder, w->aux + kAuxMeta,
+                                              w->aux + kAuxCounter, w->aux + kAuxErr, w->stream);
+        if (s == FS3D_OK)
+            w->flags_t = w->step + (uint64_t)n_steps;
+        else
+            w->flags_ok = false;
         w->counts_valid = false;  // the next frame recounts
     }
     if (s == FS3D_OK) w->step += (uint64_t)n_steps;

@@ -147,3 +147,32 @@ def test_thin_and_tiny_worlds(fs3d, orc, dims):
         orc.run(ref, seed, t0, n, nthreads=0)
         got = b.retire(t, (Y, Z, X))
         assert (got == ref).all(), describe_diff(got, ref, t0 + n - 1)
+
+
+@pytest.mark.parametrize("dims", [(64, 48, 40), (96, 96, 96), (130, 70, 90)])
+def test_world_resident_one_step_per_call(fs3d, orc, dims):
+    """A world that fits the resident kernels, stepped one step per call (an
+    engine's frame loop): the layer flags carry from call to call (set from
+    the cells at creation and after a rewrite), every hash equal to the
+    oracle's, across the 8-bit wrap of the flags."""
+    X, Y, Z = dims
+    seed = 900 + X
+    g = settled(orc, X, Y, Z, seed, steps=80)
+    t0, n = 250, 24
+    exp = orc.run(g.copy(), seed, t0, n, nthreads=0, hashes=True)
+    with fs3d.World(g, seed, t0, fs3d.LAYOUT_PLANES) as w:
+        for s in range(n):
+            w.step(1)
+            if w.hash() != int(exp[s]):
+                ref = g.copy()
+                orc.run(ref, seed, t0, s + 1, nthreads=0)
+                pytest.fail(describe_diff(w.read(), ref, t0 + s))
+        g2 = settled(orc, X, Y, Z, seed + 1, steps=60)
+        w.write(g2)
+        for _ in range(5):
+            w.step(1)
+        w.step(3)
+        ref2 = g2.copy()
+        orc.run(ref2, seed, t0 + n, 8, nthreads=0)
+        got = w.read()
+        assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 7)
