@@ -676,6 +676,9 @@ def run_fs3d(args):
     # ---- mesh materials: the upstream cube-grid scene
     mesh = None if args.skip_large else run_mesh(fs3d, torch, args, checks)
 
+    # ---- an engine's frame loop: the 64^3 parity world, one step per call
+    engine = run_engine_loop(fs3d, torch, checks)
+
     # ---- roofline of the dominant work: the segment graph, whose time is the
     # resident kernels (one launch per size class steps its worlds 64 times).
     # Algorithmic bytes = the 2-bit state read and written by every EVALUATED
@@ -793,7 +796,7 @@ def run_fs3d(args):
                 "processed": {"voxel_updates_per_s": value * proc_frac, "fraction_of_dense": round(proc_frac, 4),
                               "note": "value counts every cell of every world each step (dense-equivalent); "
                                       "this counts the cell-steps the kernels evaluated"},
-                "plain_512": p512, "served": served, "large_render": large, "mesh_render": mesh, "parity": parity,
+                "plain_512": p512, "served": served, "large_render": large, "mesh_render": mesh, "engine_loop": engine, "parity": parity,
                 "segment_ms": [round(x, 4) for x in seg_ms], "fresh_segment_ms": [round(x, 4) for x in fresh_ms]}
         print(json.dumps(line))
     if world > 1:
@@ -843,6 +846,36 @@ def run_large(fs3d, torch, dev, args, checks=None, X=1024, Y=1024, Z=1024, W=192
             "frame_us": round(frame_ms / sampled * 1e3, 2),
             "voxel_updates_per_s": cells * n / wall, "rays_per_s": W * H * n / wall,
             "mass_conserved": bool((counts == counts0).all())}
+
+
+def run_engine_loop(fs3d, torch, checks=None, steps=200):
+    """The drop-in use of an engine's main loop (upstream engine.cpp:54-74):
+    the 64^3 parity world (two stone layers, sand and water in the upper
+    half) stepped one step per call, as a frame loop would.  The world fits
+    one CTA's shared memory and keeps its layer flags from call to call.
+    Device time per call with CUDA events on the world's stream, and the
+    host's time per call; the final grid is checked against the oracle."""
+    g = fs3d.gen_parity(1)
+    with fs3d.World(g, 1, 0, fs3d.LAYOUT_PLANES) as w:
+        ws = torch.cuda.ExternalStream(w.stream())
+        for _ in range(5):
+            w.step(1)
+        w.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(ws)
+        for _ in range(steps):
+            w.step(1)
+        e1.record(ws)
+        host_s = time.perf_counter() - t0
+        e1.synchronize()
+        final = w.read()
+    if checks is not None:
+        checks.add_run("engine loop", g, 1, 0, 5 + steps, final)
+    dev_ms = e0.elapsed_time(e1)
+    return {"workload": f"64^3 parity world, {steps} calls of one step each (steps 5..{4 + steps})",
+            "us_per_step": round(dev_ms * 1e3 / steps, 2), "host_us_per_call": round(host_s * 1e6 / steps, 2),
+            "voxel_updates_per_s": 64 ** 3 * steps / (dev_ms / 1e3)}
 
 
 def run_mesh(fs3d, torch, args, checks=None, W=1920, H=1080, frames=20):

@@ -150,23 +150,29 @@ def test_thin_and_tiny_worlds(fs3d, orc, dims):
 
 
 @pytest.mark.parametrize("dims", [(64, 48, 40), (96, 96, 96), (130, 70, 90)])
-def test_world_resident_one_step_per_call(fs3d, orc, dims):
-    """A world that fits the resident kernels, stepped one step per call (an
-    engine's frame loop): the layer flags carry from call to call (set from
-    the cells at creation and after a rewrite), every hash equal to the
-    oracle's, across the 8-bit wrap of the flags."""
+def test_world_calls_of_few_and_many_steps(fs3d, orc, dims):
+    """A world that fits the resident kernels, stepped in calls of one to
+    eight steps, as an engine's frame loop would: short calls take the
+    per-step kernel (row flags), longer ones a resident launch (layer flags)
+    when the world is small; each kind of flags carries from call to call or
+    is set again from the cells, and every call's hash equals the oracle's,
+    across the 8-bit wrap of the flags."""
     X, Y, Z = dims
     seed = 900 + X
     g = settled(orc, X, Y, Z, seed, steps=80)
-    t0, n = 250, 24
+    t0 = 250
+    calls = [1, 1, 5, 1, 8, 2, 4, 1, 1, 6, 3, 4]
+    n = sum(calls)
     exp = orc.run(g.copy(), seed, t0, n, nthreads=0, hashes=True)
     with fs3d.World(g, seed, t0, fs3d.LAYOUT_PLANES) as w:
-        for s in range(n):
-            w.step(1)
-            if w.hash() != int(exp[s]):
+        done = 0
+        for c in calls:
+            w.step(c)
+            done += c
+            if w.hash() != int(exp[done - 1]):
                 ref = g.copy()
-                orc.run(ref, seed, t0, s + 1, nthreads=0)
-                pytest.fail(describe_diff(w.read(), ref, t0 + s))
+                orc.run(ref, seed, t0, done, nthreads=0)
+                pytest.fail(describe_diff(w.read(), ref, t0 + done - 1))
         g2 = settled(orc, X, Y, Z, seed + 1, steps=60)
         w.write(g2)
         for _ in range(5):
@@ -176,3 +182,7 @@ def test_world_resident_one_step_per_call(fs3d, orc, dims):
         orc.run(ref2, seed, t0 + n, 8, nthreads=0)
         got = w.read()
         assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 7)
+        w.step(16)  # a resident launch (small worlds) after the rewrite's per-step calls
+        orc.run(ref2, seed, t0 + n + 8, 16, nthreads=0)
+        got = w.read()
+        assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 23)
