@@ -74,9 +74,11 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     cudaStream_t st = (cudaStream_t)stream;
     if (n_steps == 0) return FS3D_OK;
     if (X > kPlaneMaxX) return launch_step_bytes(grid_dev, X, Y, Z, seed, t0, n_steps, st);
-    const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
-    // worlds too large for shared memory: the per-step kernel that skips
-    // settled row-pairs (per-row flags in the scratch)
+    const int nw = plane_nw(X), lg = plane_lg(nw);
+    // a resident launch, or the per-step kernel (prefer_resident)
+    const int cls = prefer_resident(resident_class(X, Y, Z), n_steps, (int64_t)X * Y * Z) ? resident_class(X, Y, Z) : -1;
+    // worlds too large for shared memory, and short calls: the per-step
+    // kernel that skips settled row-pairs (per-row flags in the scratch)
     int* err = nullptr;
     {
         const fs3d_status se = run_error_word(&err);

@@ -119,7 +119,9 @@ extern "C" fs3d_status fs3d_run_device_noalloc(uint8_t* grid_dev, int X, int Y, 
         return set_error(FS3D_ERR_INVALID_ARG,
                          "fs3d_run_device_noalloc: world too large for the static scratch (planes of at most "
                          "64 MiB, about 268 M cells, and rows of at most 2048 cells)");
-    const int nw = plane_nw(X), lg = plane_lg(nw), cls = resident_class(X, Y, Z);
+    const int nw = plane_nw(X), lg = plane_lg(nw);
+    // a resident launch, or the per-step kernel (prefer_resident)
+    const int cls = prefer_resident(resident_class(X, Y, Z), n_steps, (int64_t)X * Y * Z) ? resident_class(X, Y, Z) : -1;
     if (n_steps == 0) return FS3D_OK;
     unsigned char* base = nullptr;
     fs3d_status s = noalloc_scratch_base(&base);

@@ -44,12 +44,6 @@ struct fs3d_world {
 
 namespace {
 
-// A world that fits the resident kernels takes a call's steps in one resident
-// launch when the call has at least this many steps and the world at most
-// this many cells; otherwise the per-step kernel (measured crossovers).
-constexpr int kResidentMinSteps = 4;
-constexpr int64_t kResidentMaxCells = 300000;
-
 // layout of fs3d_world::aux (device ints)
 constexpr int kAuxMeta = 0;                              // kMetaInts ints
 constexpr int kAuxOrder = kMetaInts;      // order[0] = 0
@@ -201,14 +195,8 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
         d.steps = n_steps;
         d.lg = plane_lg(nw);
         s = FS3D_OK;
-        // A resident launch runs the world on one CTA (or cluster), the
-        // per-step kernel on the whole GPU, one launch per step.  The first
-        // pays its load, store and launch once per call, the second per step:
-        // a few steps of a small world, or any steps of a larger one, go
-        // faster per step (64^3, one step per call: 6.4 us against 12.7 us;
-        // eight steps per call: 4.5 us resident against 6.5 us; 128^3: 7.1 us
-        // per step against 9.8-22 us resident).
-        const bool resident = w->cls >= 0 && n_steps >= kResidentMinSteps && w->cells() <= kResidentMaxCells;
+        // one resident launch, or one per-step launch per step (prefer_resident)
+        const bool resident = prefer_resident(w->cls, n_steps, w->cells());
         if (!resident) {
             // one launch per step, settled row-pairs skipped; the row flags
             // carry over from the previous call when nothing else touched the

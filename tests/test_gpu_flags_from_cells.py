@@ -98,24 +98,28 @@ def test_world_created_settled_every_step(fs3d, orc, t0):
         assert (got == ref2).all(), describe_diff(got, ref2, t0 + n + 4)
 
 
-@pytest.mark.parametrize("dims", [(1024, 48, 160), (64, 48, 40), (130, 70, 90)])
+@pytest.mark.parametrize("dims", [(1024, 48, 160), (64, 48, 40), (96, 40, 64)])
 @pytest.mark.parametrize("entry", ["fs3d_run_device", "fs3d_run_device_noalloc"])
 def test_drop_in_run_of_settled_world(fs3d, orc, cuda, entry, dims):
-    """The per-step kernel (1024 x 48 x 160: too large for shared memory, row
-    flags) and the resident launch (one CTA, and a cluster: layer flags)."""
+    """Settled worlds through both drop-in entries at start steps across the
+    8-bit wrap: the per-step kernel (1024 x 48 x 160, too large for shared
+    memory, and every call of fewer than four steps: row flags) and the
+    resident launch (the smaller worlds' longer calls: layer flags)."""
     X, Y, Z = dims
     seed = 57
     g = settled(orc, X, Y, Z, seed, steps=100)
     d = to_device(cuda, g)
     st = stream_ptr(cuda)
     fn = getattr(fs3d.lib(), entry)
-    assert fn(d.data_ptr(), X, Y, Z, seed, 255, 9, st) == 0
-    assert fn(d.data_ptr(), X, Y, Z, seed, 264, 4, st) == 0
+    t = 255
+    for n in (9, 4, 2, 1):
+        assert fn(d.data_ptr(), X, Y, Z, seed, t, n, st) == 0
+        t += n
     fs3d.run_device_check(st)
     ref = g.copy()
-    orc.run(ref, seed, 255, 13, nthreads=0)
+    orc.run(ref, seed, 255, t - 255, nthreads=0)
     got = d.cpu().numpy()
-    assert (got == ref).all(), describe_diff(got, ref, 267)
+    assert (got == ref).all(), describe_diff(got, ref, t - 1)
 
 
 @pytest.mark.parametrize("dims", [(2048, 1, 700), (2048, 700, 1), (1000, 3, 333), (1, 900, 900), (4, 2, 4)])
