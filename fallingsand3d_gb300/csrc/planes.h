@@ -56,14 +56,14 @@ constexpr int kMetaInts = kMetaWorlds + 1;
 // smallest class that holds a world of these dims, -1 if none does
 int resident_class(int X, int Y, int Z);
 // Whether a call of n steps on one world of class cls takes them in one
-// resident launch (one CTA or cluster, its load, store and launch paid once
-// per call) rather than n launches of the per-step kernel (each step on the
-// whole GPU): only calls of at least 4 steps on worlds of at most 300 000
-// cells (measured crossovers: 64^3 one step per call 6.5 us per step against
-// 12.7 us resident, eight steps 4.7 us resident against 6.5 us; 128^3 the
-// per-step kernel at any call length, 7.3 us against 9.8-22 us).
+// resident launch (one CTA or cluster: its load, store and launch paid once
+// per call, then about 3-4.3 us per step up to 112^3) rather than n launches
+// of the per-step kernel (each step on the whole GPU, about 6.2-7.4 us).
+// Measured crossovers: 64^3 at 3-4 steps per call, 80^3 at 5, 96^3 at 7-8,
+// 112^3 at 11; 128^3 (a cluster) the per-step kernel at 1 and 8 steps per
+// call (7.1 against 9.8-22 us resident).
 inline bool prefer_resident(int cls, int n_steps, int64_t cells) {
-    return cls >= 0 && n_steps >= 4 && cells <= 300000;
+    return cls >= 0 && n_steps >= 4 && cells <= 1500000 && (int64_t)n_steps * 120000 >= cells;
 }
 // largest plane buffer (bytes) one CTA can hold; 0 if unavailable
 int smem_world_limit();
