@@ -114,8 +114,8 @@ fs3d_status fs3d_step_device_many(int n, uint8_t* const* grids_dev, const int* d
  * converted into 2-bit planes held in device scratch taken from the
  * stream-ordered pool (about X*Y*Z/4 bytes, freed on `stream` when done), the
  * n steps run there (one launch for all of them when the world fits in shared
- * memory, has at most 300 000 cells and n >= 4; otherwise one launch per step
- * over the whole GPU) and the planes are converted back.  Settled rows or
+ * memory and n repays the launch: n >= 4 and at least one step per 120 000
+ * cells, up to 1.5 M cells; otherwise one launch per step over the whole GPU) and the planes are converted back.  Settled rows or
  * layers are skipped exactly, starting from flags computed from the cells.
  * Asynchronous on `stream`. */
 fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, uint64_t seed, uint64_t t0,
@@ -157,9 +157,10 @@ fs3d_status fs3d_first_diff_device(const uint8_t* a_dev, const uint8_t* b_dev, i
 /* ---- world objects (library-owned device state) ---- */
 fs3d_status fs3d_world_create(const uint8_t* grid_host, int X, int Y, int Z, uint64_t seed,
                               uint64_t start_step, int layout, fs3d_world** out);
-/* async; a PLANES world takes the call's steps in one resident launch (world
- * of at most 300 000 cells fitting shared memory, n_steps >= 4) or one launch
- * per step over the whole GPU, and keeps its change flags from call to call */
+/* async; a PLANES world takes the call's steps in one resident launch (a world
+ * fitting shared memory, n_steps >= 4 and at least one step per 120 000 cells,
+ * up to 1.5 M cells) or one launch per step over the whole GPU, and keeps its
+ * change flags from call to call */
 fs3d_status fs3d_world_step(fs3d_world* w, int n_steps);
 /* Bounded wait (timeout_ns < 0: without limit).  FS3D_ERR_TIMEOUT also when a
  * step launch of the world met a bulk copy that did not complete within its
