@@ -5,6 +5,7 @@ fixtures to take them from); they pin the oracle, the generators and the rule
 against silent change and across hosts (x86_64 here, aarch64 on the GPU host).
 Run from the repository root: python tests/golden/make_golden.py
 """
+import hashlib
 import json
 import os
 import sys
@@ -15,6 +16,28 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 import oracle_lib  # noqa: E402
 import rule_py  # noqa: E402
+
+
+def dda_camera():
+    """A fixed camera looking into a 64^3 world from outside (oracle_lib.Camera)."""
+    c = oracle_lib.Camera()
+    vals = {"origin": (-20.5, 70.25, -30.0), "forward": (0.48, -0.6, 0.64), "right": (0.8, 0.0, -0.6),
+            "up": (0.36, 0.8, 0.48)}
+    for k, v in vals.items():
+        for a in range(3):
+            getattr(c, k)[a] = v[a]
+    c.tan_half_fov, c.aspect = 0.7, 64 / 48
+    c.light_pos[0], c.light_pos[1], c.light_pos[2] = 30.0, 90.0, 20.0
+    return c
+
+
+def dda_digest(orc) -> str:
+    """SHA-256 of the float32 RGBA image of the voxel DDA on the 64^3 dunes
+    world after 30 oracle steps."""
+    g = orc.gen_c5(1, 64, 64, 64)
+    orc.run(g, 1, 0, 30, nthreads=0)
+    img = orc.render_dda(g, dda_camera(), 64, 48)
+    return hashlib.sha256(np.ascontiguousarray(img, dtype=np.float32).tobytes()).hexdigest()
 
 
 def main():
@@ -33,6 +56,7 @@ def main():
     for w in range(4):
         X, Y, Z = (int(v) for v in dims[w])
         gen["batch_world_%d" % w] = str(orc.hash(orc.gen_c3_world(int(seeds[w]), X, Y, Z)))
+    out["renders"] = {"dda_dunes64_s1_t30_64x48": dda_digest(orc)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)
         f.write("\n")

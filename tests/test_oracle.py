@@ -196,6 +196,11 @@ def test_golden_vectors(orc):
     for w in range(4):
         X, Y, Z = (int(v) for v in dims[w])
         assert orc.hash(orc.gen_c3_world(int(seeds[w]), X, Y, Z)) == int(gen["batch_world_%d" % w])
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(GOLDEN), "make_golden.py"))
+    make_golden = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(make_golden)
+    assert make_golden.dda_digest(orc) == gold["renders"]["dda_dunes64_s1_t30_64x48"]
 
 
 # ---- raymarch_sphere material (rasterised mesh + box SDF march)
