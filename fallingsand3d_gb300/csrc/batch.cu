@@ -205,6 +205,8 @@ struct fs3d_batch {
     void* graph_worlds = nullptr;  // table pointers baked into the graphs
     void* graph_items = nullptr;
     void* graph_order = nullptr;
+    // classes with worlds in the current tables (bit c), and those the graphs launch
+    uint32_t class_mask = ~0u, graph_mask = 0;
     int grid = 0;
     int promote = 0;  // single-CTA resident worlds run this many classes wider (autotuned)
     unsigned long long* hash_dev = nullptr;
@@ -488,6 +490,15 @@ fs3d_status finalize_admits(fs3d_batch* b, uint64_t upto, bool wait) {
 // fit in shared memory take all their steps in one launch) and
 // steps_per_segment launches of the per-step kernel (the larger worlds).
 // With `fork` each goes to its own branch stream so they run concurrently.
+// resident-kernel launches of one segment under a mode (enqueue_segment's),
+// of the classes in `mask`
+int resident_launches(int mode, uint32_t mask) {
+    uint32_t launched = 0;
+    if (mode == 1 || mode == 3) launched |= (1u << kResidentClasses) - 1u;
+    if (mode == 2 || mode == 3) launched |= ((1u << kGmClasses) - 1u) << kResidentClasses;
+    return __builtin_popcount(launched & mask);
+}
+
 fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_steps) {
     if (fork) {
         FS3D_CUDA(cudaEventRecord(b->fork, a));
@@ -502,7 +513,11 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
     // In a graph the branches' kernels are all pending at once and the launch
     // order alone does not decide which grid is placed first: the dense class
     // carries the greatest priority.
+    // Classes without a world in the tables are not launched (the graph is
+    // captured again when that set changes).
+    auto has = [&](int cls) { return (b->class_mask >> cls) & 1u; };
     auto gm = [&](int c) {
+        if (!has(kResidentClasses + c)) return FS3D_OK;
         return launch_plane_segment_gm(c, b->tw.d, b->to.d, b->tn.d, b->counter + kResidentClasses + c, b->err,
                                        fork ? b->branch[kResidentClasses + c] : a, b->processed_dev,
                                        mode == 3 && c == kGmDense);
@@ -510,8 +525,9 @@ fs3d_status enqueue_segment(fs3d_batch* b, cudaStream_t a, bool fork, bool with_
     if (mode == 3) s = gm(kGmDense);
     if (mode == 1 || mode == 3)
         for (int c = kResidentClasses - 1; c >= 0 && s == FS3D_OK; --c)
-            s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
-                                              fork ? b->branch[c] : a, b->processed_dev);
+            if (has(c))
+                s = launch_plane_segment_resident(c, b->tw.d, b->to.d, b->tn.d, b->counter + c, b->err,
+                                                  fork ? b->branch[c] : a, b->processed_dev);
     if (mode == 2 || mode == 3)
         for (int c = 0; c < kGmClasses && s == FS3D_OK; ++c)
             if (c != kGmDense || mode == 2) s = gm(c);
@@ -555,6 +571,7 @@ fs3d_status capture_graph(fs3d_batch* b) {
     b->graph_worlds = b->tw.d;
     b->graph_items = b->ti.d;
     b->graph_order = b->to.d;
+    b->graph_mask = b->class_mask;
     return FS3D_OK;
 }
 
@@ -814,6 +831,10 @@ fs3d_status build_tables(fs3d_batch* b) {
         meta[1 + kAllClasses + c] = (int)si;
         for (int x : v) b->to.h[si++] = x;
     }
+    uint32_t mask = 0;
+    for (int c = 0; c < kAllClasses; ++c)
+        if (!by_class[c].empty()) mask |= 1u << c;
+    b->class_mask = mask;
     // admissions complete before the segment reads their planes
     for (auto& ev : b->pending_ready) FS3D_CUDA(cudaStreamWaitEvent(b->stream, ev.get(), 0));
     b->pending_ready.clear();
@@ -830,8 +851,8 @@ fs3d_status build_tables(fs3d_batch* b) {
     if (si) FS3D_CUDA(b->to.upload(si, b->stream));
     FS3D_CUDA(b->tn.upload(kMetaInts, b->stream));
     FS3D_CUDA(cudaEventRecord(b->tables_free[b->tab_cur], b->stream));
-    if (b->cfg.use_graphs &&
-        (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d || b->graph_order != b->to.d)) {
+    if (b->cfg.use_graphs && (!b->graph || b->graph_worlds != b->tw.d || b->graph_items != b->ti.d ||
+                              b->graph_order != b->to.d || b->graph_mask != b->class_mask)) {
         s = capture_graph(b);
         if (s != FS3D_OK) {
             b->running.clear();
@@ -877,9 +898,7 @@ fs3d_status fs3d_batch_run_segment(fs3d_batch* b) {
     const size_t ii = b->table_items;
     if (b->cfg.use_graphs) {
         FS3D_CUDA(cudaGraphLaunch(ii ? b->graph_steps : b->graph, b->stream));
-        note_launch((ii ? (uint64_t)S : 0u) +
-                    (b->cfg.use_smem == 1 || b->cfg.use_smem == 3 ? kResidentClasses : 0) +
-                    (b->cfg.use_smem == 2 || b->cfg.use_smem == 3 ? kGmClasses : 0) + 1u);
+        note_launch((ii ? (uint64_t)S : 0u) + (uint64_t)resident_launches(b->cfg.use_smem, b->graph_mask) + 1u);
     } else {
         const fs3d_status s = enqueue_segment(b, b->stream, false, ii > 0);
         if (s != FS3D_OK) return s;
