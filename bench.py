@@ -2,17 +2,23 @@
 
 Headline workload (one "step" = one 64-step segment of the batched pool):
 2048 independent worlds, dims iid from {16,24,32,48,64,96,128}^3 (seeded),
-stepped together by the bit-plane step kernel inside one CUDA graph per
+stepped together by the resident segment kernels (each world takes all of a
+segment's steps in one launch of its size class) inside one CUDA graph per
 segment.  The same line carries:
+  * value_fresh: the same worlds generated anew, one segment from step 0;
   * plain_per_world: the drop-in byte kernel launched once per world per step
     (2048 x 64 launches per segment) on the same worlds;
   * plain_512: the drop-in byte kernel on one 512^3 pillar world (HBM-bound);
-  * roofline of the dominant kernel (CUDA-event time per launch);
+  * roofline of the dominant kernel (CUDA-event time per launch), with the
+    issue-rate roof beside it;
   * cpu_baseline: the CPU oracle timed on this host (bounded sample);
   * parity: results of the timed GPU runs, read back and checked against the
     oracle in the CPU leg once every GPU measurement has ended;
-  * e2e: the same metric through the C ABI from pinned host buffers
-    (admit = H2D + conversion, one segment, retire = conversion + D2H).
+  * e2e / e2e_fresh: the same metric through the C ABI from pinned host
+    buffers (admit = H2D + conversion, one segment, retire = conversion + D2H);
+  * served, large_render, mesh_render, engine_loop: the serving loop, the
+    1024^3 world with a frame per step, the mesh materials, and one step per
+    call of a 64^3 world.
 `--impl reference` times the CPU oracle (the upstream project has no step of
 its own) on a bounded sample of the same workload with all host threads.
 
