@@ -1056,7 +1056,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
-    ap.add_argument("--e2e-steps", type=int, default=20, help="timed steps of the e2e leg")
+    ap.add_argument("--e2e-steps", type=int, default=60, help="timed steps of the e2e leg (each of its three timed runs)")
     ap.add_argument("--e2e-batches", type=int, default=1, help="batches taking the e2e steps in turn (1 or 2)")
     ap.add_argument("--impl", default="fs3d", choices=["fs3d", "reference"])
     ap.add_argument("--worlds", type=int, default=2048)
