@@ -380,22 +380,25 @@ def run_fs3d(args):
     # ---- headline: batched pool, device-resident
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
-    # untimed: warm-up segments (at least five, so the worlds are past their
+    # untimed: warm-up segments (at least four, so the worlds are past their
     # first steps, the phase where everything still falls), the launch
     # configuration chosen on real segments, then plain segments up to step
     # --timed-from, where the timed segments start (the reference arm steps
     # the same states)
-    pre = max(args.warmup, 5)
+    pre = max(args.warmup, 4)  # segments before tuning (the worlds are past their young steps by then)
     untimed = args.timed_from // S
     total_steps = S * (untimed + args.steps + 1 + 32)
     tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
     bstream = torch.cuda.ExternalStream(b.stream())
     for _ in range(pre):
         b.run_segment()
-    tune = b.autotune(trial_segments=1) if not args.no_autotune else {"segments": 0}
+    # two timed segments per candidate (the fastest counts): one alone let the
+    # segment-to-segment spread pick the slower promotion now and then
+    tune = b.autotune(trial_segments=2) if not args.no_autotune else {"segments": 0}
     done_untimed = pre + tune["segments"]
-    if done_untimed > untimed:
-        raise SystemExit(f"warm-up and tuning took {done_untimed} segments, more than --timed-from allows")
+    # a longer warm-up than --timed-from allows moves the timed segments later
+    # (the config line records where they start)
+    untimed = max(untimed, done_untimed)
     for _ in range(untimed - done_untimed):
         b.run_segment()
     b.sync()
@@ -759,12 +762,12 @@ def run_fs3d(args):
                 "vs_baseline": None, "dtype": "u8", "data": "synthetic",
                 "config": {"workload": f"batched: {args.worlds} worlds, dims iid from {{16,24,32,48,64,96,128}}^3, "
                                        f"{S}-step CUDA-graph segments (one step = one segment), timed from step "
-                                       f"{args.timed_from}",
+                                       f"{S * untimed}",
                            "worlds_per_gpu": args.worlds, "cells_per_gpu": cells, "steps_per_segment": S,
                            "master_seed": args.master, "l2": "flushed between timed segments (512 MB write)",
                            "layout": "2-bit planes", "parallelism": f"replicas x{world}",
                            "launch_config": {k: tune.get(k) for k in ("mode", "promote", "ctas_per_sm", "trials")},
-                           "timed_from_step": args.timed_from, "untimed_segments": untimed},
+                           "timed_from_step": S * untimed, "untimed_segments": untimed},
                 "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms": round(e2e_ms, 2), "steps": args.e2e_steps, "ms_runs": e2e_runs,
@@ -1027,7 +1030,7 @@ def run_only(args):
                 b.run_segment()
             tune = {"segments": 0}
             if not args.no_autotune:
-                tune = b.autotune(trial_segments=1)  # as the headline run does before its timed segments
+                tune = b.autotune(trial_segments=2)  # as the headline run does before its timed segments
             for _ in range(args.steps):
                 b.run_segment()
             b.sync()
