@@ -299,6 +299,25 @@ class OracleChecks:
         return out
 
 
+# untimed segments of the headline run that precede its timed ones: the
+# autotuner's six (two candidate promotions, each one untimed segment and two
+# timed ones; every world of the batch fits a resident class, so the per-step
+# grid is not a candidate) follow the warm-up, and one plain segment follows
+# them (the tuner leaves the chosen configuration freshly captured: its first
+# segment rebuilds the tables and uploads the graph)
+TUNE_SEGMENTS = 6
+
+
+def untimed_segments(args) -> int:
+    """Segments stepped before the timed ones, the same in both arms: at least
+    --timed-from / --segment, more when the warm-up (at least three segments,
+    so the worlds are past their young steps before tuning) and the tuner
+    need them."""
+    pre = max(args.warmup, 3)
+    tune = 0 if args.no_autotune else TUNE_SEGMENTS
+    return max(args.timed_from // args.segment, pre + tune + 1)
+
+
 def run_reference(args):
     """The reference arm: the upstream project has no step of its own, so the
     CPU oracle (FS3D-rule v1) stands in, on the batch's worlds made by the
@@ -310,6 +329,7 @@ def run_reference(args):
         return 0
     orc = load_oracle()
     threads = os.cpu_count() or 1
+    start = args.segment * untimed_segments(args)  # where the GPU arm's timed segments begin
     worlds = oracle_worlds(orc, args.master, args.worlds)
     sample = [worlds[i] for i in oracle_sample_index(args.worlds)]
 
@@ -323,8 +343,8 @@ def run_reference(args):
     def advance(st):
         g, seed, _ = st
         Y, Z, X = g.shape
-        orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, 0, args.timed_from, None, 1)
-        st[2] = args.timed_from
+        orc.L.orc_run(g.ctypes.data, X, Y, Z, seed, 0, start, None, 1)
+        st[2] = start
 
     t0 = time.perf_counter()
     run_parallel(advance, sorted(settled, key=lambda st: -st[0].size), threads)
@@ -338,14 +358,14 @@ def run_reference(args):
     v = float(np.mean(vals))
     vf, info_f = oracle_rate(orc, fresh, args.cpu_budget / 2, threads, window=args.segment)
     sample_txt = (f"{len(sample)} of the {args.worlds} worlds (every 16th), advanced untimed to step "
-                  f"{args.timed_from} ({advance_s:.1f} s), then their next {args.segment} steps, over and over, "
+                  f"{start} ({advance_s:.1f} s), then their next {args.segment} steps, over and over, "
                   f"in 4-step takes for {args.cpu_budget:g} s over {args.steps} timed steps; {ORACLE_FLAGS}")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
             "config": {"workload": f"batched: {args.worlds} mixed worlds (bounded CPU sample), the states from "
-                                   f"step {args.timed_from} on, as the GPU arm's timed segments",
-                       "master_seed": args.master, "timed_from_step": args.timed_from},
+                                   f"step {start} on, as the GPU arm's timed segments",
+                       "master_seed": args.master, "timed_from_step": start},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_txt},
             "value_fresh": {"value": vf, "unit": UNIT,
                             "states": f"the same worlds freshly generated, their first {args.segment} steps",
@@ -380,13 +400,12 @@ def run_fs3d(args):
     # ---- headline: batched pool, device-resident
     host = gen_grids(fs3d, worlds, pinned_torch=torch)
     b = fs3d.Batch(150 << 30, steps_per_segment=S)
-    # untimed: warm-up segments (at least four, so the worlds are past their
-    # first steps, the phase where everything still falls), the launch
-    # configuration chosen on real segments, then plain segments up to step
-    # --timed-from, where the timed segments start (the reference arm steps
-    # the same states)
-    pre = max(args.warmup, 4)  # segments before tuning (the worlds are past their young steps by then)
-    untimed = args.timed_from // S
+    # untimed: warm-up segments (the worlds leave their first steps, the phase
+    # where everything still falls), the launch configuration chosen on real
+    # segments, then plain segments up to where the timed segments start (the
+    # reference arm steps the same states)
+    pre = max(args.warmup, 3)
+    untimed = untimed_segments(args)
     total_steps = S * (untimed + args.steps + 1 + 32)
     tickets = [b.admit(g.numpy(), seed, total_steps) for g, (_, seed) in zip(host, worlds)]
     bstream = torch.cuda.ExternalStream(b.stream())
@@ -396,9 +415,9 @@ def run_fs3d(args):
     # segment-to-segment spread pick the slower promotion now and then
     tune = b.autotune(trial_segments=2) if not args.no_autotune else {"segments": 0}
     done_untimed = pre + tune["segments"]
-    # a longer warm-up than --timed-from allows moves the timed segments later
-    # (the config line records where they start)
-    untimed = max(untimed, done_untimed)
+    if tune["segments"] not in (0, TUNE_SEGMENTS):
+        raise RuntimeError(f"the autotuner ran {tune['segments']} segments, not {TUNE_SEGMENTS}: "
+                           "the reference arm would step other states")
     for _ in range(untimed - done_untimed):
         b.run_segment()
     b.sync()
