@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <deque>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -112,7 +113,14 @@ fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_req
             fs3d_serve_request& q = reqs[queue.front()];
             uint64_t ticket = 0;
             const fs3d_status a = fs3d_batch_admit_generated(b, q.X, q.Y, q.Z, q.seed, 0, q.n_steps, &ticket);
-            if (a == FS3D_ERR_BUDGET) break;
+            if (a == FS3D_ERR_BUDGET) {
+                // with no world live the batch holds no memory: this request
+                // needs more than the whole budget and would wait forever
+                if (live.empty())
+                    s = set_error(FS3D_ERR_BUDGET, "fs3d_serve_run: request " + std::to_string(queue.front()) +
+                                                       " needs more memory than the whole budget");
+                break;
+            }
             if (a != FS3D_OK) {
                 s = a;
                 break;

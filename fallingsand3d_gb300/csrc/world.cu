@@ -207,16 +207,17 @@ fs3d_status fs3d_world_step(fs3d_world* w, int n_steps) {
                 w->flags_ok = s == FS3D_OK;
             }
             int* counts = w->counts_valid ? w->brick_counts : nullptr;
-            for (int a = 0; a < n_steps && s == FS3D_OK; ++a) {
-                d.t = w->step + (uint64_t)a;
+            int launched = 0;
+            while (s == FS3D_OK && launched < n_steps) {
+                d.t = w->step + (uint64_t)launched;
                 s = launch_plane_step_skip(d, w->rflags, counts, w->stream);
+                if (s == FS3D_OK) ++launched;
             }
-            if (s == FS3D_OK) {
-                w->flags_t = w->step + (uint64_t)n_steps;
-                w->step += (uint64_t)n_steps;
-            } else {
+            w->step += (uint64_t)launched;  // the steps that went out before a failed launch still count
+            if (s == FS3D_OK)
+                w->flags_t = w->step;
+            else
                 w->flags_ok = false;
-            }
             return s;
         }
         // the world fits in shared memory (one CTA or a cluster): all n steps

@@ -314,7 +314,10 @@ typedef struct fs3d_serve_stats {
 fs3d_status fs3d_serve_plan(const fs3d_serve_params* p, int64_t capacity, fs3d_serve_request* reqs,
                             int64_t* n_reqs);
 /* Serves the n planned requests in real time; fills their admitted/finished
- * times and hashes and the summary statistics. */
+ * times and hashes and the summary statistics.  A request waits for memory
+ * while other worlds are live; FS3D_ERR_BUDGET if one needs more than the
+ * whole budget (nothing live and still no room); FS3D_ERR_TIMEOUT if a
+ * segment does not end within segment_timeout_ms (default 10 s). */
 fs3d_status fs3d_serve_run(const fs3d_serve_params* p, int64_t n, fs3d_serve_request* reqs,
                            fs3d_serve_stats* stats);
 

@@ -59,6 +59,21 @@ def test_tight_budget_defers_but_stays_exact(fs3d, orc):
         assert r.hash == alone_hash(fs3d, r)
 
 
+def test_request_larger_than_the_whole_budget_is_an_error(fs3d):
+    """A request that cannot fit even with nothing else live ends the run with
+    FS3D_ERR_BUDGET instead of waiting for memory that never frees."""
+    budget = 48 << 10  # a 16^3 or 48^3 world fits, a 64 x 64 cross-section does not
+    p = fs3d.serve_params(2000.0, 0.05, master_seed=6, min_steps=10, max_steps=40, hbm_budget=budget)
+    reqs, n = fs3d.serve_plan(p)
+    planes = [r.Y * r.Z * ((r.X + 63) // 64) * 16 for r in reqs[:n]]
+    assert max(planes) > budget and min(planes) < budget
+    with pytest.raises(fs3d.Fs3dError) as e:
+        fs3d.serve(p)
+    assert e.value.status == fs3d.ERR_BUDGET
+    stats, done = fs3d.serve(fs3d.serve_params(2000.0, 0.05, master_seed=6, min_steps=10, max_steps=40))
+    assert stats["completed"] == len(done) == n
+
+
 def test_serving_reports_a_device_wait_that_gave_up(fs3d):
     """Young requests run in the shared-memory step kernels; with every bulk
     copy wait made to run out (test hook), the first segment's wait reports
