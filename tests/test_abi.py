@@ -75,6 +75,39 @@ def test_bad_arguments_return_status(fs3d):
     assert L.fs3d_world_load(b"/nonexistent/ckp", 0, C.byref(h)) == fs3d.ERR_IO
 
 
+# every entry point that takes a handle or a required pointer, with it NULL:
+# refused on the host with FS3D_ERR_INVALID_ARG (no CUDA call, no crash)
+NULL_CALLS = {
+    "fs3d_world_step": (None, 1), "fs3d_world_sync": (None, 0), "fs3d_world_read": (None, None),
+    "fs3d_world_write": (None, None), "fs3d_world_hash": (None, None), "fs3d_world_device_ptr": (None, None, None),
+    "fs3d_world_stream": (None, None), "fs3d_world_destroy": (None,), "fs3d_world_save": (None, b"ckp"),
+    "fs3d_world_info": (None, None, None, None, None, None, None),
+    "fs3d_world_create": (None, 2, 2, 2, 0, 0, 0, None), "fs3d_world_load": (None, 0, None),
+    "fs3d_batch_create": (0, None, None),
+    "fs3d_batch_admit": (None, None, 1, 1, 1, 0, 0, 1, None),
+    "fs3d_batch_admit_generated": (None, 16, 16, 16, 0, 0, 1, None),
+    "fs3d_batch_admit_many": (None, 1, None, None, None), "fs3d_batch_admit_many_async": (None, 1, None, None, None),
+    "fs3d_batch_run_segment": (None,), "fs3d_batch_prepare": (None,), "fs3d_batch_sync": (None, 0),
+    "fs3d_batch_poll": (None, 1, None, None), "fs3d_batch_poll_many": (None, 1, None, None, None),
+    "fs3d_batch_retire": (None, 1, None), "fs3d_batch_retire_many": (None, 1, None, None),
+    "fs3d_batch_retire_many_async": (None, 1, None, None), "fs3d_batch_read_many": (None, 1, None, None),
+    "fs3d_batch_wait_copies": (None, 0), "fs3d_batch_autotune": (None, 1, None),
+    "fs3d_batch_counters": (None, None, None), "fs3d_batch_stream": (None, None), "fs3d_batch_destroy": (None,),
+    "fs3d_batch_stats": (None, None, None, None, None),
+    "fs3d_step_device": (None, 2, 2, 2, 0, 0, 1, None), "fs3d_step_device_many": (1, None, None, None, 0, 1, None),
+    "fs3d_run_device": (None, 2, 2, 2, 0, 0, 1, None), "fs3d_run_device_noalloc": (None, 2, 2, 2, 0, 0, 1, None),
+    "fs3d_serve_plan": (None, 0, None, None), "fs3d_serve_run": (None, 0, None, None),
+    "fs3d_render": (None, None, 16, 16, 0, None, 0), "fs3d_render_sdf": (None, 16, 16, None, None),
+}
+
+
+@pytest.mark.parametrize("name", sorted(NULL_CALLS))
+def test_null_handles_and_pointers_are_refused(fs3d, name):
+    L = fs3d.lib()
+    assert getattr(L, name)(*NULL_CALLS[name]) == fs3d.ERR_INVALID_ARG
+    assert L.fs3d_last_error() != b""
+
+
 def test_object_render_rejects_before_launch(fs3d):
     """Views the restatement does not cover are refused on the host, with no
     device work: an eye inside the cube (a vertex behind the camera), a
