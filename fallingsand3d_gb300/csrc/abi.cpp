@@ -22,6 +22,10 @@ fs3d_status set_error(fs3d_status s, const std::string& msg) {
 
 fs3d_status cuda_fail(cudaError_t e, const char* what) {
     g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    // the error is reported here: taken off the runtime's per-thread slot, so
+    // that a later launch check of this thread does not report it again (an
+    // error that leaves the context unusable keeps coming back regardless)
+    cudaGetLastError();
     if (e == cudaErrorMemoryAllocation) return FS3D_ERR_OOM;
     return FS3D_ERR_CUDA;
 }

@@ -125,10 +125,9 @@ extern "C" fs3d_status fs3d_run_device(uint8_t* grid_dev, int X, int Y, int Z, u
     }
     // a recorded failure (this run's or an earlier one's) leaves the grid as it was
     if (s == FS3D_OK) s = planes_to_bytes(sc.rows, grid_dev, X, Y, Z, grid_dev, st, err);
-    cudaFreeAsync(sc.rows, st);
-    cudaFreeAsync(sc.desc, st);
-    cudaFreeAsync(sc.ints, st);
-    if (rflags) cudaFreeAsync(rflags, st);
+    // only what was allocated (the allocations stop at the first failure)
+    for (void* p : {(void*)sc.rows, (void*)sc.desc, (void*)sc.ints, (void*)rflags})
+        if (p) cudaFreeAsync(p, st);
     return s;
 }
 
