@@ -29,6 +29,41 @@ def test_library_exports_every_declared_symbol(fs3d):
     assert L.fs3d_status_string(-3) == b"over the memory budget"
 
 
+def test_struct_layouts_match_header(fs3d, tmp_path):
+    """Every struct of the binding has the header's size and field offsets:
+    a C program compiled against include/fs3d.h prints them (gcc, no GPU)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    structs = {"fs3d_camera": fs3d.Camera, "fs3d_config": fs3d.Config, "fs3d_world_spec": fs3d.WorldSpec,
+               "fs3d_tune_report": fs3d.TuneReport, "fs3d_serve_params": fs3d.ServeParams,
+               "fs3d_serve_request": fs3d.ServeRequest, "fs3d_serve_stats": fs3d.ServeStats,
+               "fs3d_object_view": fs3d.ObjectView, "fs3d_mesh_draw": fs3d.MeshDraw}
+    cname = lambda f: "lambda" if f == "lambda_" else f  # a Python keyword renamed in the binding
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "fs3d.h"', "int main(void) {"]
+    for s, cls in structs.items():
+        lines.append(f'    printf("{s} size %zu\\n", sizeof({s}));')
+        for f, _ in cls._fields_:
+            lines.append(f'    printf("{s} {f} %zu\\n", offsetof({s}, {cname(f)}));')
+    lines += ["    return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        s, f, v = ln.split()
+        got[(s, f)] = int(v)
+    for s, cls in structs.items():
+        assert got[(s, "size")] == C.sizeof(cls), s
+        for f, _ in cls._fields_:
+            assert got[(s, f)] == getattr(cls, f).offset, (s, f)
+    # the numpy view used to build many world specs at once
+    for f in fs3d._SPEC_DTYPE.names:
+        assert fs3d._SPEC_DTYPE.fields[f][1] == got[("fs3d_world_spec", f)], f
+    assert fs3d._SPEC_DTYPE.itemsize == got[("fs3d_world_spec", "size")]
+
+
 def test_default_config(fs3d):
     c = fs3d.lib().fs3d_default_config()
     assert c.steps_per_segment == 64 and c.use_graphs == 1
