@@ -64,6 +64,30 @@ def test_struct_layouts_match_header(fs3d, tmp_path):
     assert fs3d._SPEC_DTYPE.itemsize == got[("fs3d_world_spec", "size")]
 
 
+def test_integration_binding_compiles_against_the_header(tmp_path):
+    """The C++ binding INTEGRATION.md shows a maintainer adding to the engine
+    type-checks against include/fs3d.h (g++ -fsyntax-only, the engine's own
+    names stubbed)."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("g++ not found")
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```cpp\n(.*?)```", txt, flags=re.S)
+    assert len(blocks) == 1
+    body = "\n".join(ln for ln in blocks[0].splitlines() if not ln.startswith("#include"))
+    src = tmp_path / "binding.cpp"
+    src.write_text('#include <cstdint>\n#include <vector>\n#include "fs3d.h"\n'
+                   "namespace util { inline void displayError(const char*) {} }\n"
+                   "struct Vec3 { float x, y, z; };\n"
+                   "static Vec3 camPos, camRot;\n"
+                   "static float *frameDevPtr, *objectFrameDevPtr;\n"
+                   "void engine_hooks() {\n" + body + "\n}\n")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wno-unused-variable",
+                        "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_default_config(fs3d):
     c = fs3d.lib().fs3d_default_config()
     assert c.steps_per_segment == 64 and c.use_graphs == 1
