@@ -64,6 +64,68 @@ def test_struct_layouts_match_header(fs3d, tmp_path):
     assert fs3d._SPEC_DTYPE.itemsize == got[("fs3d_world_spec", "size")]
 
 
+def header_declarations():
+    """(return type, name, [parameter declarations]) of every function in include/fs3d.h."""
+    txt = open(os.path.join(ROOT, "include", "fs3d.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"^\s*#.*$", "", txt, flags=re.M)
+    out = []
+    for ret, name, params in re.findall(r"([A-Za-z_][\w \t\*]*?)\b(fs3d_\w+)\s*\(([^;{()]*)\)\s*;", txt):
+        ps = [p.strip() for p in " ".join(params.split()).split(",")]
+        out.append((" ".join(ret.split()), name, [] if ps == ["void"] else ps))
+    return out
+
+
+def test_binding_signatures_match_header(fs3d, tmp_path):
+    """Each function's ctypes signature agrees with its C prototype: the
+    parameter count, pointer or value for each parameter, the value widths
+    (sizes from a gcc-compiled probe), the struct a pointer points to, and
+    the return type."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    structs = {"fs3d_camera": fs3d.Camera, "fs3d_config": fs3d.Config, "fs3d_world_spec": fs3d.WorldSpec,
+               "fs3d_tune_report": fs3d.TuneReport, "fs3d_serve_params": fs3d.ServeParams,
+               "fs3d_serve_request": fs3d.ServeRequest, "fs3d_serve_stats": fs3d.ServeStats,
+               "fs3d_object_view": fs3d.ObjectView, "fs3d_mesh_draw": fs3d.MeshDraw}
+    decls = header_declarations()
+    assert sorted(n for _, n, _ in decls) == declared_functions()
+
+    def split(p):  # "const uint8_t* grid" -> ("const uint8_t*", pointer?)
+        if "*" in p:
+            return p[:p.rindex("*") + 1], True
+        toks = p.split()
+        return " ".join(toks[:-1]), False
+
+    value_types = sorted({split(p)[0] for _, _, ps in decls for p in ps if not split(p)[1]})
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "fs3d.h"\nint main(void) {\n' +
+                   "".join(f'    printf("{t}=%zu\\n", sizeof({t}));\n' for t in value_types) + "    return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    size = dict(ln.split("=") for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.split())
+    pointer_types = (C.c_void_p, C.c_char_p)
+    rets = {"fs3d_status": C.c_int, "int": C.c_int, "const char*": C.c_char_p, "uint64_t": C.c_uint64,
+            "fs3d_config": fs3d.Config, "void": None}
+    L = fs3d.lib()
+    for ret, name, params in decls:
+        fn = getattr(L, name)
+        assert fn.restype is rets[ret], (name, ret)
+        assert len(fn.argtypes) == len(params), name
+        for p, at in zip(params, fn.argtypes):
+            ctype, is_ptr = split(p)
+            if is_ptr:
+                assert at in pointer_types or issubclass(at, C._Pointer), (name, p, at)
+                base = ctype.replace("const", "").replace("*", "").strip()
+                if base in structs and ctype.count("*") == 1:
+                    assert at is C.c_void_p or at._type_ is structs[base], (name, p, at)
+            else:
+                assert at not in pointer_types and not issubclass(at, C._Pointer), (name, p, at)
+                assert C.sizeof(at) == int(size[ctype]), (name, p, at)
+
+
 def test_integration_binding_compiles_against_the_header(tmp_path):
     """The C++ binding INTEGRATION.md shows a maintainer adding to the engine
     type-checks against include/fs3d.h (g++ -fsyntax-only, the engine's own
