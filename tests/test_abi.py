@@ -127,9 +127,9 @@ def test_binding_signatures_match_header(fs3d, tmp_path):
 
 
 def test_integration_binding_compiles_against_the_header(tmp_path):
-    """The C++ binding INTEGRATION.md shows a maintainer adding to the engine
-    type-checks against include/fs3d.h (g++ -fsyntax-only, the engine's own
-    names stubbed)."""
+    """The C++ binding that the integration guide shows a maintainer adding
+    to the engine type-checks against include/fs3d.h (g++ -fsyntax-only, the
+    engine's own names stubbed)."""
     import shutil
     import subprocess
     if not shutil.which("g++"):
