@@ -1,5 +1,6 @@
-"""CPU checks of the C ABI: the library loads, exports every entry point that
-include/fs3d.h declares, its host-side generators match the oracle's and bad
+"""CPU checks of the C ABI: the library loads and exports every entry point
+that include/fs3d.h declares, the ctypes binding's signatures and structs
+match the header, its host-side generators match the oracle's, and bad
 arguments come back as status codes (no GPU work is issued here)."""
 import ctypes as C
 import os
