@@ -195,9 +195,11 @@ _oracle = None
 
 
 def load() -> Oracle:
+    """The oracle; FS3D_ORACLE_SO names another build of the same source (the
+    tests run it once more built at -O0 with the undefined-behaviour checks)."""
     global _oracle
     if _oracle is None:
-        _oracle = Oracle(build())
+        _oracle = Oracle(os.environ.get("FS3D_ORACLE_SO") or build())
     return _oracle
 
 
