@@ -1,7 +1,8 @@
 """The library's host-only code (the seeded generators, the request planner,
 the status and error plumbing) built once more at -O0 with gcc's
-undefined-behaviour checks (every report aborts), and run on odd and full
-sizes: its outputs must equal the shipped library's byte for byte.  The batch
+undefined-behaviour checks and, where its runtime is installed, its address
+checks (every report aborts), and run on odd and full sizes: its outputs must
+equal the shipped library's byte for byte.  The batch
 entry points the server calls are stubbed (the planner never reaches them);
 nothing here touches a GPU."""
 import ctypes as C
@@ -12,6 +13,8 @@ import sys
 
 import numpy as np
 import pytest
+
+from sanitize_util import report_found, sanitize_flags
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "fallingsand3d_gb300", "csrc")
@@ -72,20 +75,20 @@ print("ok")
 """
 
 
-def test_host_code_under_ubsan_at_O0(fs3d, tmp_path):
+def test_host_code_under_sanitizers_at_O0(fs3d, tmp_path):
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
     if not shutil.which("g++") or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
         pytest.skip("g++ or the CUDA headers not found")
     stub = tmp_path / "stubs.cpp"
     stub.write_text(STUBS)
-    so = tmp_path / "libhost_ubsan.so"
-    r = subprocess.run(["g++", "-O0", "-std=c++17", "-fPIC", "-fsanitize=undefined", "-fno-sanitize-recover=undefined",
-                        "-I", cuda_inc, "-I", CSRC, "-shared", "-o", str(so),
+    flags, env_add, _ = sanitize_flags()
+    so = tmp_path / "libhost_checked.so"
+    r = subprocess.run(["g++", "-O0", "-std=c++17", "-fPIC", *flags, "-I", cuda_inc, "-I", CSRC, "-shared", "-o", str(so),
                         *(os.path.join(CSRC, f) for f in ("gen.cpp", "abi.cpp", "serve.cpp")), str(stub),
                         "-L", cuda_lib, "-lcudart"], capture_output=True, text=True)
-    if r.returncode != 0 and "ubsan" in r.stderr:
-        pytest.skip("gcc's undefined-behaviour runtime is not installed")
+    if r.returncode != 0 and "san" in r.stderr:
+        pytest.skip("gcc's sanitizer runtime is not installed")
     assert r.returncode == 0, r.stderr
     # the shipped library's outputs
     L = fs3d.lib()
@@ -105,6 +108,6 @@ def test_host_code_under_ubsan_at_O0(fs3d, tmp_path):
     npz = tmp_path / "expected.npz"
     np.savez(npz, **data)
     t = subprocess.run([sys.executable, "-c", CHILD, str(so), str(npz)], capture_output=True, text=True,
-                       timeout=600)
+                       env=dict(os.environ, **env_add), timeout=600)
     out = t.stdout + t.stderr
-    assert t.returncode == 0 and "runtime error" not in out and "ok" in t.stdout, out[-3000:]
+    assert t.returncode == 0 and not report_found(out) and "ok" in t.stdout, out[-3000:]
