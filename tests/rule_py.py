@@ -54,6 +54,37 @@ def draw(n: int, rk: int, i: int, s: int) -> int:
     return 0 if u < 85 else (1 if u < 170 else 2)
 
 
+def block(val, rk: int, i: int) -> list:
+    """The rule on block i of its row-pair (row key rk): val[s] are the eight
+    slot values (slots 0-3 the top layer, 4-7 the bottom one, column q = s & 3;
+    a cell outside the grid holds 1).  Returns the new values."""
+    val = [int(v) for v in val]
+    empty = lambda s: val[s] == 0  # noqa: E731
+    moved = set()
+    for s in range(8):
+        m = val[s]
+        if m not in (2, 3) or s in moved:
+            continue
+        q = s & 3
+        dst = None
+        if s < 4:
+            if empty(4 + q):
+                dst = 4 + q
+            else:
+                cand = [4 + q2 for q2 in range(4) if q2 != q and empty(4 + q2)]
+                if cand:
+                    dst = cand[draw(len(cand), rk, i, s)]
+        if dst is None and m == 3:
+            base = s & 4
+            cand = [base + q2 for q2 in range(4) if q2 != q and empty(base + q2)]
+            if cand:
+                dst = cand[draw(len(cand), rk, i, s)]
+        if dst is not None:
+            val[dst], val[s] = m, 0
+            moved.add(dst)
+    return val
+
+
 def step(grid: np.ndarray, seed: int, t: int) -> None:
     """One step in place; grid shape (Y, Z, X)."""
     Y, Z, X = grid.shape
@@ -70,30 +101,7 @@ def step(grid: np.ndarray, seed: int, t: int) -> None:
                     x, y, z = 2 * i - o + (q & 1), 2 * j - o + (1 - layer), 2 * k - o + (q >> 1)
                     inside = 0 <= x < X and 0 <= y < Y and 0 <= z < Z
                     cells.append((y, z, x) if inside else None)
-                val = [int(grid[c]) if c else 1 for c in cells]
-                empty = lambda s: cells[s] is not None and val[s] == 0  # noqa: E731
-                moved = set()
-                for s in range(8):
-                    m = val[s]
-                    if m not in (2, 3) or s in moved:
-                        continue
-                    q = s & 3
-                    dst = None
-                    if s < 4:
-                        if empty(4 + q):
-                            dst = 4 + q
-                        else:
-                            cand = [4 + q2 for q2 in range(4) if q2 != q and empty(4 + q2)]
-                            if cand:
-                                dst = cand[draw(len(cand), rk, i, s)]
-                    if dst is None and m == 3:
-                        base = s & 4
-                        cand = [base + q2 for q2 in range(4) if q2 != q and empty(base + q2)]
-                        if cand:
-                            dst = cand[draw(len(cand), rk, i, s)]
-                    if dst is not None:
-                        val[dst], val[s] = m, 0
-                        moved.add(dst)
+                val = block([int(grid[c]) if c else 1 for c in cells], rk, i)
                 for s in range(8):
                     if cells[s]:
                         grid[cells[s]] = val[s]
